@@ -1,0 +1,158 @@
+// Internal declarations of libacdc_gpu.so (sm_103a).
+//
+// Device layout of one problem (the column operand: A for the Lasso, X^T for
+// the SVM dual; "column" = coordinate, "row" = residual entry):
+//   meta[n]   int4 {start4, len, Li, x}: start4 = column start / 4 in the
+//             padded arrays, len = nonzeros, Li = 1/(beta ||a_j||^2) (FP32
+//             bits; for the SVM the sign carries y_j), x = coordinate value
+//             (FP32 bits, updated in place with red.global.add.f32).
+//   vals[]    FP32 values, each column starting on a 16-byte boundary and
+//             zero-padded to a multiple of 4 entries (so one 128-bit load
+//             covers 4 entries and never crosses into the next column).
+//   idx[]     int32 row indices, same padding (pad index 0, pad value 0).
+//   r32[m]    FP32 working residual: Ax - b (Lasso) or w (SVM).
+//   r64[m]    FP64 residual of the last refresh.
+//   rhs64[]   FP64 b (m entries, Lasso) or y (n entries, SVM).
+//   col_sq[n] FP64 ||a_j||^2.
+//   active[n] q-shrinking active set (int32 coordinate list).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/acdc_gpu.h"
+#include "acdc_philox.h"
+
+#define ACDC_FULL_MASK 0xffffffffu
+
+// Slots of the per-problem counter block (unsigned long long).
+enum {
+  CNT_WORK = 0,        // per-launch work counter of the update kernel
+  CNT_UPDATES = 1,
+  CNT_NONZERO = 2,
+  CNT_NNZ_READ = 3,
+  CNT_NNZ_SCATTERED = 4,
+  CNT_ACTIVE = 5,      // active-set length written by the gap kernel
+  CNT_STATUS = 6,      // device-side error flags (DEV_ERR_*)
+  CNT_K_BASE = 7,      // sampler counter of the next update (graph-friendly)
+  CNT_GMAX_BITS = 8,   // max |a_j^T r| as FP64 bits (non-negative, so integer max works)
+  CNT_SLOTS = 16
+};
+
+enum { DEV_ERR_BAD_INDEX = 1, DEV_ERR_BAD_LAYOUT = 2, DEV_ERR_BAD_STATE = 4 };
+
+// Fixed grid for the reductions, so partial sums are combined in a fixed order.
+#define ACDC_RED_BLOCKS 608
+#define ACDC_RED_THREADS 256
+#define ACDC_NPART 8  // partial slots per block
+
+// Parameters of one launch of the update kernel.
+struct UpdateParams {
+  int4* meta;
+  const float* vals;
+  const int32_t* idx;
+  float* r;
+  const int32_t* active;
+  unsigned long long* counters;
+  int64_t n;
+  uint64_t count;       // updates in this launch
+  uint64_t seed;
+  float lambda;         // Lasso: lambda; SVM: lambda * n
+  float inv_lambda_n;   // SVM scatter factor 1/(lambda n)
+  uint32_t shrink_q32;  // probability of an active-set draw, scaled by 2^32 (0 = off)
+  int32_t n_warps;      // tau
+  int32_t loss;
+};
+
+// Parameters of the evaluation kernels.
+struct EvalParams {
+  int4* meta;
+  const float* vals;
+  const int32_t* idx;
+  float* r32;
+  double* r64;
+  const double* rhs64;
+  int32_t* active;
+  unsigned long long* counters;
+  double* part;         // ACDC_RED_BLOCKS * ACDC_NPART
+  double* eval_out;     // 16 doubles
+  int64_t m, n;
+  double lambda;
+  double shrink_thresh; // Lasso: (1-eps) lambda
+  int32_t loss;
+};
+
+struct DevProblem {
+  int64_t m = 0, n = 0, nnz = 0, nnz_pad = 0;
+  int4* meta = nullptr;
+  float* vals = nullptr;
+  int32_t* idx = nullptr;
+  float* r32 = nullptr;
+  double* r64 = nullptr;
+  double* rhs64 = nullptr;
+  double* col_sq = nullptr;
+  int32_t* active = nullptr;
+  float* xbuf = nullptr;    // n floats: staging for x up/downloads
+  double* part = nullptr;
+  double* eval_out = nullptr;
+  unsigned long long* counters = nullptr;
+  int64_t bytes = 0;
+};
+
+struct acdc_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::string last_error;
+};
+
+struct acdc_problem {
+  acdc_ctx* ctx = nullptr;
+  int32_t loss = 0;
+  DevProblem d;
+  acdc_settings s;
+  double lambda = 0;
+  double beta = 1;
+  int64_t omega = 1;
+  uint64_t k_next = 0;      // sampler counter of the next update
+  int64_t epochs_done = 0;  // epochs since the start (shrinking starts after a few)
+  bool active_valid = false;
+  acdc_stats stats;
+  double* h_eval = nullptr;               // pinned, 16 doubles
+  unsigned long long* h_counters = nullptr;  // pinned, CNT_SLOTS
+};
+
+// ---- helpers shared by the translation units ----
+int acdc_set_error(acdc_ctx* ctx, int code, const std::string& msg);
+int acdc_cuda_error(acdc_ctx* ctx, cudaError_t e, const char* what);
+
+#define ACDC_CK(ctx, call)                                             \
+  do {                                                                 \
+    cudaError_t _e = (call);                                           \
+    if (_e != cudaSuccess) return acdc_cuda_error((ctx), _e, #call);   \
+  } while (0)
+
+// ---- kernel launchers (kernels_*.cu) ----
+int64_t layout_scan_tiles(int64_t n);
+cudaError_t launch_layout_scan(const int64_t* col_ptr, int64_t n, int64_t* scratch,
+                               unsigned long long* counters, cudaStream_t st);
+cudaError_t launch_layout_fill(const int64_t* col_ptr, const int32_t* row_idx,
+                               const double* vals64, int64_t m, int64_t n, int64_t* scratch,
+                               DevProblem& d, cudaStream_t st);
+cudaError_t launch_row_counts(const int32_t* idx, int64_t nnz, int32_t* counts, int64_t m,
+                              unsigned long long* counters, cudaStream_t st);
+cudaError_t launch_max_i32(const int32_t* v, int64_t len, unsigned long long* out_slot,
+                           cudaStream_t st);
+cudaError_t launch_widen_i32(const int32_t* src, int64_t* dst, int64_t len, cudaStream_t st);
+cudaError_t launch_set_li(const DevProblem& d, int32_t loss, double beta, cudaStream_t st);
+cudaError_t launch_set_x(const DevProblem& d, const float* x32, cudaStream_t st);
+cudaError_t launch_get_x(const DevProblem& d, float* x32, cudaStream_t st);
+cudaError_t launch_update(const UpdateParams& p, uint64_t k_base, int warps_per_block,
+                          cudaStream_t st);
+cudaError_t launch_refresh(const EvalParams& p, cudaStream_t st);
+cudaError_t launch_gap(const EvalParams& p, cudaStream_t st);
+cudaError_t launch_debug_sample(uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
+                                int64_t* out, cudaStream_t st);

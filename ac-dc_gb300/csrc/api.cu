@@ -1,0 +1,568 @@
+// C-ABI of libacdc_gpu.so: contexts, problem upload, the engine calls and the
+// solve loop.  See include/acdc_gpu.h for the contract of every entry point.
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "acdc_internal.cuh"
+
+// ---- errors ----
+
+int acdc_set_error(acdc_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  return code;
+}
+
+int acdc_cuda_error(acdc_ctx* ctx, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return acdc_set_error(ctx, ACDC_ENOMEM, m);
+  return acdc_set_error(ctx, ACDC_ECUDA, m);
+}
+
+extern "C" const char* acdc_last_error(const acdc_ctx* ctx) {
+  return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+extern "C" const char* acdc_status_string(int status) {
+  switch (status) {
+    case ACDC_OK: return "ok";
+    case ACDC_EINVAL: return "invalid argument";
+    case ACDC_ENOMEM: return "out of memory";
+    case ACDC_EUNSUPPORTED: return "unsupported loss";
+    case ACDC_ECUDA: return "CUDA error";
+    case ACDC_ETIMEOUT: return "device wait timed out";
+    case ACDC_EDEVICE: return "device reported a bad index or state";
+    case ACDC_EBUSY: return "admission refused";
+    case ACDC_ENOTFOUND: return "unknown ticket";
+    case ACDC_ENODEV: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+extern "C" void acdc_settings_default(acdc_settings* s) {
+  if (!s) return;
+  std::memset(s, 0, sizeof(*s));
+  s->loss = ACDC_LOSS_L1_SQUARE;
+  s->tau = 4096;
+  s->warps_per_block = 8;
+  s->refresh_every = 5;
+  s->seed = 0;
+  s->sigma = 0;
+  s->gap_target = 1e-6;
+  s->gap_relative = 1;
+  s->max_epochs = 1000;
+  s->use_shrinking = 0;
+  s->shrinking_starting_iter = 2;
+  s->shrinking_probability = 0.9;
+  s->shrink_eps = 0.1;
+}
+
+// ---- context ----
+
+extern "C" int acdc_ctx_create(int device, acdc_ctx** out) {
+  if (!out) return ACDC_EINVAL;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return ACDC_ENODEV;
+  if (device < 0 || device >= count) return ACDC_EINVAL;
+  acdc_ctx* ctx = new acdc_ctx();
+  ctx->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
+  if (e != cudaSuccess) {
+    delete ctx;
+    return ACDC_ECUDA;
+  }
+  *out = ctx;
+  return ACDC_OK;
+}
+
+extern "C" int acdc_ctx_destroy(acdc_ctx* ctx) {
+  if (!ctx) return ACDC_EINVAL;
+  cudaSetDevice(ctx->device);
+  for (int i = 0; i < 4; ++i)
+    if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return ACDC_OK;
+}
+
+// ---- problem ----
+
+namespace {
+
+template <typename T>
+cudaError_t dalloc(T** p, int64_t count, int64_t* bytes) {
+  size_t b = sizeof(T) * (size_t)(count > 0 ? count : 1);
+  *bytes += (int64_t)b;
+  return cudaMalloc((void**)p, b);
+}
+
+void free_problem_buffers(DevProblem& d) {
+  cudaFree(d.meta);
+  cudaFree(d.vals);
+  cudaFree(d.idx);
+  cudaFree(d.r32);
+  cudaFree(d.r64);
+  cudaFree(d.rhs64);
+  cudaFree(d.col_sq);
+  cudaFree(d.active);
+  cudaFree(d.xbuf);
+  cudaFree(d.part);
+  cudaFree(d.eval_out);
+  cudaFree(d.counters);
+  d = DevProblem();
+}
+
+int check_status_word(acdc_problem* p) {
+  acdc_ctx* ctx = p->ctx;
+  ACDC_CK(ctx, cudaMemcpyAsync(p->h_counters, p->d.counters, sizeof(unsigned long long) * CNT_SLOTS,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  ACDC_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  unsigned long long st = p->h_counters[CNT_STATUS];
+  if (st) {
+    char buf[160];
+    std::snprintf(buf, sizeof buf, "device status 0x%llx (%s%s%s)", st,
+                  (st & DEV_ERR_BAD_INDEX) ? "row index out of range " : "",
+                  (st & DEV_ERR_BAD_LAYOUT) ? "decreasing column pointers " : "",
+                  (st & DEV_ERR_BAD_STATE) ? "bad state" : "");
+    return acdc_set_error(ctx, ACDC_EDEVICE, buf);
+  }
+  return ACDC_OK;
+}
+
+EvalParams eval_params(acdc_problem* p, bool build_active) {
+  EvalParams e;
+  e.meta = p->d.meta;
+  e.vals = p->d.vals;
+  e.idx = p->d.idx;
+  e.r32 = p->d.r32;
+  e.r64 = p->d.r64;
+  e.rhs64 = p->d.rhs64;
+  e.active = build_active ? p->d.active : nullptr;
+  e.counters = p->d.counters;
+  e.part = p->d.part;
+  e.eval_out = p->d.eval_out;
+  e.m = p->d.m;
+  e.n = p->d.n;
+  e.lambda = p->lambda;
+  e.shrink_thresh = (1.0 - p->s.shrink_eps) * p->lambda;
+  e.loss = p->loss;
+  return e;
+}
+
+UpdateParams update_params(acdc_problem* p, uint64_t count, bool shrink) {
+  UpdateParams u;
+  u.meta = p->d.meta;
+  u.vals = p->d.vals;
+  u.idx = p->d.idx;
+  u.r = p->d.r32;
+  u.active = p->d.active;
+  u.counters = p->d.counters;
+  u.n = p->d.n;
+  u.count = count;
+  u.seed = p->s.seed;
+  if (p->loss == ACDC_LOSS_SVM_DUAL) {
+    u.lambda = (float)(p->lambda * (double)p->d.n);
+    u.inv_lambda_n = (float)(1.0 / (p->lambda * (double)p->d.n));
+  } else {
+    u.lambda = (float)p->lambda;
+    u.inv_lambda_n = 0.f;
+  }
+  double q = p->s.shrinking_probability;
+  if (!shrink || q <= 0)
+    u.shrink_q32 = 0;
+  else if (q >= 1)
+    u.shrink_q32 = 0xffffffffu;
+  else
+    u.shrink_q32 = (uint32_t)(q * 4294967296.0);
+  u.n_warps = p->s.tau;
+  u.loss = p->loss;
+  return u;
+}
+
+void fill_eval(const double* h, acdc_eval* out) {
+  out->primal = h[0];
+  out->dual = h[1];
+  out->gap = h[2];
+  out->rel_gap = h[3];
+  out->zero_one_accuracy = h[4];
+  out->reg_norm = h[5];
+  out->sq_norm = h[6];
+  out->max_abs_grad = h[7];
+  out->support = (int64_t)h[8];
+  out->active = (int64_t)h[9];
+}
+
+bool shrink_now(const acdc_problem* p) {
+  return p->s.use_shrinking && p->active_valid && p->epochs_done >= p->s.shrinking_starting_iter;
+}
+
+int apply_settings(acdc_problem* p, const acdc_settings* s) {
+  acdc_ctx* ctx = p->ctx;
+  if (s->loss != p->loss) return acdc_set_error(ctx, ACDC_EINVAL, "settings.loss differs from the problem's loss");
+  if (s->tau < 1 || s->warps_per_block < 1 || s->warps_per_block > 8 || s->refresh_every < 1 ||
+      s->max_epochs < 0 || !(s->gap_target >= 0) || s->shrinking_probability < 0 ||
+      s->shrinking_probability > 1 || s->shrink_eps < 0 || s->shrink_eps >= 1)
+    return acdc_set_error(ctx, ACDC_EINVAL, "invalid settings value");
+  p->s = *s;
+  const double n = (double)p->d.n;
+  if (s->sigma > 0)
+    p->beta = s->sigma;
+  else
+    p->beta = n > 1 ? 1.0 + ((double)p->omega - 1.0) * ((double)s->tau - 1.0) / (n - 1.0) : 1.0;
+  ACDC_CK(ctx, launch_set_li(p->d, p->loss, p->beta, ctx->stream));
+  return ACDC_OK;
+}
+
+int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t* col_ptr64,
+                const int32_t* col_ptr32, const int32_t* row_idx, const double* vals,
+                const double* rhs, double lambda, acdc_problem** out) {
+  if (!ctx || !out) return ACDC_EINVAL;
+  *out = nullptr;
+  if (loss == ACDC_LOSS_L2_SQUARE || loss == ACDC_LOSS_LOGISTIC)
+    return acdc_set_error(ctx, ACDC_EUNSUPPORTED, "loss 1 and 3 are not on this path");
+  if (loss != ACDC_LOSS_L1_SQUARE && loss != ACDC_LOSS_SVM_DUAL)
+    return acdc_set_error(ctx, ACDC_EINVAL, "unknown loss code");
+  if (m <= 0 || n <= 0 || m > INT32_MAX || n > INT32_MAX || !(lambda > 0) || !rhs ||
+      (!col_ptr64 && !col_ptr32))
+    return acdc_set_error(ctx, ACDC_EINVAL, "invalid sizes, lambda or null pointer");
+  const int64_t c0 = col_ptr64 ? col_ptr64[0] : col_ptr32[0];
+  const int64_t nnz = col_ptr64 ? col_ptr64[n] : col_ptr32[n];
+  if (c0 != 0 || nnz < 0) return acdc_set_error(ctx, ACDC_EINVAL, "col_ptr must start at 0 and end at nnz >= 0");
+  if (nnz > 0 && (!row_idx || !vals)) return acdc_set_error(ctx, ACDC_EINVAL, "null row_idx or vals");
+  ACDC_CK(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+
+  acdc_problem* p = new acdc_problem();
+  p->ctx = ctx;
+  p->loss = loss;
+  p->lambda = lambda;
+  std::memset(&p->stats, 0, sizeof(p->stats));
+  DevProblem& d = p->d;
+  d.m = m;
+  d.n = n;
+  d.nnz = nnz;
+  int rc = ACDC_OK;
+  // Staging: col_ptr (int64), row_idx, FP64 values, scan scratch / row counts.
+  const int64_t tiles = layout_scan_tiles(n);
+  const int64_t scratch_len = std::max<int64_t>(n + tiles + 1, (m + 1) / 2 + 1);
+  int64_t* s_colptr = nullptr;
+  int32_t* s_rows = nullptr;
+  double* s_vals = nullptr;
+  int64_t* s_scratch = nullptr;
+  int64_t stage_bytes = 0;
+  auto fail = [&](int code) {
+    cudaFree(s_colptr);
+    cudaFree(s_rows);
+    cudaFree(s_vals);
+    cudaFree(s_scratch);
+    free_problem_buffers(d);
+    if (p->h_eval) cudaFreeHost(p->h_eval);
+    if (p->h_counters) cudaFreeHost(p->h_counters);
+    delete p;
+    return code;
+  };
+#define STEP(call)                                          \
+  do {                                                      \
+    cudaError_t _e = (call);                                \
+    if (_e != cudaSuccess) return fail(acdc_cuda_error(ctx, _e, #call)); \
+  } while (0)
+  STEP(cudaMallocHost((void**)&p->h_eval, sizeof(double) * 16));
+  STEP(cudaMallocHost((void**)&p->h_counters, sizeof(unsigned long long) * CNT_SLOTS));
+  STEP(dalloc(&d.counters, CNT_SLOTS, &d.bytes));
+  STEP(cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long) * CNT_SLOTS, st));
+  STEP(dalloc(&s_colptr, n + 1, &stage_bytes));
+  STEP(dalloc(&s_scratch, scratch_len, &stage_bytes));
+  if (col_ptr64) {
+    STEP(cudaMemcpyAsync(s_colptr, col_ptr64, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st));
+  } else {
+    // Stage the int32 pointers in the scratch area and widen them on the device.
+    int32_t* tmp = reinterpret_cast<int32_t*>(s_scratch);
+    STEP(cudaMemcpyAsync(tmp, col_ptr32, sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, st));
+    STEP(launch_widen_i32(tmp, s_colptr, n + 1, st));
+  }
+  if (nnz > 0) {
+    STEP(dalloc(&s_rows, nnz, &stage_bytes));
+    STEP(dalloc(&s_vals, nnz, &stage_bytes));
+    STEP(cudaMemcpyAsync(s_rows, row_idx, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, st));
+    STEP(cudaMemcpyAsync(s_vals, vals, sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
+  }
+  // Layout pass 1 and the padded size.
+  STEP(launch_layout_scan(s_colptr, n, s_scratch, d.counters, st));
+  // Decreasing column pointers would send the fill pass outside the staged
+  // arrays: stop here if the scan flagged any.
+  rc = check_status_word(p);
+  if (rc != ACDC_OK) return fail(rc);
+  int64_t units = 0;
+  STEP(cudaMemcpyAsync(&units, s_scratch + n + tiles, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  STEP(cudaStreamSynchronize(st));
+  if (units < 0 || units >= ((int64_t)1 << 32))
+    return fail(acdc_set_error(ctx, ACDC_EINVAL, "matrix too large for 32-bit column starts"));
+  d.nnz_pad = units * 4;
+  const int64_t rhs_len = loss == ACDC_LOSS_L1_SQUARE ? m : n;
+  STEP(dalloc(&d.meta, n, &d.bytes));
+  STEP(dalloc(&d.vals, d.nnz_pad, &d.bytes));
+  STEP(dalloc(&d.idx, d.nnz_pad, &d.bytes));
+  STEP(dalloc(&d.r32, m, &d.bytes));
+  STEP(dalloc(&d.r64, m, &d.bytes));
+  STEP(dalloc(&d.rhs64, rhs_len, &d.bytes));
+  STEP(dalloc(&d.col_sq, n, &d.bytes));
+  STEP(dalloc(&d.active, n, &d.bytes));
+  STEP(dalloc(&d.xbuf, n, &d.bytes));
+  STEP(dalloc(&d.part, (int64_t)ACDC_RED_BLOCKS * ACDC_NPART, &d.bytes));
+  STEP(dalloc(&d.eval_out, 16, &d.bytes));
+  STEP(cudaMemsetAsync(d.part, 0, sizeof(double) * ACDC_RED_BLOCKS * ACDC_NPART, st));
+  STEP(cudaMemcpyAsync(d.rhs64, rhs, sizeof(double) * rhs_len, cudaMemcpyHostToDevice, st));
+  STEP(launch_layout_fill(s_colptr, s_rows, s_vals, m, n, s_scratch, d, st));
+  // omega: the largest number of entries in one residual row, counted on the
+  // unpadded input (pad entries all point at row 0).
+  int32_t* counts = reinterpret_cast<int32_t*>(s_scratch);
+  STEP(cudaMemsetAsync(counts, 0, sizeof(int32_t) * m, st));
+  STEP(launch_row_counts(s_rows, nnz, counts, m, d.counters, st));
+  unsigned long long* omega_slot = d.counters + CNT_GMAX_BITS;
+  STEP(cudaMemsetAsync(omega_slot, 0, sizeof(unsigned long long), st));
+  STEP(launch_max_i32(counts, m, omega_slot, st));
+  rc = check_status_word(p);
+  if (rc != ACDC_OK) return fail(rc);
+  // The reference starts its running maximum at 1 (MultiCoreSolver.cpp:24).
+  p->omega = std::max<int64_t>(1, (int64_t)p->h_counters[CNT_GMAX_BITS]);
+  STEP(cudaFree(s_colptr));
+  s_colptr = nullptr;
+  STEP(cudaFree(s_rows));
+  s_rows = nullptr;
+  STEP(cudaFree(s_vals));
+  s_vals = nullptr;
+  STEP(cudaFree(s_scratch));
+  s_scratch = nullptr;
+#undef STEP
+  acdc_settings s;
+  acdc_settings_default(&s);
+  s.loss = loss;
+  if (loss == ACDC_LOSS_SVM_DUAL) s.gap_relative = 0;
+  rc = apply_settings(p, &s);
+  if (rc != ACDC_OK) return fail(rc);
+  *out = p;
+  return ACDC_OK;
+}
+
+}  // namespace
+
+extern "C" int acdc_problem_create(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n,
+                                   const int64_t* col_ptr, const int32_t* row_idx,
+                                   const double* vals, const double* rhs, double lambda,
+                                   acdc_problem** out) {
+  return create_impl(ctx, loss, m, n, col_ptr, nullptr, row_idx, vals, rhs, lambda, out);
+}
+
+extern "C" int acdc_problem_create_i32(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n,
+                                       const int32_t* col_ptr, const int32_t* row_idx,
+                                       const double* vals, const double* rhs, double lambda,
+                                       acdc_problem** out) {
+  return create_impl(ctx, loss, m, n, nullptr, col_ptr, row_idx, vals, rhs, lambda, out);
+}
+
+extern "C" int acdc_problem_destroy(acdc_problem* p) {
+  if (!p) return ACDC_EINVAL;
+  cudaSetDevice(p->ctx->device);
+  cudaStreamSynchronize(p->ctx->stream);
+  free_problem_buffers(p->d);
+  if (p->h_eval) cudaFreeHost(p->h_eval);
+  if (p->h_counters) cudaFreeHost(p->h_counters);
+  delete p;
+  return ACDC_OK;
+}
+
+extern "C" int acdc_problem_info_get(acdc_problem* p, acdc_problem_info* info) {
+  if (!p || !info) return ACDC_EINVAL;
+  info->m = p->d.m;
+  info->n = p->d.n;
+  info->nnz = p->d.nnz;
+  info->nnz_padded = p->d.nnz_pad;
+  info->omega = p->omega;
+  info->sigma = p->beta;
+  info->lambda = p->lambda;
+  info->device_bytes = p->d.bytes;
+  info->loss = p->loss;
+  info->tau = p->s.tau;
+  return ACDC_OK;
+}
+
+extern "C" int acdc_problem_set_settings(acdc_problem* p, const acdc_settings* s) {
+  if (!p || !s) return ACDC_EINVAL;
+  return apply_settings(p, s);
+}
+
+extern "C" int acdc_problem_set_lambda(acdc_problem* p, double lambda) {
+  if (!p) return ACDC_EINVAL;
+  if (!(lambda > 0)) return acdc_set_error(p->ctx, ACDC_EINVAL, "lambda must be positive");
+  p->lambda = lambda;
+  p->active_valid = false;
+  return ACDC_OK;
+}
+
+extern "C" int acdc_run_updates(acdc_problem* p, uint64_t n_updates) {
+  if (!p) return ACDC_EINVAL;
+  acdc_ctx* ctx = p->ctx;
+  UpdateParams u = update_params(p, n_updates, shrink_now(p));
+  ACDC_CK(ctx, launch_update(u, p->k_next, p->s.warps_per_block, ctx->stream));
+  p->k_next += n_updates;
+  p->stats.update_launches++;
+  return ACDC_OK;
+}
+
+extern "C" int acdc_recompute_residuals(acdc_problem* p) {
+  if (!p) return ACDC_EINVAL;
+  EvalParams e = eval_params(p, false);
+  ACDC_CK(p->ctx, launch_refresh(e, p->ctx->stream));
+  return ACDC_OK;
+}
+
+namespace {
+// Refresh + gap; copies the result to the pinned host buffer and waits.
+int evaluate_impl(acdc_problem* p, acdc_eval* out, float* ms) {
+  acdc_ctx* ctx = p->ctx;
+  const bool build_active = p->s.use_shrinking != 0;
+  EvalParams e = eval_params(p, build_active);
+  ACDC_CK(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+  ACDC_CK(ctx, launch_refresh(e, ctx->stream));
+  ACDC_CK(ctx, launch_gap(e, ctx->stream));
+  ACDC_CK(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
+  ACDC_CK(ctx, cudaMemcpyAsync(p->h_eval, p->d.eval_out, sizeof(double) * 16,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  int rc = check_status_word(p);  // synchronises the stream
+  if (rc != ACDC_OK) return rc;
+  float t = 0;
+  ACDC_CK(ctx, cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]));
+  p->stats.eval_ms += t;
+  p->stats.eval_launches++;
+  if (ms) *ms = t;
+  if (build_active) p->active_valid = true;
+  if (out) fill_eval(p->h_eval, out);
+  if (!std::isfinite(p->h_eval[0]))
+    return acdc_set_error(ctx, ACDC_EDEVICE, "objective is not finite (diverged or bad input)");
+  return ACDC_OK;
+}
+
+bool converged(const acdc_settings& s, const acdc_eval& ev) {
+  return (s.gap_relative ? ev.rel_gap : ev.gap) <= s.gap_target;
+}
+}  // namespace
+
+extern "C" int acdc_evaluate(acdc_problem* p, acdc_eval* out) {
+  if (!p) return ACDC_EINVAL;
+  return evaluate_impl(p, out, nullptr);
+}
+
+extern "C" int acdc_solve(acdc_problem* p, acdc_solve_result* out) {
+  if (!p || !out) return ACDC_EINVAL;
+  acdc_ctx* ctx = p->ctx;
+  std::memset(out, 0, sizeof(*out));
+  auto t0 = std::chrono::steady_clock::now();
+  acdc_eval ev;
+  int rc = evaluate_impl(p, &ev, nullptr);
+  if (rc != ACDC_OK) return rc;
+  int epochs = 0;
+  while (!converged(p->s, ev) && epochs < p->s.max_epochs) {
+    const int k = std::min(p->s.refresh_every, p->s.max_epochs - epochs);
+    const uint64_t count = (uint64_t)k * (uint64_t)p->d.n;
+    UpdateParams u = update_params(p, count, shrink_now(p));
+    ACDC_CK(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+    ACDC_CK(ctx, launch_update(u, p->k_next, p->s.warps_per_block, ctx->stream));
+    ACDC_CK(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+    p->k_next += count;
+    p->stats.update_launches++;
+    epochs += k;
+    p->epochs_done += k;
+    rc = evaluate_impl(p, &ev, nullptr);
+    if (rc != ACDC_OK) return rc;
+    float t = 0;
+    ACDC_CK(ctx, cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]));
+    p->stats.update_ms += t;
+  }
+  out->eval = ev;
+  out->converged = converged(p->s, ev) ? 1 : 0;
+  out->epochs = epochs;
+  out->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return acdc_get_stats(p, &out->stats);
+}
+
+extern "C" int acdc_get_x(acdc_problem* p, double* x) {
+  if (!p || !x) return ACDC_EINVAL;
+  acdc_ctx* ctx = p->ctx;
+  std::vector<float> h((size_t)p->d.n);
+  ACDC_CK(ctx, launch_get_x(p->d, p->d.xbuf, ctx->stream));
+  ACDC_CK(ctx, cudaMemcpyAsync(h.data(), p->d.xbuf, sizeof(float) * p->d.n, cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  ACDC_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int64_t j = 0; j < p->d.n; ++j) x[j] = (double)h[(size_t)j];
+  return ACDC_OK;
+}
+
+extern "C" int acdc_set_x(acdc_problem* p, const double* x) {
+  if (!p || !x) return ACDC_EINVAL;
+  acdc_ctx* ctx = p->ctx;
+  std::vector<float> h((size_t)p->d.n);
+  for (int64_t j = 0; j < p->d.n; ++j) h[(size_t)j] = (float)x[j];
+  ACDC_CK(ctx, cudaMemcpyAsync(p->d.xbuf, h.data(), sizeof(float) * p->d.n, cudaMemcpyHostToDevice,
+                               ctx->stream));
+  ACDC_CK(ctx, launch_set_x(p->d, p->d.xbuf, ctx->stream));
+  ACDC_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  p->active_valid = false;
+  return acdc_recompute_residuals(p);
+}
+
+extern "C" int acdc_get_residuals(acdc_problem* p, double* r) {
+  if (!p || !r) return ACDC_EINVAL;
+  acdc_ctx* ctx = p->ctx;
+  std::vector<float> h((size_t)p->d.m);
+  ACDC_CK(ctx, cudaMemcpyAsync(h.data(), p->d.r32, sizeof(float) * p->d.m, cudaMemcpyDeviceToHost, ctx->stream));
+  ACDC_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int64_t i = 0; i < p->d.m; ++i) r[i] = (double)h[(size_t)i];
+  return ACDC_OK;
+}
+
+extern "C" int acdc_get_stats(acdc_problem* p, acdc_stats* s) {
+  if (!p || !s) return ACDC_EINVAL;
+  int rc = check_status_word(p);
+  if (rc != ACDC_OK) return rc;
+  p->stats.updates = p->h_counters[CNT_UPDATES];
+  p->stats.nonzero_updates = p->h_counters[CNT_NONZERO];
+  p->stats.nnz_read = p->h_counters[CNT_NNZ_READ];
+  p->stats.nnz_scattered = p->h_counters[CNT_NNZ_SCATTERED];
+  *s = p->stats;
+  return ACDC_OK;
+}
+
+extern "C" int acdc_reset_stats(acdc_problem* p) {
+  if (!p) return ACDC_EINVAL;
+  acdc_ctx* ctx = p->ctx;
+  ACDC_CK(ctx, cudaMemsetAsync(p->d.counters + CNT_UPDATES, 0, sizeof(unsigned long long) * 4, ctx->stream));
+  ACDC_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  std::memset(&p->stats, 0, sizeof(p->stats));
+  return ACDC_OK;
+}
+
+extern "C" int acdc_synchronize(acdc_problem* p) {
+  if (!p) return ACDC_EINVAL;
+  ACDC_CK(p->ctx, cudaStreamSynchronize(p->ctx->stream));
+  return check_status_word(p);
+}
+
+extern "C" int acdc_debug_sample(acdc_ctx* ctx, uint64_t seed, uint64_t k0, uint64_t count,
+                                 int64_t n, int64_t* out) {
+  if (!ctx || (count > 0 && !out) || n <= 0) return ACDC_EINVAL;
+  int64_t* d = nullptr;
+  ACDC_CK(ctx, cudaMalloc((void**)&d, sizeof(int64_t) * (count > 0 ? count : 1)));
+  cudaError_t e = launch_debug_sample(seed, k0, count, n, d, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, d, sizeof(int64_t) * count, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return acdc_cuda_error(ctx, e, "acdc_debug_sample");
+  return ACDC_OK;
+}

@@ -1,0 +1,546 @@
+// Layout build, Lipschitz constants, FP64 residual refresh and FP64
+// objective / duality-gap kernels (sm_103a).
+//
+// Refresh: MulticoreSquareLoss::recomputeResiduals
+// (cpp/src/solver/lossFunctions/squareLoss/MulticoreSquareLoss.h:42-53) and
+// MulticoreSVMDualLoss::recomputeResiduals (MulticoreSVMDualLoss.h:31-46),
+// scattering only coordinates that are nonzero, in FP64.
+// Objective: MulticoreL1RegSquareLoss::computeObjectiveValue
+// (MulticoreL1RegSquareLoss.h:30-39) plus the Lasso dual point
+// u = s r, s = min(1, lambda/||A^T r||_inf); MulticoreSVMDualLoss::computeObjectiveValue
+// (MulticoreSVMDualLoss.h:63-117).  Every reduction runs on a fixed grid of
+// ACDC_RED_BLOCKS blocks whose partials one block then adds in index order.
+#include <algorithm>
+
+#include "acdc_internal.cuh"
+
+namespace {
+
+constexpr int kScanItems = 8;
+constexpr int kScanThreads = 512;
+constexpr int kScanTile = kScanItems * kScanThreads;
+
+__device__ __forceinline__ int64_t padded_units(const int64_t* col_ptr, int64_t j) {
+  const int64_t len = col_ptr[j + 1] - col_ptr[j];
+  return len > 0 ? (len + 3) >> 2 : 0;
+}
+
+// Block-wide exclusive scan of int64 values held kScanItems per thread.
+__device__ int64_t block_exclusive_scan(int64_t v, int64_t* smem, int64_t* total) {
+  const int t = threadIdx.x;
+  smem[t] = v;
+  __syncthreads();
+  for (int off = 1; off < blockDim.x; off <<= 1) {
+    int64_t a = t >= off ? smem[t - off] : 0;
+    __syncthreads();
+    smem[t] += a;
+    __syncthreads();
+  }
+  int64_t incl = smem[t];
+  *total = smem[blockDim.x - 1];
+  __syncthreads();
+  return incl - v;
+}
+
+// Pass 1: per-tile totals of padded column lengths (units of 4 entries); also
+// flags decreasing column pointers.
+__global__ void k_scan_tiles(const int64_t* col_ptr, int64_t n, int64_t* tile_sums,
+                             unsigned long long* counters) {
+  __shared__ int64_t smem[kScanThreads];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  int64_t s = 0;
+  for (int i = 0; i < kScanItems; ++i) {
+    int64_t j = base + i;
+    if (j < n) {
+      if (col_ptr[j + 1] < col_ptr[j]) atomicOr(counters + CNT_STATUS, (unsigned long long)DEV_ERR_BAD_LAYOUT);
+      s += padded_units(col_ptr, j);
+    }
+  }
+  int64_t total;
+  block_exclusive_scan(s, smem, &total);
+  if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+// Pass 2: exclusive scan of the tile totals (one block, sequential over chunks).
+__global__ void k_scan_offsets(int64_t* tile_sums, int64_t tiles, int64_t* grand_total) {
+  __shared__ int64_t smem[kScanThreads];
+  int64_t carry = 0;
+  for (int64_t base = 0; base < tiles; base += kScanThreads) {
+    int64_t i = base + threadIdx.x;
+    int64_t v = i < tiles ? tile_sums[i] : 0;
+    int64_t total;
+    int64_t ex = block_exclusive_scan(v, smem, &total);
+    if (i < tiles) tile_sums[i] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) *grand_total = carry;
+}
+
+// Pass 3: start4[j] = exclusive prefix of padded units.
+__global__ void k_scan_apply(const int64_t* col_ptr, int64_t n, const int64_t* tile_offsets,
+                             int64_t* start4) {
+  __shared__ int64_t smem[kScanThreads];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  int64_t s = 0;
+  for (int i = 0; i < kScanItems; ++i) {
+    int64_t j = base + i;
+    if (j < n) s += padded_units(col_ptr, j);
+  }
+  int64_t total;
+  int64_t ex = block_exclusive_scan(s, smem, &total) + tile_offsets[blockIdx.x];
+  for (int i = 0; i < kScanItems; ++i) {
+    int64_t j = base + i;
+    if (j < n) {
+      start4[j] = ex;
+      ex += padded_units(col_ptr, j);
+    }
+  }
+}
+
+// One warp per column: copy FP64 values to FP32 and indices into the padded
+// segment, zero the pad, check indices, compute ||a_j||^2 in FP64 and write meta.
+__global__ void k_build_columns(const int64_t* col_ptr, const int32_t* row_idx,
+                                const double* vals64, const int64_t* start4, int64_t m, int64_t n,
+                                DevProblem d) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < n; j += warps) {
+    const int64_t s = col_ptr[j];
+    const int64_t len = col_ptr[j + 1] - s;
+    const int64_t dst = start4[j] << 2;
+    const int64_t plen = len > 0 ? ((len + 3) >> 2) << 2 : 0;
+    double sq = 0;
+    for (int64_t e = lane; e < plen; e += 32) {
+      float v = 0.f;
+      int32_t r = 0;
+      if (e < len) {
+        double dv = vals64[s + e];
+        r = row_idx[s + e];
+        if (r < 0 || r >= m) {
+          atomicOr(d.counters + CNT_STATUS, (unsigned long long)DEV_ERR_BAD_INDEX);
+          r = 0;
+          dv = 0;
+        }
+        v = (float)dv;
+        sq += dv * dv;
+      }
+      d.vals[dst + e] = v;
+      d.idx[dst + e] = r;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(ACDC_FULL_MASK, sq, o);
+    if (lane == 0) {
+      d.col_sq[j] = sq;
+      d.meta[j] = make_int4((int)(uint32_t)start4[j], (int)len, 0, 0);
+    }
+  }
+}
+
+__global__ void k_row_counts(const int32_t* idx, int64_t nnz, int32_t* counts, int64_t m) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += stride) {
+    int32_t r = idx[e];
+    if (r >= 0 && r < m) atomicAdd(counts + r, 1);
+  }
+}
+
+__global__ void k_max_i32(const int32_t* v, int64_t len, unsigned long long* out) {
+  int32_t best = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
+    best = max(best, v[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(ACDC_FULL_MASK, best, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)best);
+}
+
+// Li = 1/(beta ||a_j||^2) (0 for an empty column); the SVM stores y_j Li.
+__global__ void k_set_li(DevProblem d, int32_t loss, double beta) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < d.n; j += stride) {
+    double sq = d.col_sq[j];
+    double li = sq > 0 ? 1.0 / (beta * sq) : 0.0;
+    if (loss == ACDC_LOSS_SVM_DUAL && d.rhs64[j] < 0) li = -li;
+    d.meta[j].z = __float_as_int((float)li);
+  }
+}
+
+__global__ void k_widen_i32(const int32_t* src, int64_t* dst, int64_t len) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
+    dst[i] = (int64_t)src[i];
+}
+
+__global__ void k_set_x(DevProblem d, const float* x) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < d.n; j += stride)
+    d.meta[j].w = __float_as_int(x[j]);
+}
+
+__global__ void k_get_x(DevProblem d, float* x) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < d.n; j += stride)
+    x[j] = __int_as_float(__ldcg(&d.meta[j].w));
+}
+
+// ---- refresh ----
+
+// r64 = -b (Lasso) or 0 (SVM).
+__global__ void k_refresh_init(EvalParams p) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.m; i += stride)
+    p.r64[i] = p.loss == ACDC_LOSS_L1_SQUARE ? -p.rhs64[i] : 0.0;
+}
+
+// Each warp reads 32 consecutive coordinates, then scatters the nonzero ones
+// cooperatively: r64 += coef_j a_j with coef = x_j (Lasso) or
+// alpha_j y_j / (lambda n) after clipping alpha_j into [0, 1] (SVM).
+__global__ void k_refresh_scatter(EvalParams p) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const double inv_ln = 1.0 / (p.lambda * (double)p.n);
+  for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < p.n;
+       base += warps * 32) {
+    const int64_t j = base + lane;
+    double coef = 0;
+    int4 mt = make_int4(0, 0, 0, 0);
+    if (j < p.n) {
+      mt = p.meta[j];
+      float xv = __int_as_float(mt.w);
+      if (p.loss == ACDC_LOSS_SVM_DUAL) {
+        float c = xv > 1.f ? 1.f : (xv < 0.f ? 0.f : xv);
+        if (c != xv) p.meta[j].w = __float_as_int(c);
+        coef = (double)c * p.rhs64[j] * inv_ln;
+      } else {
+        coef = (double)xv;
+      }
+    }
+    unsigned live = __ballot_sync(ACDC_FULL_MASK, coef != 0.0 && mt.y > 0);
+    while (live) {
+      const int src = __ffs(live) - 1;
+      live &= live - 1;
+      const double cj = __shfl_sync(ACDC_FULL_MASK, coef, src);
+      const int64_t start = (int64_t)(uint32_t)__shfl_sync(ACDC_FULL_MASK, mt.x, src) << 2;
+      const int32_t len = __shfl_sync(ACDC_FULL_MASK, mt.y, src);
+      for (int32_t e = lane; e < len; e += 32)
+        atomicAdd(p.r64 + p.idx[start + e], cj * (double)p.vals[start + e]);
+    }
+  }
+}
+
+// r32 = (float) r64 and the partial sums sum r^2 (slot 0), sum b r (slot 1).
+__global__ void __launch_bounds__(ACDC_RED_THREADS) k_refresh_finish(EvalParams p) {
+  __shared__ double s0[ACDC_RED_THREADS / 32], s1[ACDC_RED_THREADS / 32];
+  double a0 = 0, a1 = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.m; i += stride) {
+    double v = p.r64[i];
+    p.r32[i] = (float)v;
+    a0 += v * v;
+    if (p.loss == ACDC_LOSS_L1_SQUARE) a1 += p.rhs64[i] * v;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a0 += __shfl_down_sync(ACDC_FULL_MASK, a0, o);
+    a1 += __shfl_down_sync(ACDC_FULL_MASK, a1, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s0[threadIdx.x >> 5] = a0;
+    s1[threadIdx.x >> 5] = a1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0, t1 = 0;
+    for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) {
+      t0 += s0[w];
+      t1 += s1[w];
+    }
+    p.part[blockIdx.x * ACDC_NPART + 0] = t0;
+    p.part[blockIdx.x * ACDC_NPART + 1] = t1;
+  }
+}
+
+// ---- gap ----
+
+// Lasso: groups of 8 lanes per column; slots 2: sum |x|, 3: max |a_j^T r|,
+// 4: support count.  Columns with x_j != 0 or |a_j^T r| > shrink_thresh join the
+// active set.
+__global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso(EvalParams p) {
+  __shared__ double s_l1[ACDC_RED_THREADS / 32], s_gm[ACDC_RED_THREADS / 32],
+      s_sp[ACDC_RED_THREADS / 32];
+  const int lane = threadIdx.x & 31;
+  const int sub = lane & 7;
+  const int grp = lane >> 3;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double l1 = 0, gmax = 0, sp = 0;
+  for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 4; base < p.n;
+       base += warps * 4) {
+    const int64_t j = base + grp;
+    int4 mt = make_int4(0, 0, 0, 0);
+    if (j < p.n) mt = p.meta[j];
+    const int64_t start = (int64_t)(uint32_t)mt.x << 2;
+    const int32_t len = mt.y;
+    double g = 0;
+    // The four groups may have different lengths: loop to the longest.
+    int32_t lmax = len;
+    lmax = max(lmax, __shfl_xor_sync(ACDC_FULL_MASK, lmax, 8));
+    lmax = max(lmax, __shfl_xor_sync(ACDC_FULL_MASK, lmax, 16));
+    for (int32_t off = 4 * sub; off < lmax; off += 32) {
+      if (off < len) {
+        float4 v = __ldcs(reinterpret_cast<const float4*>(p.vals + start + off));
+        int4 id = __ldcs(reinterpret_cast<const int4*>(p.idx + start + off));
+        g += (double)v.x * p.r64[id.x];
+        g += (double)v.y * p.r64[id.y];
+        g += (double)v.z * p.r64[id.z];
+        g += (double)v.w * p.r64[id.w];
+      }
+    }
+    g += __shfl_xor_sync(ACDC_FULL_MASK, g, 4);
+    g += __shfl_xor_sync(ACDC_FULL_MASK, g, 2);
+    g += __shfl_xor_sync(ACDC_FULL_MASK, g, 1);
+    bool join = false;
+    if (sub == 0 && j < p.n) {
+      const float xv = __int_as_float(mt.w);
+      const double ag = fabs(g);
+      gmax = fmax(gmax, ag);
+      l1 += fabs((double)xv);
+      sp += xv != 0.f ? 1.0 : 0.0;
+      join = p.active && (xv != 0.f || ag > p.shrink_thresh);
+    }
+    // One counter increment per warp for the (up to four) joining columns.
+    const unsigned joiners = __ballot_sync(ACDC_FULL_MASK, join);
+    if (joiners) {
+      unsigned long long first = 0;
+      if (lane == __ffs(joiners) - 1) first = atomicAdd(p.counters + CNT_ACTIVE, (unsigned long long)__popc(joiners));
+      first = __shfl_sync(ACDC_FULL_MASK, first, __ffs(joiners) - 1);
+      if (join) {
+        unsigned long long pos = first + __popc(joiners & ((1u << lane) - 1u));
+        if (pos < (unsigned long long)p.n) p.active[pos] = (int32_t)j;
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    l1 += __shfl_down_sync(ACDC_FULL_MASK, l1, o);
+    gmax = fmax(gmax, __shfl_down_sync(ACDC_FULL_MASK, gmax, o));
+    sp += __shfl_down_sync(ACDC_FULL_MASK, sp, o);
+  }
+  if (lane == 0) {
+    s_l1[threadIdx.x >> 5] = l1;
+    s_gm[threadIdx.x >> 5] = gmax;
+    s_sp[threadIdx.x >> 5] = sp;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0, t1 = 0, t2 = 0;
+    for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) {
+      t0 += s_l1[w];
+      t1 = fmax(t1, s_gm[w]);
+      t2 += s_sp[w];
+    }
+    p.part[blockIdx.x * ACDC_NPART + 2] = t0;
+    p.part[blockIdx.x * ACDC_NPART + 3] = t1;
+    p.part[blockIdx.x * ACDC_NPART + 4] = t2;
+  }
+}
+
+// SVM: one warp per sample; slots 2: sum alpha, 3: sum hinge, 4: support,
+// 5: correctly classified count.  Samples that are margin-violating or have
+// 0 < alpha < 1 join the active set.
+__global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_svm(EvalParams p) {
+  __shared__ double s_a[ACDC_RED_THREADS / 32], s_h[ACDC_RED_THREADS / 32],
+      s_sp[ACDC_RED_THREADS / 32], s_ok[ACDC_RED_THREADS / 32];
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double sa = 0, sh = 0, sp = 0, ok = 0;
+  for (int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < p.n; j += warps) {
+    const int4 mt = p.meta[j];
+    const int64_t start = (int64_t)(uint32_t)mt.x << 2;
+    const int32_t len = mt.y;
+    double g = 0;
+    for (int32_t off = 4 * lane; off < len; off += 128) {
+      float4 v = __ldcs(reinterpret_cast<const float4*>(p.vals + start + off));
+      int4 id = __ldcs(reinterpret_cast<const int4*>(p.idx + start + off));
+      g += (double)v.x * p.r64[id.x];
+      g += (double)v.y * p.r64[id.y];
+      g += (double)v.z * p.r64[id.z];
+      g += (double)v.w * p.r64[id.w];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(ACDC_FULL_MASK, g, o);
+    if (lane == 0) {
+      const double y = p.rhs64[j];
+      const double a = (double)__int_as_float(mt.w);
+      if (y * g > 0) ok += 1.0;
+      double h = 1.0 - y * g;
+      if (h < 0) h = 0;
+      sh += h;
+      sa += a;
+      sp += a != 0.0 ? 1.0 : 0.0;
+      if (p.active && ((a > 0.0 && a < 1.0) || (h > 0.0 && a < 1.0) || (h == 0.0 && a > 0.0))) {
+        unsigned long long pos = atomicAdd(p.counters + CNT_ACTIVE, 1ull);
+        if (pos < (unsigned long long)p.n) p.active[pos] = (int32_t)j;
+      }
+    }
+  }
+  if (lane == 0) {
+    s_a[threadIdx.x >> 5] = sa;
+    s_h[threadIdx.x >> 5] = sh;
+    s_sp[threadIdx.x >> 5] = sp;
+    s_ok[threadIdx.x >> 5] = ok;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0, t1 = 0, t2 = 0, t3 = 0;
+    for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) {
+      t0 += s_a[w];
+      t1 += s_h[w];
+      t2 += s_sp[w];
+      t3 += s_ok[w];
+    }
+    p.part[blockIdx.x * ACDC_NPART + 2] = t0;
+    p.part[blockIdx.x * ACDC_NPART + 3] = t1;
+    p.part[blockIdx.x * ACDC_NPART + 4] = t2;
+    p.part[blockIdx.x * ACDC_NPART + 5] = t3;
+  }
+}
+
+// Adds the per-block partials in block order and forms P, D and the gap.
+// eval_out: [0] P [1] D [2] gap [3] rel_gap [4] 0-1 accuracy [5] reg_norm
+//           [6] sq_norm [7] max_abs_grad [8] support [9] active
+__global__ void k_finalize(EvalParams p) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double rr = 0, br = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
+  for (int b = 0; b < ACDC_RED_BLOCKS; ++b) {
+    const double* q = p.part + b * ACDC_NPART;
+    rr += q[0];
+    br += q[1];
+    s2 += q[2];
+    s4 += q[4];
+    s5 += q[5];
+    if (p.loss == ACDC_LOSS_L1_SQUARE)
+      s3 = fmax(s3, q[3]);
+    else
+      s3 += q[3];
+  }
+  double P, D, acc = 0, gmax = 0;
+  const double nn = (double)p.n;
+  if (p.loss == ACDC_LOSS_L1_SQUARE) {
+    gmax = s3;
+    P = 0.5 * rr + p.lambda * s2;
+    const double s = gmax > p.lambda ? p.lambda / gmax : 1.0;
+    D = -s * br - 0.5 * s * s * rr;
+  } else {
+    P = p.lambda * 0.5 * rr + s3 / nn;
+    D = -p.lambda * 0.5 * rr + s2 / nn;
+    acc = s5 / nn;
+  }
+  const double gap = P - D;
+  double* o = p.eval_out;
+  o[0] = P;
+  o[1] = D;
+  o[2] = gap;
+  o[3] = gap / fmax(1.0, fabs(P));
+  o[4] = acc;
+  o[5] = s2;
+  o[6] = rr;
+  o[7] = gmax;
+  o[8] = s4;
+  o[9] = (double)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n);
+}
+
+}  // namespace
+
+// ---- launchers ----
+
+// Pass 1 of the layout: padded column lengths are scanned per tile and the
+// grand total (in units of 4 entries) lands in scratch[n + tiles].
+// scratch must hold n + tiles + 1 int64 entries (start4[n], tile sums, total).
+int64_t layout_scan_tiles(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
+
+cudaError_t launch_layout_scan(const int64_t* col_ptr, int64_t n, int64_t* scratch,
+                               unsigned long long* counters, cudaStream_t st) {
+  const int64_t tiles = layout_scan_tiles(n);
+  int64_t* tile_sums = scratch + n;
+  int64_t* total = tile_sums + tiles;
+  cudaError_t e = cudaMemsetAsync(total, 0, sizeof(int64_t), st);
+  if (e != cudaSuccess || n == 0) return e;
+  k_scan_tiles<<<(unsigned)tiles, kScanThreads, 0, st>>>(col_ptr, n, tile_sums, counters);
+  k_scan_offsets<<<1, kScanThreads, 0, st>>>(tile_sums, tiles, total);
+  return cudaGetLastError();
+}
+
+// Pass 2: column starts and the padded FP32 / int32 arrays with ||a_j||^2.
+cudaError_t launch_layout_fill(const int64_t* col_ptr, const int32_t* row_idx,
+                               const double* vals64, int64_t m, int64_t n, int64_t* scratch,
+                               DevProblem& d, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const int64_t tiles = layout_scan_tiles(n);
+  int64_t* start4 = scratch;
+  int64_t* tile_sums = scratch + n;
+  k_scan_apply<<<(unsigned)tiles, kScanThreads, 0, st>>>(col_ptr, n, tile_sums, start4);
+  const int64_t blocks = std::min<int64_t>((n + 7) / 8, 152 * 32);
+  k_build_columns<<<(unsigned)blocks, 256, 0, st>>>(col_ptr, row_idx, vals64, start4, m, n, d);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_row_counts(const int32_t* idx, int64_t nnz, int32_t* counts, int64_t m,
+                              unsigned long long* counters, cudaStream_t st) {
+  (void)counters;
+  if (nnz == 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((nnz + 255) / 256, 152 * 16);
+  k_row_counts<<<(unsigned)blocks, 256, 0, st>>>(idx, nnz, counts, m);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_max_i32(const int32_t* v, int64_t len, unsigned long long* out_slot,
+                           cudaStream_t st) {
+  if (len == 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((len + 255) / 256, 152 * 8);
+  k_max_i32<<<(unsigned)blocks, 256, 0, st>>>(v, len, out_slot);
+  return cudaGetLastError();
+}
+
+static unsigned grid_for(int64_t n, int threads, int64_t cap) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  return (unsigned)std::min<int64_t>(b, cap);
+}
+
+cudaError_t launch_set_li(const DevProblem& d, int32_t loss, double beta, cudaStream_t st) {
+  k_set_li<<<grid_for(d.n, 256, 152 * 8), 256, 0, st>>>(d, loss, beta);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_widen_i32(const int32_t* src, int64_t* dst, int64_t len, cudaStream_t st) {
+  k_widen_i32<<<grid_for(len, 256, 152 * 8), 256, 0, st>>>(src, dst, len);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_x(const DevProblem& d, const float* x32, cudaStream_t st) {
+  k_set_x<<<grid_for(d.n, 256, 152 * 8), 256, 0, st>>>(d, x32);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_get_x(const DevProblem& d, float* x32, cudaStream_t st) {
+  k_get_x<<<grid_for(d.n, 256, 152 * 8), 256, 0, st>>>(d, x32);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_refresh(const EvalParams& p, cudaStream_t st) {
+  k_refresh_init<<<grid_for(p.m, 256, 152 * 8), 256, 0, st>>>(p);
+  k_refresh_scatter<<<grid_for((p.n + 31) / 32 * 32, 256, 152 * 16), 256, 0, st>>>(p);
+  k_refresh_finish<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gap(const EvalParams& p, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(p.counters + CNT_ACTIVE, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  if (p.loss == ACDC_LOSS_L1_SQUARE)
+    k_gap_lasso<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
+  else
+    k_gap_svm<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
+  k_finalize<<<1, 32, 0, st>>>(p);
+  return cudaGetLastError();
+}

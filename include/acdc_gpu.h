@@ -1,0 +1,259 @@
+/*
+ * acdc_gpu.h - C-ABI of the GB300 (sm_103a) PCDM library, libacdc_gpu.so.
+ *
+ * The library replaces the hot path of optml/ac-dc's multicore engine:
+ * randomized parallel coordinate descent (PCDM) for
+ *   loss 0: L1-regularised least squares  min_x 0.5||Ax-b||^2 + lambda||x||_1
+ *   loss 2: hinge-loss SVM dual (SDCA)    max_a (1/n)sum a_i - (lambda/2)||w(a)||^2,
+ *                                          w(a) = (1/(lambda n)) sum_i a_i y_i x_i
+ * behind plain pointers and sizes.  A C++ engine (CudaEngineExecutor.h) plugs
+ * these calls into the reference's AbstractEngineExecutor / Solver structure.
+ *
+ * Conventions
+ *  - Every function returns 0 (ACDC_OK) or a negative ACDC_E* status; no C++
+ *    exception crosses this boundary.  acdc_last_error() gives the message.
+ *  - Matrices arrive as compressed columns of the coordinate operand:
+ *      loss 0: CSC of A (m rows x n columns), vector b of length m;
+ *      loss 2: CSR of X by sample == CSC of X^T (m = features, n = samples),
+ *              labels y of length n.
+ *    This matches ProblemData<L,D> (cpp/src/solver/structures.h:31-97): the
+ *    multicore Lasso reads A_csc_*, the SVM dual reads A_csr_*, and in both
+ *    instance.m is the residual length and instance.n the coordinate count.
+ *  - Host arrays are only read during the call that takes them; the library
+ *    owns every device buffer until the matching *_destroy.
+ *  - One context per host thread; calls on one context are serialised.
+ */
+#ifndef ACDC_GPU_H_
+#define ACDC_GPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define ACDC_OK 0
+#define ACDC_EINVAL (-1)      /* invalid argument (sizes, pointers, indices)        */
+#define ACDC_ENOMEM (-2)      /* device or host allocation failed                   */
+#define ACDC_EUNSUPPORTED (-3)/* loss code 1 or 3 (not on this path)                */
+#define ACDC_ECUDA (-4)       /* CUDA runtime error                                 */
+#define ACDC_ETIMEOUT (-5)    /* a bounded device wait ran out                      */
+#define ACDC_EDEVICE (-6)     /* a kernel reported a bad index or state             */
+#define ACDC_EBUSY (-7)       /* server admission refused (budget or slots)         */
+#define ACDC_ENOTFOUND (-8)   /* unknown ticket                                     */
+#define ACDC_ENODEV (-9)      /* no CUDA device                                     */
+
+/* ---- loss codes (OptimizationSettings::lossFunction,
+ *      cpp/src/solver/MulticoreEngineExecutor.h:32-58) ------------------- */
+#define ACDC_LOSS_L1_SQUARE 0
+#define ACDC_LOSS_L2_SQUARE 1 /* unsupported: returns ACDC_EUNSUPPORTED */
+#define ACDC_LOSS_SVM_DUAL 2
+#define ACDC_LOSS_LOGISTIC 3  /* unsupported: returns ACDC_EUNSUPPORTED */
+
+typedef struct acdc_ctx acdc_ctx;
+typedef struct acdc_problem acdc_problem;
+typedef struct acdc_server acdc_server;
+
+/* Solver settings: the OptimizationSettings fields this path reads
+ * (cpp/src/solver/settingsAndStatistics.h:11-93) plus the device knobs. */
+typedef struct acdc_settings {
+  int32_t loss;                   /* lossFunction: 0 or 2                          */
+  int32_t tau;                    /* updates in flight (= totalThreads); >= 1      */
+  int32_t warps_per_block;        /* CTA size in warps for the update kernel       */
+  int32_t refresh_every;          /* epochs between FP64 refresh + gap in solve    */
+  uint64_t seed;                  /* sampler key                                   */
+  double sigma;                   /* ESO beta; <= 0: 1+(omega-1)(tau-1)/(n-1)      */
+  double gap_target;              /* solve stops when the gap reaches this         */
+  int32_t gap_relative;           /* 1: compare (P-D)/max(1,|P|); 0: P-D           */
+  int32_t max_epochs;             /* solve gives up after this many epochs         */
+  int32_t use_shrinking;          /* q-shrinking (use_shrinking)                   */
+  int32_t shrinking_starting_iter;/* epochs before shrinking starts                */
+  double shrinking_probability;   /* q: probability of drawing from the active set */
+  double shrink_eps;              /* Lasso active test |a_j^T r| > (1-eps) lambda   */
+  int32_t reserved[8];
+} acdc_settings;
+
+/* FP64 evaluation of the current iterate (after an FP64 refresh). */
+typedef struct acdc_eval {
+  double primal;            /* P                                                  */
+  double dual;              /* D                                                  */
+  double gap;               /* P - D                                              */
+  double rel_gap;           /* (P - D) / max(1, |P|)                              */
+  double zero_one_accuracy; /* SVM: fraction of y_i x_i^T w > 0; Lasso: 0         */
+  double reg_norm;          /* Lasso ||x||_1; SVM sum alpha_i                     */
+  double sq_norm;           /* Lasso ||Ax-b||^2; SVM ||w||^2                      */
+  double max_abs_grad;      /* Lasso ||A^T r||_inf; SVM 0                         */
+  int64_t support;          /* nonzeros of x (alpha)                              */
+  int64_t active;           /* size of the q-shrinking active set                 */
+} acdc_eval;
+
+/* Work counters of the update kernel since the last reset. */
+typedef struct acdc_stats {
+  uint64_t updates;         /* coordinate updates                                 */
+  uint64_t nonzero_updates; /* updates whose step was nonzero                     */
+  uint64_t nnz_read;        /* matrix entries gathered                            */
+  uint64_t nnz_scattered;   /* matrix entries scattered into the residual         */
+  double update_ms;         /* device time of update kernels (CUDA events)        */
+  double eval_ms;           /* device time of refresh + gap kernels               */
+  int64_t update_launches;
+  int64_t eval_launches;
+} acdc_stats;
+
+typedef struct acdc_solve_result {
+  acdc_eval eval;
+  int32_t converged;
+  int32_t epochs;
+  double seconds;           /* host wall time of the call                         */
+  acdc_stats stats;
+} acdc_solve_result;
+
+typedef struct acdc_problem_info {
+  int64_t m, n, nnz, nnz_padded;
+  int64_t omega;            /* max entries per residual row                       */
+  double sigma;             /* ESO beta in use                                    */
+  double lambda;
+  int64_t device_bytes;
+  int32_t loss;
+  int32_t tau;
+} acdc_problem_info;
+
+/* ---- context ---------------------------------------------------------- */
+void acdc_settings_default(acdc_settings* s);
+int acdc_ctx_create(int device, acdc_ctx** out);
+int acdc_ctx_destroy(acdc_ctx* ctx);
+const char* acdc_last_error(const acdc_ctx* ctx);
+const char* acdc_status_string(int status);
+
+/* ---- problem upload (replaces InputOuputHelper::loadCSCData /
+ *      loadDistributedSparseSVMRowData feeding MulticoreEngineExecutor's
+ *      constructor, cpp/src/solver/MulticoreEngineExecutor.h:25-66) ------- */
+/* col_ptr: n+1 offsets; row_idx/vals: col_ptr[n] entries; rhs: b (loss 0, m
+ * entries) or y (loss 2, n entries, +-1).  Values are stored on the device as
+ * FP32 in 16-byte aligned column segments; x starts at 0. */
+int acdc_problem_create(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t* col_ptr,
+                        const int32_t* row_idx, const double* vals, const double* rhs,
+                        double lambda, acdc_problem** out);
+/* The same with the reference's ProblemData<int,double> index type. */
+int acdc_problem_create_i32(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n,
+                            const int32_t* col_ptr, const int32_t* row_idx, const double* vals,
+                            const double* rhs, double lambda, acdc_problem** out);
+int acdc_problem_destroy(acdc_problem* p);
+int acdc_problem_info_get(acdc_problem* p, acdc_problem_info* info);
+
+/* Settings: computes beta and the reciprocal Lipschitz constants
+ * Li = 1/(beta ||a_j||^2) (MulticoreSquareLoss.h:27-40 without, and
+ * MulticoreSVMDualLoss.h:48-61 with, the sigma factor). */
+int acdc_problem_set_settings(acdc_problem* p, const acdc_settings* s);
+int acdc_problem_set_lambda(acdc_problem* p, double lambda);
+
+/* ---- the engine (AbstractEngineExecutor, cpp/src/solver/AbstractEngineExecutor.h:14-37) */
+/* executeBulkOfIterations: n_updates sampled coordinate updates
+ * (MulticoreEngineExecutor.h:83-89 with the loss updates of
+ * MulticoreL1RegSquareLoss.h:41-63 / MulticoreSVMDualLoss.h:119-141).
+ * Asynchronous on the context's stream. */
+int acdc_run_updates(acdc_problem* p, uint64_t n_updates);
+/* recomputeResiduals in FP64 (MulticoreSquareLoss.h:42-53, MulticoreSVMDualLoss.h:31-46);
+ * the FP32 working residual is replaced by the rounded FP64 one. */
+int acdc_recompute_residuals(acdc_problem* p);
+/* FP64 refresh + objective and duality gap (MulticoreL1RegSquareLoss.h:30-39,
+ * MulticoreSVMDualLoss.h:63-117; the Lasso dual point is theta = -s r,
+ * s = min(1, lambda/||A^T r||_inf)).  Synchronises. */
+int acdc_evaluate(acdc_problem* p, acdc_eval* out);
+/* Bulks of refresh_every epochs, each followed by refresh + gap, until the gap
+ * target or max_epochs. */
+int acdc_solve(acdc_problem* p, acdc_solve_result* out);
+
+int acdc_get_x(acdc_problem* p, double* x);        /* n entries (alpha for loss 2) */
+int acdc_set_x(acdc_problem* p, const double* x);  /* warm start; refreshes r      */
+int acdc_get_residuals(acdc_problem* p, double* r);/* m entries: Ax-b or w, FP32 working copy */
+int acdc_get_stats(acdc_problem* p, acdc_stats* s);
+int acdc_reset_stats(acdc_problem* p);
+int acdc_synchronize(acdc_problem* p);
+
+/* Diagnostic: the coordinates the device sampler draws for updates
+ * k0 .. k0+count-1 of a solve keyed by seed over n coordinates (shrinking
+ * off); out receives count entries.  Lets a caller check the device stream
+ * against acdc_sample_coordinate (acdc_host.h). */
+int acdc_debug_sample(acdc_ctx* ctx, uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
+                      int64_t* out);
+
+/* ---- batched lambda paths (many instances, one launch sequence) --------- */
+typedef struct acdc_batch_options {
+  int32_t path_len;         /* lambdas per instance                               */
+  int32_t max_epochs;       /* per lambda                                         */
+  double gap_target;        /* per lambda, relative gap                           */
+  int32_t refresh_every;    /* epochs between gap checks                          */
+  int32_t autotune;         /* 1: choose tau / CTA packing per instance           */
+  int32_t tau_override;     /* > 0: fixed tau for every instance                  */
+  int32_t plain;            /* 1: solve one instance per launch sequence (baseline) */
+  int32_t reserved[8];
+} acdc_batch_options;
+
+typedef struct acdc_batch_result {
+  acdc_eval eval;           /* at the end of this lambda                          */
+  double lambda;
+  int32_t converged;
+  int32_t epochs;
+  int32_t tau;
+  int32_t reserved;
+} acdc_batch_result;
+
+/* Solves problems[i] along lambdas[i*path_len + k] (k = 0..path_len-1), each
+ * lambda warm-started from the previous solution (the pattern of
+ * cpp/src/experiments/lasso_console_solver.cpp:149-172).  results has
+ * count*path_len entries; x_out (optional) receives each problem's final x
+ * at x_out[i] (n_i entries each). */
+int acdc_batch_solve_path(acdc_ctx* ctx, int32_t count, acdc_problem* const* problems,
+                          const double* lambdas, const acdc_batch_options* opt,
+                          acdc_batch_result* results, double* const* x_out);
+
+/* ---- serving: continuous batching of solve requests -------------------- */
+typedef struct acdc_server_options {
+  int64_t memory_budget_bytes;  /* device bytes admitted at once                  */
+  int32_t max_slots;            /* requests on the device at once                 */
+  int32_t quantum_epochs;       /* epochs per scheduling round                    */
+  int32_t max_epochs;           /* per request                                    */
+  int32_t reserved[7];
+} acdc_server_options;
+
+typedef struct acdc_request {
+  int32_t loss;
+  int32_t reserved0;
+  int64_t m, n;
+  const int64_t* col_ptr;
+  const int32_t* row_idx;
+  const double* vals;
+  const double* rhs;
+  double lambda;
+  double gap_target;
+  uint64_t seed;
+} acdc_request;
+
+typedef struct acdc_request_result {
+  int32_t state;            /* 0 queued, 1 running, 2 done, 3 failed              */
+  int32_t converged;
+  int32_t epochs;
+  int32_t status;           /* ACDC_* code for failed requests                    */
+  acdc_eval eval;
+  double submit_time, start_time, finish_time; /* seconds, host monotonic clock   */
+} acdc_request_result;
+
+int acdc_server_create(acdc_ctx* ctx, const acdc_server_options* opt, acdc_server** out);
+/* Copies the request's arrays; returns a ticket.  ACDC_EBUSY if the request can
+ * never fit the memory budget. */
+int acdc_server_submit(acdc_server* s, const acdc_request* req, int64_t* ticket);
+/* Runs one scheduling round: admits queued requests that fit, advances every
+ * resident request by quantum_epochs, retires converged ones.  Returns the
+ * number of requests still queued or running in *pending. */
+int acdc_server_step(acdc_server* s, int32_t* pending);
+/* Result of a ticket; x (optional, n entries) once done.  A done ticket is
+ * released by acdc_server_release. */
+int acdc_server_poll(acdc_server* s, int64_t ticket, acdc_request_result* res, double* x);
+int acdc_server_release(acdc_server* s, int64_t ticket);
+int acdc_server_destroy(acdc_server* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ACDC_GPU_H_ */

@@ -1,0 +1,241 @@
+"""ctypes front end of the CPU checker (TEST INFRASTRUCTURE ONLY).
+
+Loads oracle/_build/libpcdm_oracle.so (the C restatement of the reference's
+PCDM hot path) and, when it was built, oracle/_ref/libacdc_ref.so (the
+reference's own multicore engine compiled from its sources).  Only tests, the
+smoke check and the CPU-baseline leg of bench.py use this module.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libpcdm_oracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libacdc_ref.so")
+REF_ROOT_DEFAULT = "/root/reference"
+
+_lib = None
+_ref = None
+
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+I64, U64, D, I = C.c_int64, C.c_uint64, C.c_double, C.c_int
+
+EVAL_KEYS = ("primal", "dual", "gap", "rel_gap", "zero_one_accuracy", "reg_norm", "sq_norm",
+             "max_abs_grad", "support")
+
+
+def build(ref_root=None):
+    """Compile the restatement (and the reference engine when its sources exist)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    root = ref_root or REF_ROOT_DEFAULT
+    if os.path.isdir(os.path.join(root, "cpp", "src")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF_ROOT=" + root], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.orc_philox4x32_10.argtypes = [u32p, u32p, u32p]
+        L.orc_sample.argtypes = [U64, U64, U64]
+        L.orc_sample.restype = U64
+        L.orc_lasso_lipschitz.argtypes = [I64, i64p, f64p, D, f64p]
+        L.orc_lasso_residuals.argtypes = [I64, I64, i64p, i32p, f64p, f64p, f64p, f64p]
+        L.orc_lasso_updates.argtypes = [I64, i64p, i32p, f64p, D, f64p, f64p, f64p, U64, U64, U64]
+        L.orc_lasso_eval.argtypes = [I64, I64, i64p, i32p, f64p, f64p, D, f64p, f64p, I, f64p]
+        L.orc_lasso_solve.argtypes = [I64, I64, i64p, i32p, f64p, f64p, D, D, U64, D, I, I64, I64,
+                                      f64p, f64p, f64p]
+        L.orc_lasso_solve.restype = I64
+        L.orc_svm_lipschitz.argtypes = [I64, i64p, f64p, D, f64p]
+        L.orc_svm_residuals.argtypes = [I64, I64, i64p, i32p, f64p, f64p, D, f64p, f64p]
+        L.orc_svm_updates.argtypes = [I64, i64p, i32p, f64p, f64p, D, f64p, f64p, f64p, U64, U64,
+                                      U64]
+        L.orc_svm_eval.argtypes = [I64, I64, i64p, i32p, f64p, f64p, D, f64p, f64p, I, f64p]
+        L.orc_svm_solve.argtypes = [I64, I64, i64p, i32p, f64p, f64p, D, D, U64, D, I64, I64, f64p,
+                                    f64p, f64p]
+        L.orc_svm_solve.restype = I64
+        L.orc_lasso_hogwild.argtypes = [I64, i64p, i32p, f64p, D, f64p, f64p, f64p, U64, U64, U64,
+                                        I]
+        L.orc_lasso_hogwild.restype = D
+        L.orc_svm_hogwild.argtypes = [I64, i64p, i32p, f64p, f64p, D, f64p, f64p, f64p, U64, U64,
+                                      U64, I]
+        L.orc_svm_hogwild.restype = D
+        L.orc_omega.argtypes = [I64, I64, i64p, i32p]
+        L.orc_omega.restype = I64
+        L.orc_eso_beta.argtypes = [D, D, D]
+        L.orc_eso_beta.restype = D
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's engine, or None when it was not built here."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        R = C.CDLL(REF_PATH)
+        R.ref_lasso_run.argtypes = [I, I, i32p, i32p, f64p, f64p, D, I, U64, I, C.c_ulong, f64p,
+                                    f64p, f64p]
+        R.ref_svm_run.argtypes = [I, I, i32p, i32p, f64p, f64p, D, D, I, U64, I, C.c_ulong, f64p,
+                                  f64p, f64p]
+        _ref = R
+    return _ref
+
+
+def _eval_dict(out):
+    return {k: float(v) for k, v in zip(EVAL_KEYS, out)}
+
+
+def philox(ctr, key):
+    out = np.zeros(4, np.uint32)
+    lib().orc_philox4x32_10(np.asarray(ctr, np.uint32), np.asarray(key, np.uint32), out)
+    return out
+
+
+def sample(seed, k, n):
+    return int(lib().orc_sample(seed, k, n))
+
+
+def omega(m, n, col_ptr, row_idx):
+    return int(lib().orc_omega(m, n, col_ptr, row_idx))
+
+
+def eso_beta(omega_, tau, n):
+    return float(lib().orc_eso_beta(omega_, tau, n))
+
+
+class Lasso:
+    """Serial FP64 restatement of MulticoreL1RegSquareLoss driven by the sampler."""
+
+    def __init__(self, m, n, col_ptr, row_idx, vals, b, lam, beta=1.0, x0=None):
+        self.m, self.n, self.lam = int(m), int(n), float(lam)
+        self.col_ptr = np.ascontiguousarray(col_ptr, np.int64)
+        self.row_idx = np.ascontiguousarray(row_idx, np.int32)
+        self.vals = np.ascontiguousarray(vals, np.float64)
+        self.b = np.ascontiguousarray(b, np.float64)
+        self.x = np.zeros(self.n) if x0 is None else np.array(x0, np.float64)
+        self.r = np.zeros(self.m)
+        self.Li = np.zeros(self.n)
+        lib().orc_lasso_lipschitz(self.n, self.col_ptr, self.vals, float(beta), self.Li)
+        self.refresh()
+        self.k = 0
+
+    def refresh(self):
+        lib().orc_lasso_residuals(self.m, self.n, self.col_ptr, self.row_idx, self.vals, self.b,
+                                  self.x, self.r)
+
+    def updates(self, count, seed):
+        lib().orc_lasso_updates(self.n, self.col_ptr, self.row_idx, self.vals, self.lam, self.Li,
+                                self.x, self.r, seed, self.k, int(count))
+        self.k += int(count)
+
+    def hogwild(self, count, seed, threads):
+        t = lib().orc_lasso_hogwild(self.n, self.col_ptr, self.row_idx, self.vals, self.lam,
+                                    self.Li, self.x, self.r, seed, self.k, int(count), threads)
+        self.k += int(count)
+        return t
+
+    def evaluate(self, threads=0):
+        out = np.zeros(9)
+        lib().orc_lasso_eval(self.m, self.n, self.col_ptr, self.row_idx, self.vals, self.b,
+                             self.lam, self.x, self.r, threads, out)
+        return _eval_dict(out)
+
+
+def lasso_solve(m, n, col_ptr, row_idx, vals, b, lam, beta=1.0, seed=1, target=1e-9, rel=False,
+                max_epochs=100000, check_every=1, x0=None):
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64)
+    r = np.zeros(m)
+    out = np.zeros(9)
+    ep = lib().orc_lasso_solve(m, n, np.ascontiguousarray(col_ptr, np.int64),
+                               np.ascontiguousarray(row_idx, np.int32),
+                               np.ascontiguousarray(vals, np.float64),
+                               np.ascontiguousarray(b, np.float64), lam, beta, seed, target,
+                               int(rel), max_epochs, check_every, x, r, out)
+    return x, r, _eval_dict(out), int(ep)
+
+
+class SVM:
+    """Serial FP64 restatement of MulticoreSVMDualLoss driven by the sampler."""
+
+    def __init__(self, d, n, row_ptr, col_idx, vals, y, lam, sigma=1.0, alpha0=None):
+        self.m, self.n, self.lam = int(d), int(n), float(lam)
+        self.row_ptr = np.ascontiguousarray(row_ptr, np.int64)
+        self.col_idx = np.ascontiguousarray(col_idx, np.int32)
+        self.vals = np.ascontiguousarray(vals, np.float64)
+        self.y = np.ascontiguousarray(y, np.float64)
+        self.x = np.zeros(self.n) if alpha0 is None else np.array(alpha0, np.float64)
+        self.r = np.zeros(self.m)
+        self.Li = np.zeros(self.n)
+        lib().orc_svm_lipschitz(self.n, self.row_ptr, self.vals, float(sigma), self.Li)
+        self.refresh()
+        self.k = 0
+
+    def refresh(self):
+        lib().orc_svm_residuals(self.m, self.n, self.row_ptr, self.col_idx, self.vals, self.y,
+                                self.lam, self.x, self.r)
+
+    def updates(self, count, seed):
+        lib().orc_svm_updates(self.n, self.row_ptr, self.col_idx, self.vals, self.y, self.lam,
+                              self.Li, self.x, self.r, seed, self.k, int(count))
+        self.k += int(count)
+
+    def hogwild(self, count, seed, threads):
+        t = lib().orc_svm_hogwild(self.n, self.row_ptr, self.col_idx, self.vals, self.y, self.lam,
+                                  self.Li, self.x, self.r, seed, self.k, int(count), threads)
+        self.k += int(count)
+        return t
+
+    def evaluate(self, threads=0):
+        out = np.zeros(9)
+        lib().orc_svm_eval(self.m, self.n, self.row_ptr, self.col_idx, self.vals, self.y,
+                           self.lam, self.x, self.r, threads, out)
+        return _eval_dict(out)
+
+
+def svm_solve(d, n, row_ptr, col_idx, vals, y, lam, sigma=1.0, seed=1, target=1e-9,
+              max_epochs=100000, check_every=1):
+    a = np.zeros(n)
+    w = np.zeros(d)
+    out = np.zeros(9)
+    ep = lib().orc_svm_solve(d, n, np.ascontiguousarray(row_ptr, np.int64),
+                             np.ascontiguousarray(col_idx, np.int32),
+                             np.ascontiguousarray(vals, np.float64),
+                             np.ascontiguousarray(y, np.float64), lam, sigma, seed, target,
+                             max_epochs, check_every, a, w, out)
+    return a, w, _eval_dict(out), int(ep)
+
+
+def ref_lasso(m, n, col_ptr, row_idx, vals, b, lam, seed, bulks, inner, threads=1):
+    """The reference engine's x, residuals and objective after each bulk."""
+    R = ref_lib()
+    if R is None:
+        return None
+    x = np.zeros(n)
+    r = np.zeros(m)
+    obj = np.zeros(bulks + 1)
+    R.ref_lasso_run(m, n, np.ascontiguousarray(col_ptr, np.int32),
+                    np.ascontiguousarray(row_idx, np.int32), np.ascontiguousarray(vals, np.float64),
+                    np.ascontiguousarray(b, np.float64), lam, threads, seed, bulks, inner, x, r, obj)
+    return x, r, obj
+
+
+def ref_svm(d, n, row_ptr, col_idx, vals, y, lam, sigma, seed, bulks, inner, threads=1):
+    """The reference engine's alpha, w and (gap, P, D, acc) after each bulk."""
+    R = ref_lib()
+    if R is None:
+        return None
+    a = np.zeros(n)
+    w = np.zeros(d)
+    ev = np.zeros(4 * (bulks + 1))
+    R.ref_svm_run(d, n, np.ascontiguousarray(row_ptr, np.int32),
+                  np.ascontiguousarray(col_idx, np.int32), np.ascontiguousarray(vals, np.float64),
+                  np.ascontiguousarray(y, np.float64), lam, sigma, threads, seed, bulks, inner, a, w,
+                  ev)
+    return a, w, ev.reshape(bulks + 1, 4)

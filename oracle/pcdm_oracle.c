@@ -1,0 +1,385 @@
+/*
+ * pcdm_oracle.c - CPU restatement of optml/ac-dc's PCDM hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the GPU library (tests, smoke
+ * check, CPU-baseline leg of the benchmark).  Never part of the product path.
+ *
+ * Each function restates a reference routine, cited by file:line relative to
+ * the reference project root.  The arithmetic keeps the reference's operation
+ * order so that the serial trajectory is bit-identical to the reference's
+ * engine run with one thread and the same coordinate sequence (compile with
+ * -ffp-contract=off so no multiply-add is fused).
+ */
+#include "pcdm_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ---- sampler ---- */
+
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+  uint32_t k0 = key[0], k1 = key[1];
+  for (int round = 0; round < 10; ++round) {
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+    uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+    uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+    c0 = n0;
+    c1 = (uint32_t)p1;
+    c2 = n2;
+    c3 = (uint32_t)p0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+
+uint64_t orc_sample(uint64_t seed, uint64_t k, uint64_t n) {
+  uint32_t ctr[4] = {(uint32_t)k, (uint32_t)(k >> 32), 0x5A3D0001u, 0u};
+  uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t o[4];
+  orc_philox4x32_10(ctr, key, o);
+  uint64_t u = ((uint64_t)o[0] << 32) | o[1];
+  return (uint64_t)(((unsigned __int128)u * n) >> 64);
+}
+
+/* sgn(X) (|X| - T)_+ : cpp/src/solver/treshhold_functions.h:27-33 with
+ * sgn from cpp/src/helpers/utils.h:29-32 (an int promoted to double). */
+static double soft_threshold(double T, double X) {
+  double a = fabs(X) - T;
+  if (a < 0) a = 0;
+  int s = (X > 0) - (X < 0);
+  return s * a;
+}
+
+/* ---- Lasso ---- */
+
+/* MulticoreSquareLoss::computeReciprocalLipConstants
+ * (cpp/src/solver/lossFunctions/squareLoss/MulticoreSquareLoss.h:27-40);
+ * beta = 1 reproduces the reference, which applies no ESO factor here. */
+void orc_lasso_lipschitz(int64_t n, const int64_t* col_ptr, const double* vals, double beta,
+                         double* Li) {
+  for (int64_t i = 0; i < n; ++i) {
+    double s = 0;
+    for (int64_t j = col_ptr[i]; j < col_ptr[i + 1]; ++j) s += vals[j] * vals[j];
+    Li[i] = s > 0 ? 1 / (beta * s) : 0;
+  }
+}
+
+/* MulticoreSquareLoss::recomputeResiduals (MulticoreSquareLoss.h:42-53): r = -b + A x. */
+void orc_lasso_residuals(int64_t m, int64_t n, const int64_t* col_ptr, const int32_t* row_idx,
+                         const double* vals, const double* b, const double* x, double* r) {
+  for (int64_t i = 0; i < m; ++i) r[i] = -b[i];
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t j = col_ptr[i]; j < col_ptr[i + 1]; ++j) r[row_idx[j]] += vals[j] * x[i];
+}
+
+/* One serial update: MulticoreL1RegSquareLoss::compute_update and
+ * performOneCoordinateUpdate (MulticoreL1RegSquareLoss.h:41-63). */
+static void lasso_update(int64_t idx, const int64_t* col_ptr, const int32_t* row_idx,
+                         const double* vals, double lambda, const double* Li, double* x,
+                         double* r) {
+  double tmp = 0;
+  for (int64_t j = col_ptr[idx]; j < col_ptr[idx + 1]; ++j) tmp += vals[j] * r[row_idx[j]];
+  tmp = soft_threshold(Li[idx] * lambda, x[idx] - Li[idx] * tmp) - x[idx];
+  x[idx] = x[idx] + tmp;
+  for (int64_t j = col_ptr[idx]; j < col_ptr[idx + 1]; ++j)
+    r[row_idx[j]] = r[row_idx[j]] + tmp * vals[j];
+}
+
+/* MulticoreEngineExecutor::executeBulkOfIterations (MulticoreEngineExecutor.h:83-89)
+ * with one thread: update k draws its coordinate from the counter-based sampler. */
+void orc_lasso_updates(int64_t n, const int64_t* col_ptr, const int32_t* row_idx,
+                       const double* vals, double lambda, const double* Li, double* x, double* r,
+                       uint64_t seed, uint64_t k0, uint64_t count) {
+  for (uint64_t k = 0; k < count; ++k) {
+    int64_t idx = (int64_t)orc_sample(seed, k0 + k, (uint64_t)n);
+    lasso_update(idx, col_ptr, row_idx, vals, lambda, Li, x, r);
+  }
+}
+
+/* Primal as MulticoreL1RegSquareLoss::computeObjectiveValue
+ * (MulticoreL1RegSquareLoss.h:30-39); the dual point u = s r with
+ * s = min(1, lambda/||A^T r||_inf) gives D = -s b^T r - s^2 ||r||^2 / 2. */
+void orc_lasso_eval(int64_t m, int64_t n, const int64_t* col_ptr, const int32_t* row_idx,
+                    const double* vals, const double* b, double lambda, const double* x,
+                    const double* r, int threads, double* out) {
+  double rr = 0, br = 0, l1 = 0, gmax = 0;
+  int64_t support = 0;
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#else
+  (void)threads;
+#endif
+#pragma omp parallel for schedule(static) reduction(+ : rr, br)
+  for (int64_t i = 0; i < m; ++i) {
+    rr += r[i] * r[i];
+    br += b[i] * r[i];
+  }
+#pragma omp parallel for schedule(static) reduction(+ : l1, support) reduction(max : gmax)
+  for (int64_t j = 0; j < n; ++j) {
+    double g = 0;
+    for (int64_t e = col_ptr[j]; e < col_ptr[j + 1]; ++e) g += vals[e] * r[row_idx[e]];
+    g = fabs(g);
+    if (g > gmax) gmax = g;
+    l1 += fabs(x[j]);
+    support += x[j] != 0;
+  }
+  double P = 0.5 * rr + lambda * l1;
+  double s = (gmax > lambda) ? lambda / gmax : 1.0;
+  double D = -s * br - 0.5 * s * s * rr;
+  out[0] = P;
+  out[1] = D;
+  out[2] = P - D;
+  out[3] = (P - D) / (fabs(P) > 1 ? fabs(P) : 1);
+  out[4] = 0;
+  out[5] = l1;
+  out[6] = rr;
+  out[7] = gmax;
+  out[8] = (double)support;
+}
+
+int64_t orc_lasso_solve(int64_t m, int64_t n, const int64_t* col_ptr, const int32_t* row_idx,
+                        const double* vals, const double* b, double lambda, double beta,
+                        uint64_t seed, double target, int rel, int64_t max_epochs,
+                        int64_t check_every, double* x, double* r, double* out) {
+  double* Li = (double*)malloc(sizeof(double) * (size_t)n);
+  orc_lasso_lipschitz(n, col_ptr, vals, beta, Li);
+  orc_lasso_residuals(m, n, col_ptr, row_idx, vals, b, x, r);
+  orc_lasso_eval(m, n, col_ptr, row_idx, vals, b, lambda, x, r, 0, out);
+  int64_t epochs = 0;
+  uint64_t k = 0;
+  if (check_every < 1) check_every = 1;
+  while ((rel ? out[3] : out[2]) > target && epochs < max_epochs) {
+    orc_lasso_updates(n, col_ptr, row_idx, vals, lambda, Li, x, r, seed, k,
+                      (uint64_t)(check_every * n));
+    k += (uint64_t)(check_every * n);
+    epochs += check_every;
+    orc_lasso_residuals(m, n, col_ptr, row_idx, vals, b, x, r);
+    orc_lasso_eval(m, n, col_ptr, row_idx, vals, b, lambda, x, r, 0, out);
+  }
+  free(Li);
+  return epochs;
+}
+
+/* ---- SVM dual ---- */
+
+/* MulticoreSVMDualLoss::computeReciprocalLipConstants (MulticoreSVMDualLoss.h:48-61). */
+void orc_svm_lipschitz(int64_t n, const int64_t* row_ptr, const double* vals, double sigma,
+                       double* Li) {
+  for (int64_t i = 0; i < n; ++i) {
+    double s = 0;
+    for (int64_t j = row_ptr[i]; j < row_ptr[i + 1]; ++j) s += vals[j] * vals[j];
+    Li[i] = s > 0 ? 1 / (sigma * s) : 0;
+  }
+}
+
+/* MulticoreSVMDualLoss::recomputeResiduals (MulticoreSVMDualLoss.h:31-46):
+ * clip alpha into [0,1], then w = (1/(lambda n)) sum_i y_i alpha_i x_i. */
+void orc_svm_residuals(int64_t m, int64_t n, const int64_t* row_ptr, const int32_t* col_idx,
+                       const double* vals, const double* y, double lambda, double* alpha,
+                       double* w) {
+  for (int64_t i = 0; i < m; ++i) w[i] = 0;
+  const double delta = 1 / (lambda * (double)n + 0.0);
+  for (int64_t s = 0; s < n; ++s) {
+    if (alpha[s] > 1) alpha[s] = 1;
+    if (alpha[s] < 0) alpha[s] = 0;
+    for (int64_t t = row_ptr[s]; t < row_ptr[s + 1]; ++t)
+      w[col_idx[t]] += delta * y[s] * vals[t] * alpha[s];
+  }
+}
+
+/* MulticoreSVMDualLoss::performOneCoordinateUpdate (MulticoreSVMDualLoss.h:119-141). */
+static void svm_update(int64_t idx, int64_t n, const int64_t* row_ptr, const int32_t* col_idx,
+                       const double* vals, const double* y, double lambda, const double* Li,
+                       double* alpha, double* w) {
+  double tmp = 0;
+  for (int64_t i = row_ptr[idx]; i < row_ptr[idx + 1]; ++i) tmp += vals[i] * w[col_idx[i]];
+  tmp = (1 - tmp * y[idx]) * lambda * (double)n * Li[idx];
+  if (tmp < -alpha[idx])
+    tmp = -alpha[idx];
+  else if (tmp > 1 - alpha[idx])
+    tmp = 1 - alpha[idx];
+  alpha[idx] = alpha[idx] + tmp;
+  const double delta = 1 / (lambda * (double)n);
+  for (int64_t j = row_ptr[idx]; j < row_ptr[idx + 1]; ++j)
+    w[col_idx[j]] = w[col_idx[j]] + tmp * vals[j] * y[idx] * delta;
+}
+
+void orc_svm_updates(int64_t n, const int64_t* row_ptr, const int32_t* col_idx,
+                     const double* vals, const double* y, double lambda, const double* Li,
+                     double* alpha, double* w, uint64_t seed, uint64_t k0, uint64_t count) {
+  for (uint64_t k = 0; k < count; ++k) {
+    int64_t idx = (int64_t)orc_sample(seed, k0 + k, (uint64_t)n);
+    svm_update(idx, n, row_ptr, col_idx, vals, y, lambda, Li, alpha, w);
+  }
+}
+
+/* MulticoreSVMDualLoss::computeObjectiveValue (MulticoreSVMDualLoss.h:63-117). */
+void orc_svm_eval(int64_t m, int64_t n, const int64_t* row_ptr, const int32_t* col_idx,
+                  const double* vals, const double* y, double lambda, const double* alpha,
+                  const double* w, int threads, double* out) {
+  double ww = 0, sum_loss = 0, sum_alpha = 0;
+  int64_t good = 0, support = 0;
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#else
+  (void)threads;
+#endif
+#pragma omp parallel for schedule(static) reduction(+ : ww)
+  for (int64_t i = 0; i < m; ++i) ww += w[i] * w[i];
+#pragma omp parallel for schedule(static) reduction(+ : sum_loss, sum_alpha, good, support)
+  for (int64_t j = 0; j < n; ++j) {
+    double err = 0;
+    for (int64_t i = row_ptr[j]; i < row_ptr[j + 1]; ++i) err += vals[i] * w[col_idx[i]];
+    if (y[j] * err > 0) good++;
+    err = 1 - y[j] * err;
+    if (err < 0) err = 0;
+    sum_loss += err;
+    sum_alpha += alpha[j];
+    support += alpha[j] != 0;
+  }
+  double P = lambda * 0.5 * ww + sum_loss / (0.0 + (double)n);
+  double D = -lambda * 0.5 * ww + sum_alpha / (0.0 + (double)n);
+  out[0] = P;
+  out[1] = D;
+  out[2] = P - D;
+  out[3] = (P - D) / (fabs(P) > 1 ? fabs(P) : 1);
+  out[4] = (double)good / (0.0 + (double)n);
+  out[5] = sum_alpha;
+  out[6] = ww;
+  out[7] = 0;
+  out[8] = (double)support;
+}
+
+int64_t orc_svm_solve(int64_t m, int64_t n, const int64_t* row_ptr, const int32_t* col_idx,
+                      const double* vals, const double* y, double lambda, double sigma,
+                      uint64_t seed, double target, int64_t max_epochs, int64_t check_every,
+                      double* alpha, double* w, double* out) {
+  double* Li = (double*)malloc(sizeof(double) * (size_t)n);
+  orc_svm_lipschitz(n, row_ptr, vals, sigma, Li);
+  orc_svm_residuals(m, n, row_ptr, col_idx, vals, y, lambda, alpha, w);
+  orc_svm_eval(m, n, row_ptr, col_idx, vals, y, lambda, alpha, w, 0, out);
+  int64_t epochs = 0;
+  uint64_t k = 0;
+  if (check_every < 1) check_every = 1;
+  while (out[2] > target && epochs < max_epochs) {
+    orc_svm_updates(n, row_ptr, col_idx, vals, y, lambda, Li, alpha, w, seed, k,
+                    (uint64_t)(check_every * n));
+    k += (uint64_t)(check_every * n);
+    epochs += check_every;
+    orc_svm_residuals(m, n, row_ptr, col_idx, vals, y, lambda, alpha, w);
+    orc_svm_eval(m, n, row_ptr, col_idx, vals, y, lambda, alpha, w, 0, out);
+  }
+  free(Li);
+  return epochs;
+}
+
+/* ---- asynchronous OpenMP form ---- */
+
+/* CAS-loop atomic add of cpp/src/parallel/parallel_essentials_posix.h:62-68. */
+static void atomic_add_double(double* var, double add) {
+  uint64_t* p = (uint64_t*)var;
+  uint64_t oldbits = __atomic_load_n(p, __ATOMIC_RELAXED);
+  for (;;) {
+    double oldv, newv;
+    memcpy(&oldv, &oldbits, sizeof oldv);
+    newv = oldv + add;
+    uint64_t newbits;
+    memcpy(&newbits, &newv, sizeof newbits);
+    if (__atomic_compare_exchange_n(p, &oldbits, newbits, 0, __ATOMIC_SEQ_CST, __ATOMIC_RELAXED))
+      return;
+  }
+}
+
+static double load_relaxed(const double* v) {
+  uint64_t bits = __atomic_load_n((const uint64_t*)v, __ATOMIC_RELAXED);
+  double d;
+  memcpy(&d, &bits, sizeof d);
+  return d;
+}
+
+static double wall_seconds(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+double orc_lasso_hogwild(int64_t n, const int64_t* col_ptr, const int32_t* row_idx,
+                         const double* vals, double lambda, const double* Li, double* x,
+                         double* r, uint64_t seed, uint64_t k0, uint64_t count, int threads) {
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#else
+  (void)threads;
+#endif
+  double t0 = wall_seconds();
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < (int64_t)count; ++k) {
+    int64_t idx = (int64_t)orc_sample(seed, k0 + (uint64_t)k, (uint64_t)n);
+    double tmp = 0;
+    for (int64_t j = col_ptr[idx]; j < col_ptr[idx + 1]; ++j)
+      tmp += vals[j] * load_relaxed(&r[row_idx[j]]);
+    double xi = load_relaxed(&x[idx]);
+    tmp = soft_threshold(Li[idx] * lambda, xi - Li[idx] * tmp) - xi;
+    atomic_add_double(&x[idx], tmp);
+    for (int64_t j = col_ptr[idx]; j < col_ptr[idx + 1]; ++j)
+      atomic_add_double(&r[row_idx[j]], tmp * vals[j]);
+  }
+  return wall_seconds() - t0;
+}
+
+double orc_svm_hogwild(int64_t n, const int64_t* row_ptr, const int32_t* col_idx,
+                       const double* vals, const double* y, double lambda, const double* Li,
+                       double* alpha, double* w, uint64_t seed, uint64_t k0, uint64_t count,
+                       int threads) {
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#else
+  (void)threads;
+#endif
+  const double delta = 1 / (lambda * (double)n);
+  double t0 = wall_seconds();
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < (int64_t)count; ++k) {
+    int64_t idx = (int64_t)orc_sample(seed, k0 + (uint64_t)k, (uint64_t)n);
+    double tmp = 0;
+    for (int64_t i = row_ptr[idx]; i < row_ptr[idx + 1]; ++i)
+      tmp += vals[i] * load_relaxed(&w[col_idx[i]]);
+    double ai = load_relaxed(&alpha[idx]);
+    tmp = (1 - tmp * y[idx]) * lambda * (double)n * Li[idx];
+    if (tmp < -ai)
+      tmp = -ai;
+    else if (tmp > 1 - ai)
+      tmp = 1 - ai;
+    atomic_add_double(&alpha[idx], tmp);
+    for (int64_t j = row_ptr[idx]; j < row_ptr[idx + 1]; ++j)
+      atomic_add_double(&w[col_idx[j]], tmp * vals[j] * y[idx] * delta);
+  }
+  return wall_seconds() - t0;
+}
+
+int64_t orc_omega(int64_t m, int64_t n, const int64_t* col_ptr, const int32_t* row_idx) {
+  int64_t* cnt = (int64_t*)calloc((size_t)m, sizeof(int64_t));
+  int64_t w = 1; /* the reference starts from omega = 1 (MultiCoreSolver.cpp:24) */
+  for (int64_t e = 0; e < col_ptr[n]; ++e) {
+    int64_t c = ++cnt[row_idx[e]];
+    if (c > w) w = c;
+  }
+  free(cnt);
+  return w;
+}
+
+double orc_eso_beta(double omega, double tau, double n) {
+  if (n <= 1) return 1.0;
+  return 1 + (omega - 1) * (tau - 1) / (n - 1.0);
+}

@@ -1,0 +1,163 @@
+"""Host-side logic without a GPU: generators, loaders, the C-ABI export list
+and argument checking that happens before any device work."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import acdc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions(header):
+    text = open(os.path.join(ROOT, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(acdc_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.mark.parametrize("header,lib", [("acdc_gpu.h", acdc.GPU_LIB), ("acdc_host.h", acdc.HOST_LIB)])
+def test_library_exports_every_declared_symbol(header, lib):
+    names = declared_functions(header)
+    assert len(names) > 5
+    L = C.CDLL(lib)
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_gpu_library_loads_and_reports_no_device_cleanly():
+    L = acdc.gpu_lib()
+    s = acdc.default_settings()
+    assert s.tau == 4096 and s.refresh_every == 5 and s.gap_relative == 1
+    assert L.acdc_status_string(acdc.EUNSUPPORTED) == b"unsupported loss"
+    h = acdc.VP()
+    rc = L.acdc_ctx_create(0, C.byref(h))
+    import torch
+    if not torch.cuda.is_available():
+        assert rc == acdc.ENODEV
+
+
+def test_generator_is_deterministic_and_thread_independent():
+    a = acdc.gen_lasso(500, 2000, nnz_per_col=7, n_star=30, seed=42, threads=1)
+    b = acdc.gen_lasso(500, 2000, nnz_per_col=7, n_star=30, seed=42, threads=4)
+    for f in ("col_ptr", "row_idx", "vals", "rhs"):
+        assert np.array_equal(getattr(a, f), getattr(b, f))
+    assert a.lam == b.lam
+    c = acdc.gen_lasso(500, 2000, nnz_per_col=7, n_star=30, seed=43)
+    assert not np.array_equal(a.vals, c.vals)
+
+
+def test_lasso_generator_properties():
+    m, n = 1000, 3000
+    inst = acdc.gen_lasso(m, n, nnz_per_col=20, n_star=100, noise_sigma=0.01, lambda_frac=0.1, seed=7)
+    cp, ri, va = inst.col_ptr, inst.row_idx, inst.vals
+    assert cp[0] == 0 and cp[-1] == 20 * n
+    for j in range(0, n, 97):
+        rows = ri[cp[j]:cp[j + 1]]
+        assert np.all(np.diff(rows) > 0) and rows.min() >= 0 and rows.max() < m
+        assert abs(np.linalg.norm(va[cp[j]:cp[j + 1]]) - 1) < 1e-12
+    assert np.count_nonzero(inst.x_star) == 100
+    assert set(np.unique(inst.x_star[inst.x_star != 0])) <= {-1.0, 1.0}
+    # lambda = 0.1 ||A^T b||_inf
+    g = np.zeros(n)
+    for j in range(n):
+        g[j] = va[cp[j]:cp[j + 1]] @ inst.rhs[ri[cp[j]:cp[j + 1]]]
+    assert abs(inst.lam - 0.1 * np.abs(g).max()) < 1e-12
+
+
+def test_zipf_column_lengths_have_requested_mean_and_range():
+    inst = acdc.gen_lasso(100000, 200000, nnz_mode=acdc.NNZ_ZIPF, zipf_s=1.5, nnz_min=1,
+                          nnz_max=2000, nnz_mean=20.0, n_star=10, seed=9)
+    lens = np.diff(inst.col_ptr)
+    assert lens.min() >= 1 and lens.max() <= 2000
+    assert abs(lens.mean() - 20.0) < 1.0
+    assert (lens == 1).mean() > 0.2  # heavy head of single-entry columns
+
+
+def test_svm_generator_properties():
+    inst = acdc.gen_svm(300, 5000, nnz_median=60, nnz_sigma=0.8, w_star_nnz=200, flip_prob=0.05,
+                        lam=1e-3, seed=3)
+    rp, ci, va = inst.col_ptr, inst.row_idx, inst.vals
+    assert set(np.unique(inst.rhs)) <= {-1.0, 1.0}
+    for i in range(0, 300, 31):
+        v = va[rp[i]:rp[i + 1]]
+        assert np.all(v > 0) and abs(np.linalg.norm(v) - 1) < 1e-12
+        assert np.all(np.diff(ci[rp[i]:rp[i + 1]]) > 0)
+    med = np.median(np.diff(rp))
+    assert 40 < med < 90
+
+
+def test_nesterov_generator_support_and_optimality():
+    inst = acdc.gen_nesterov(200, 500, 5, 25, lam=1.0, rho=1.0, seed=2)
+    cp, ri, va = inst.col_ptr, inst.row_idx, inst.vals
+    r = -inst.rhs.copy()
+    for j in range(inst.n):
+        r[ri[cp[j]:cp[j + 1]]] += va[cp[j]:cp[j + 1]] * inst.x_star[j]
+    g = np.array([va[cp[j]:cp[j + 1]] @ r[ri[cp[j]:cp[j + 1]]] for j in range(inst.n)])
+    sup = inst.x_star != 0
+    assert sup.sum() == 25
+    # optimality: a_j^T r = -lambda sign(x_j) on the support, |a_j^T r| <= 0.9 lambda off it
+    np.testing.assert_allclose(g[sup], -np.sign(inst.x_star[sup]), atol=1e-12)
+    assert np.abs(g[~sup]).max() <= 0.9 + 1e-12
+    f = 0.5 * r @ r + np.abs(inst.x_star).sum()
+    assert abs(f - inst.f_star) < 1e-10
+
+
+def test_mix_sizes_are_log_uniform_in_range():
+    ms, ns = zip(*[acdc.mix_sizes(77, i) for i in range(400)])
+    assert min(ms) >= 500 and max(ms) <= 50000 and min(ns) >= 1000 and max(ns) <= 200000
+    assert 0.3 < np.mean(np.log(ms) < np.log(5000)) < 0.7
+
+
+def test_csc_text_loader_roundtrip(tmp_path):
+    inst = acdc.gen_lasso(40, 60, nnz_per_col=3, n_star=5, seed=1)
+    pre = str(tmp_path / "A")
+    np.savetxt(pre + "_values.txt", inst.vals, fmt="%.17g")
+    np.savetxt(pre + "_colPtr.txt", inst.col_ptr, fmt="%d")
+    np.savetxt(pre + "_rowIdx.txt", inst.row_idx, fmt="%d")
+    np.savetxt(str(tmp_path / "b.txt"), inst.rhs, fmt="%.17g")
+    got = acdc.load_csc_text(pre, str(tmp_path / "b.txt"), 0.5)
+    assert np.array_equal(got.col_ptr, inst.col_ptr)
+    assert np.array_equal(got.row_idx, inst.row_idx)
+    assert np.array_equal(got.vals, inst.vals) and np.array_equal(got.rhs, inst.rhs)
+    # a final value without a trailing newline is kept
+    with open(pre + "_values.txt", "w") as f:
+        f.write(" ".join("%.17g" % v for v in inst.vals))
+    assert np.array_equal(acdc.load_csc_text(pre, str(tmp_path / "b.txt"), 0.5).vals, inst.vals)
+
+
+def test_csc_text_loader_rejects_bad_input(tmp_path):
+    pre = str(tmp_path / "A")
+    open(pre + "_values.txt", "w").write("1 2 3\n")
+    open(pre + "_colPtr.txt", "w").write("0 2 3\n")
+    open(pre + "_rowIdx.txt", "w").write("0 5 1\n")  # row 5 out of range for m = 2
+    open(str(tmp_path / "b.txt"), "w").write("1 1\n")
+    with pytest.raises(acdc.AcdcError):
+        acdc.load_csc_text(pre, str(tmp_path / "b.txt"), 1.0)
+    with pytest.raises(acdc.AcdcError):
+        acdc.load_csc_text(str(tmp_path / "missing"), str(tmp_path / "b.txt"), 1.0)
+
+
+def test_libsvm_loader(tmp_path):
+    p = tmp_path / "d.svm"
+    p.write_text("+1 1:0.5 3:1.5\n-1 2:2\n\n0 1:1 4:-1\n")
+    inst = acdc.load_libsvm(str(p), 0.1)
+    assert inst.n == 3 and inst.m == 4 and inst.nnz == 5
+    assert inst.col_ptr.tolist() == [0, 2, 3, 5]
+    assert inst.row_idx.tolist() == [0, 2, 1, 0, 3]
+    assert inst.vals.tolist() == [0.5, 1.5, 2.0, 1.0, -1.0]
+    assert inst.rhs.tolist() == [1.0, -1.0, -1.0]
+    p.write_text("+1 0:1\n")  # indices are 1-based
+    with pytest.raises(acdc.AcdcError):
+        acdc.load_libsvm(str(p), 0.1)
+
+
+def test_host_omega_matches_oracle():
+    import oracle
+    inst = acdc.gen_lasso(300, 900, nnz_per_col=9, n_star=5, seed=12)
+    assert acdc.host_omega(inst) == oracle.omega(inst.m, inst.n, inst.col_ptr, inst.row_idx)
+    assert abs(oracle.eso_beta(10, 1, 900) - 1.0) < 1e-15
+    assert abs(oracle.eso_beta(10, 4096, 1e7) - (1 + 9 * 4095 / (1e7 - 1))) < 1e-15

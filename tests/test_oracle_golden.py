@@ -1,0 +1,162 @@
+"""The CPU oracle pinned against the reference: golden trajectories written by
+the reference's own multicore engine (tests/golden/make_golden.py) and, where
+the reference was compiled here, direct bit-for-bit comparisons."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import acdc
+import oracle
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def test_philox_known_answers_oracle_and_device_header():
+    kat = json.load(open(os.path.join(GOLDEN, "philox_kat.json")))
+    for case in kat["cases"]:
+        want = np.array(case["out"], np.uint32)
+        assert np.array_equal(oracle.philox(case["ctr"], case["key"]), want)
+        # the header the device sampler is compiled from, through the host library
+        assert np.array_equal(acdc.philox_host(case["ctr"], case["key"]), want)
+
+
+def test_sampler_streams_agree():
+    for seed in (0, 1, 0xACDC0001, 2**63 + 5):
+        for n in (1, 7, 10000, 10**7, 2**40 + 3):
+            for k in (0, 1, 2, 1000, 2**33 + 1):
+                assert acdc.sample_coordinate(seed, k, n) == oracle.sample(seed, k, n)
+                assert 0 <= oracle.sample(seed, k, n) < n
+
+
+def test_sampler_is_uniform():
+    n, draws = 97, 97 * 2000
+    counts = np.bincount([oracle.sample(3, k, n) for k in range(draws)], minlength=n)
+    chi2 = ((counts - draws / n) ** 2 / (draws / n)).sum()
+    assert chi2 < 200  # 96 degrees of freedom; p ~ 1e-9 at 200
+
+
+def test_lasso_trajectory_matches_reference_engine_bit_for_bit():
+    g = load("lasso_traj.npz")
+    L = oracle.Lasso(int(g["m"]), int(g["n"]), g["col_ptr"], g["row_idx"], g["vals"], g["b"],
+                     float(g["lam"]))
+    objs = [L.evaluate()["primal"]]
+    for _ in range(int(g["bulks"])):
+        L.updates(int(g["inner"]), int(g["seed"]))
+        objs.append(L.evaluate()["primal"])
+    assert np.array_equal(L.x, g["x"])
+    assert np.array_equal(L.r, g["r"])
+    # objective: the reference squares a norm, the oracle sums squares
+    np.testing.assert_allclose(objs, g["obj"], rtol=1e-13)
+
+
+def test_svm_trajectory_matches_reference_engine_bit_for_bit():
+    g = load("svm_traj.npz")
+    S = oracle.SVM(int(g["d"]), int(g["n"]), g["row_ptr"], g["col_idx"], g["vals"], g["y"],
+                   float(g["lam"]), float(g["sigma"]))
+    evs = [S.evaluate()]
+    for _ in range(int(g["bulks"])):
+        S.updates(int(g["inner"]), int(g["seed"]))
+        evs.append(S.evaluate())
+    assert np.array_equal(S.x, g["alpha"])
+    assert np.array_equal(S.r, g["w"])
+    got = np.array([[e["gap"], e["primal"], e["dual"], e["zero_one_accuracy"]] for e in evs])
+    np.testing.assert_allclose(got, g["evals"], rtol=1e-12, atol=1e-14)
+
+
+def _config0():
+    rec = json.load(open(os.path.join(GOLDEN, "lasso_config0.json")))
+    g = rec["generator"]
+    inst = acdc.gen_lasso(g["m"], g["n"], nnz_per_col=g["nnz_per_col"], n_star=g["n_star"],
+                          noise_sigma=g["noise_sigma"], lambda_frac=g["lambda_frac"], seed=g["seed"])
+    h = hashlib.sha256()
+    for a in (inst.col_ptr, inst.row_idx, inst.vals, inst.rhs):
+        h.update(np.ascontiguousarray(a).tobytes())
+    h.update(np.float64(inst.lam).tobytes())
+    return rec, inst, h.hexdigest()
+
+
+def test_config0_oracle_solution_matches_reference_solution():
+    rec, inst, digest = _config0()
+    if digest != rec["input_sha256"]:
+        pytest.skip("generator output differs on this machine's libm; fixture not applicable")
+    x, r, ev, ep = oracle.lasso_solve(inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals,
+                                      inst.rhs, inst.lam, seed=rec["sampler_seed"], target=1e-9)
+    assert ev["gap"] <= 1e-9
+    assert abs(ev["primal"] - rec["objective"]) <= 1e-9 * abs(rec["objective"])
+    assert np.nonzero(x)[0].tolist() == rec["support"]
+    np.testing.assert_allclose(x[rec["support"]], rec["x_support"], rtol=1e-6, atol=1e-9)
+
+
+def test_oracle_solvers_reach_tight_gaps():
+    inst = acdc.gen_lasso(150, 600, nnz_per_col=5, n_star=10, lambda_frac=0.2, seed=3)
+    x, r, ev, ep = oracle.lasso_solve(inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals,
+                                      inst.rhs, inst.lam, seed=9, target=1e-10)
+    assert ev["gap"] <= 1e-10 and ev["gap"] >= -1e-12
+    sv = acdc.gen_svm(120, 700, nnz_median=25, w_star_nnz=80, lam=1e-2, seed=4)
+    a, w, ev, ep = oracle.svm_solve(sv.m, sv.n, sv.col_ptr, sv.row_idx, sv.vals, sv.rhs, sv.lam,
+                                    seed=2, target=1e-10)
+    assert ev["gap"] <= 1e-10
+    assert np.all((a >= 0) & (a <= 1))
+
+
+def test_nesterov_known_optimum():
+    inst = acdc.gen_nesterov(300, 800, 6, 40, lam=1.0, rho=1.0, seed=21)
+    x, r, ev, ep = oracle.lasso_solve(inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals,
+                                      inst.rhs, inst.lam, seed=1, target=1e-11)
+    assert abs(ev["primal"] - inst.f_star) <= 1e-8 * inst.f_star
+    assert set(np.nonzero(x)[0]) == set(np.nonzero(inst.x_star)[0])
+    np.testing.assert_allclose(x, inst.x_star, atol=1e-5)
+
+
+ref_needed = pytest.mark.skipif(oracle.ref_lib() is None if os.path.exists(oracle.REF_PATH) else True,
+                                reason="reference engine not compiled here (needs the reference sources)")
+
+
+@ref_needed
+@pytest.mark.parametrize("shape", [(50, 200, 3), (400, 300, 1), (30, 90, 30)])
+def test_oracle_equals_reference_engine_on_random_cases(shape):
+    m, n, k = shape
+    inst = acdc.gen_lasso(m, n, nnz_per_col=k, n_star=min(10, n), lambda_frac=0.15, seed=m + n)
+    cp = inst.col_ptr.copy()
+    # edge cases: an empty column and a column holding every row
+    rows = [list(inst.row_idx[cp[j]:cp[j + 1]]) for j in range(n)]
+    vals = [list(inst.vals[cp[j]:cp[j + 1]]) for j in range(n)]
+    rows[1], vals[1] = [], []
+    rows[2] = list(range(m))
+    vals[2] = list(np.linspace(-1, 1, m) / np.sqrt(m))
+    cp = np.concatenate([[0], np.cumsum([len(r) for r in rows])]).astype(np.int64)
+    ri = np.array([i for r in rows for i in r], np.int32)
+    va = np.array([v for vv in vals for v in vv])
+    x, rr, obj = oracle.ref_lasso(m, n, cp.astype(np.int32), ri, va, inst.rhs, inst.lam, 99, 4, 3 * n)
+    L = oracle.Lasso(m, n, cp, ri, va, inst.rhs, inst.lam)
+    for _ in range(4):
+        L.updates(3 * n, 99)
+    assert np.array_equal(x, L.x) and np.array_equal(rr, L.r)
+
+
+@ref_needed
+def test_svm_oracle_equals_reference_engine_with_sigma():
+    sv = acdc.gen_svm(80, 400, nnz_median=20, w_star_nnz=50, lam=5e-3, seed=8)
+    sigma = 1.7
+    a, w, ev = oracle.ref_svm(sv.m, sv.n, sv.col_ptr.astype(np.int32), sv.row_idx, sv.vals, sv.rhs,
+                              sv.lam, sigma, 5, 3, 200)
+    S = oracle.SVM(sv.m, sv.n, sv.col_ptr, sv.row_idx, sv.vals, sv.rhs, sv.lam, sigma)
+    for _ in range(3):
+        S.updates(200, 5)
+    assert np.array_equal(a, S.x) and np.array_equal(w, S.r)
+
+
+def test_hogwild_single_thread_is_the_serial_trajectory():
+    inst = acdc.gen_lasso(100, 400, nnz_per_col=4, n_star=8, seed=5)
+    A = oracle.Lasso(inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals, inst.rhs, inst.lam)
+    B = oracle.Lasso(inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals, inst.rhs, inst.lam)
+    A.updates(5000, 4)
+    B.hogwild(5000, 4, threads=1)
+    assert np.array_equal(A.x, B.x) and np.array_equal(A.r, B.r)
