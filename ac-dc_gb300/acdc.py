@@ -18,6 +18,7 @@ OK, EINVAL, ENOMEM, EUNSUPPORTED, ECUDA, ETIMEOUT, EDEVICE, EBUSY, ENOTFOUND, EN
     0, -1, -2, -3, -4, -5, -6, -7, -8, -9)
 LOSS_L1_SQUARE, LOSS_L2_SQUARE, LOSS_SVM_DUAL, LOSS_LOGISTIC = 0, 1, 2, 3
 NNZ_FIXED, NNZ_ZIPF, NNZ_UNIFORM = 0, 1, 2
+PREC_AUTO, PREC_FP32, PREC_FP64 = 0, 1, 2
 
 I32, I64, U64, D = C.c_int32, C.c_int64, C.c_uint64, C.c_double
 VP = C.c_void_p
@@ -27,7 +28,9 @@ class Settings(C.Structure):
     _fields_ = [("loss", I32), ("tau", I32), ("warps_per_block", I32), ("refresh_every", I32),
                 ("seed", U64), ("sigma", D), ("gap_target", D), ("gap_relative", I32),
                 ("max_epochs", I32), ("use_shrinking", I32), ("shrinking_starting_iter", I32),
-                ("shrinking_probability", D), ("shrink_eps", D), ("reserved", I32 * 8)]
+                ("shrinking_probability", D), ("shrink_eps", D), ("precision", I32),
+                ("tau_active", I32), ("polish_rel_gap", D), ("active_passes", I32),
+                ("reserved", I32 * 3)]
 
 
 class Eval(C.Structure):
@@ -50,12 +53,13 @@ class Stats(C.Structure):
 
 class SolveResult(C.Structure):
     _fields_ = [("eval", Eval), ("converged", I32), ("epochs", I32), ("seconds", D),
-                ("stats", Stats)]
+                ("stats", Stats), ("device_ms", D), ("fp64_epochs", I32), ("reserved", I32)]
 
 
 class ProblemInfo(C.Structure):
     _fields_ = [("m", I64), ("n", I64), ("nnz", I64), ("nnz_padded", I64), ("omega", I64),
-                ("sigma", D), ("lambda_", D), ("device_bytes", I64), ("loss", I32), ("tau", I32)]
+                ("sigma", D), ("lambda_", D), ("device_bytes", I64), ("loss", I32), ("tau", I32),
+                ("omega_active", I64), ("active_step_scale", D), ("long_columns", I64)]
 
 
 class BatchOptions(C.Structure):
@@ -135,6 +139,7 @@ def gpu_lib():
         L.acdc_recompute_residuals.argtypes = [VP]
         L.acdc_evaluate.argtypes = [VP, C.POINTER(Eval)]
         L.acdc_solve.argtypes = [VP, C.POINTER(SolveResult)]
+        L.acdc_problem_reset.argtypes = [VP]
         L.acdc_get_x.argtypes = [VP, VP]
         L.acdc_set_x.argtypes = [VP, VP]
         L.acdc_get_residuals.argtypes = [VP, VP]
@@ -319,8 +324,8 @@ class Context:
         return rc
 
     def close(self):
-        if self.h:
-            self.L.acdc_ctx_destroy(self.h)
+        """Destroys the context once no problem created on it is alive."""
+        if self.h and self.L.acdc_ctx_destroy(self.h) == OK:
             self.h = None
 
     def __del__(self):
@@ -411,6 +416,9 @@ class Problem:
         r = SolveResult()
         self.ctx.check(self.L.acdc_solve(self.h, C.byref(r)))
         return r
+
+    def reset(self):
+        self.ctx.check(self.L.acdc_problem_reset(self.h))
 
     def get_x(self):
         x = np.zeros(self.n)

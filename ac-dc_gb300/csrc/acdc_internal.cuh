@@ -38,13 +38,15 @@ enum {
   CNT_STATUS = 6,      // device-side error flags (DEV_ERR_*)
   CNT_K_BASE = 7,      // sampler counter of the next update (graph-friendly)
   CNT_GMAX_BITS = 8,   // max |a_j^T r| as FP64 bits (non-negative, so integer max works)
+  CNT_OMEGA_ACTIVE = 9,// max entries per residual row over the active columns
+  CNT_NLONG = 10,      // number of columns with more than 32 entries
   CNT_SLOTS = 16
 };
 
 enum { DEV_ERR_BAD_INDEX = 1, DEV_ERR_BAD_LAYOUT = 2, DEV_ERR_BAD_STATE = 4 };
 
 // Fixed grid for the reductions, so partial sums are combined in a fixed order.
-#define ACDC_RED_BLOCKS 608
+#define ACDC_RED_BLOCKS 1216
 #define ACDC_RED_THREADS 256
 #define ACDC_NPART 8  // partial slots per block
 
@@ -56,14 +58,18 @@ struct UpdateParams {
   float* r;
   const int32_t* active;
   unsigned long long* counters;
+  double* x64;          // FP64 coordinates (polish mode)
+  double* r64;          // FP64 residual (polish mode)
   int64_t n;
   uint64_t count;       // updates in this launch
   uint64_t seed;
-  float lambda;         // Lasso: lambda; SVM: lambda * n
-  float inv_lambda_n;   // SVM scatter factor 1/(lambda n)
+  double lambda_d;      // Lasso: lambda; SVM: lambda * n
+  double inv_lambda_n_d;// SVM scatter factor 1/(lambda n)
+  double li_scale;      // multiplies the stored Li (1 unless beta changes)
   uint32_t shrink_q32;  // probability of an active-set draw, scaled by 2^32 (0 = off)
   int32_t n_warps;      // tau
   int32_t loss;
+  int32_t fp64;         // 1: x and r in FP64 (x64, r64)
 };
 
 // Parameters of the evaluation kernels.
@@ -78,6 +84,9 @@ struct EvalParams {
   unsigned long long* counters;
   double* part;         // ACDC_RED_BLOCKS * ACDC_NPART
   double* eval_out;     // 16 doubles
+  double* x64;          // FP64 coordinates when in polish mode, else nullptr (x in meta.w)
+  const int32_t* long_cols;  // columns with more than 32 entries
+  int64_t n_long;
   int64_t m, n;
   double lambda;
   double shrink_thresh; // Lasso: (1-eps) lambda
@@ -94,7 +103,11 @@ struct DevProblem {
   double* rhs64 = nullptr;
   double* col_sq = nullptr;
   int32_t* active = nullptr;
-  float* xbuf = nullptr;    // n floats: staging for x up/downloads
+  double* x64 = nullptr;    // n doubles: coordinates in polish mode
+  int32_t* rowcnt = nullptr;// m ints: per-row counts of active columns
+  int32_t* long_cols = nullptr;  // columns with more than 32 entries (n_long of them)
+  int64_t n_long = 0;
+  double* xbuf = nullptr;   // n doubles: staging for x up/downloads
   double* part = nullptr;
   double* eval_out = nullptr;
   unsigned long long* counters = nullptr;
@@ -105,8 +118,9 @@ struct acdc_ctx {
   int device = 0;
   int sm_count = 0;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   std::string last_error;
+  int64_t live_problems = 0;  // problems (and servers) created on this context
 };
 
 struct acdc_problem {
@@ -119,7 +133,13 @@ struct acdc_problem {
   int64_t omega = 1;
   uint64_t k_next = 0;      // sampler counter of the next update
   int64_t epochs_done = 0;  // epochs since the start (shrinking starts after a few)
+  uint64_t updates_done = 0;
   bool active_valid = false;
+  bool fp64_mode = false;   // x and r kept in FP64 (polish stage or precision FP64)
+  // Step scale while sampling from the active set: beta / max(beta, beta_A) with
+  // beta_A the ESO parameter of q*tau draws over the active columns.
+  double li_scale_shrink = 1.0;
+  int64_t omega_active = 1;
   acdc_stats stats;
   double* h_eval = nullptr;               // pinned, 16 doubles
   unsigned long long* h_counters = nullptr;  // pinned, CNT_SLOTS
@@ -148,11 +168,20 @@ cudaError_t launch_max_i32(const int32_t* v, int64_t len, unsigned long long* ou
                            cudaStream_t st);
 cudaError_t launch_widen_i32(const int32_t* src, int64_t* dst, int64_t len, cudaStream_t st);
 cudaError_t launch_set_li(const DevProblem& d, int32_t loss, double beta, cudaStream_t st);
-cudaError_t launch_set_x(const DevProblem& d, const float* x32, cudaStream_t st);
-cudaError_t launch_get_x(const DevProblem& d, float* x32, cudaStream_t st);
+// x: host-order doubles in d.xbuf <-> FP32 meta.w (and FP64 x64 when fp64).
+cudaError_t launch_set_x(const DevProblem& d, bool fp64, cudaStream_t st);
+cudaError_t launch_get_x(const DevProblem& d, bool fp64, cudaStream_t st);
+// Polish-mode transitions: x64 = (double) meta.w, or meta.w = (float) x64.
+cudaError_t launch_x32_to_x64(const DevProblem& d, cudaStream_t st);
+cudaError_t launch_x64_to_x32(const DevProblem& d, cudaStream_t st);
 cudaError_t launch_update(const UpdateParams& p, uint64_t k_base, int warps_per_block,
                           cudaStream_t st);
 cudaError_t launch_refresh(const EvalParams& p, cudaStream_t st);
+// Lists the columns with more than 32 entries into list; count (device) gets their number.
+cudaError_t launch_list_long(const DevProblem& d, int32_t* list, unsigned long long* count,
+                             cudaStream_t st);
+// omega over the active list (counters[CNT_OMEGA_ACTIVE]); rowcnt holds m ints.
+cudaError_t launch_active_omega(const EvalParams& p, int32_t* rowcnt, cudaStream_t st);
 cudaError_t launch_gap(const EvalParams& p, cudaStream_t st);
 cudaError_t launch_debug_sample(uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
                                 int64_t* out, cudaStream_t st);

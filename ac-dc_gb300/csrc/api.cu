@@ -57,6 +57,8 @@ extern "C" void acdc_settings_default(acdc_settings* s) {
   s->shrinking_starting_iter = 2;
   s->shrinking_probability = 0.9;
   s->shrink_eps = 0.1;
+  s->precision = ACDC_PREC_AUTO;
+  s->polish_rel_gap = 1e-5;
 }
 
 // ---- context ----
@@ -72,7 +74,7 @@ extern "C" int acdc_ctx_create(int device, acdc_ctx** out) {
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
-  for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
+  for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
   if (e != cudaSuccess) {
     delete ctx;
     return ACDC_ECUDA;
@@ -83,8 +85,10 @@ extern "C" int acdc_ctx_create(int device, acdc_ctx** out) {
 
 extern "C" int acdc_ctx_destroy(acdc_ctx* ctx) {
   if (!ctx) return ACDC_EINVAL;
+  if (ctx->live_problems > 0)
+    return acdc_set_error(ctx, ACDC_EBUSY, "destroy every problem of the context first");
   cudaSetDevice(ctx->device);
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < 6; ++i)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -112,6 +116,9 @@ void free_problem_buffers(DevProblem& d) {
   cudaFree(d.col_sq);
   cudaFree(d.active);
   cudaFree(d.xbuf);
+  cudaFree(d.x64);
+  cudaFree(d.rowcnt);
+  cudaFree(d.long_cols);
   cudaFree(d.part);
   cudaFree(d.eval_out);
   cudaFree(d.counters);
@@ -152,6 +159,9 @@ EvalParams eval_params(acdc_problem* p, bool build_active) {
   e.lambda = p->lambda;
   e.shrink_thresh = (1.0 - p->s.shrink_eps) * p->lambda;
   e.loss = p->loss;
+  e.x64 = p->fp64_mode ? p->d.x64 : nullptr;
+  e.long_cols = p->d.long_cols;
+  e.n_long = p->d.n_long;
   return e;
 }
 
@@ -167,12 +177,16 @@ UpdateParams update_params(acdc_problem* p, uint64_t count, bool shrink) {
   u.count = count;
   u.seed = p->s.seed;
   if (p->loss == ACDC_LOSS_SVM_DUAL) {
-    u.lambda = (float)(p->lambda * (double)p->d.n);
-    u.inv_lambda_n = (float)(1.0 / (p->lambda * (double)p->d.n));
+    u.lambda_d = p->lambda * (double)p->d.n;
+    u.inv_lambda_n_d = 1.0 / (p->lambda * (double)p->d.n);
   } else {
-    u.lambda = (float)p->lambda;
-    u.inv_lambda_n = 0.f;
+    u.lambda_d = p->lambda;
+    u.inv_lambda_n_d = 0.0;
   }
+  u.li_scale = shrink ? p->li_scale_shrink : 1.0;
+  u.x64 = p->d.x64;
+  u.r64 = p->d.r64;
+  u.fp64 = p->fp64_mode ? 1 : 0;
   double q = p->s.shrinking_probability;
   if (!shrink || q <= 0)
     u.shrink_q32 = 0;
@@ -180,7 +194,7 @@ UpdateParams update_params(acdc_problem* p, uint64_t count, bool shrink) {
     u.shrink_q32 = 0xffffffffu;
   else
     u.shrink_q32 = (uint32_t)(q * 4294967296.0);
-  u.n_warps = p->s.tau;
+  u.n_warps = (shrink && p->s.tau_active > 0) ? p->s.tau_active : p->s.tau;
   u.loss = p->loss;
   return u;
 }
@@ -205,9 +219,11 @@ bool shrink_now(const acdc_problem* p) {
 int apply_settings(acdc_problem* p, const acdc_settings* s) {
   acdc_ctx* ctx = p->ctx;
   if (s->loss != p->loss) return acdc_set_error(ctx, ACDC_EINVAL, "settings.loss differs from the problem's loss");
-  if (s->tau < 1 || s->warps_per_block < 1 || s->warps_per_block > 8 || s->refresh_every < 1 ||
+  if (s->tau < 1 || s->tau_active < 0 || s->warps_per_block < 1 || s->warps_per_block > 8 ||
+      s->refresh_every < 1 ||
       s->max_epochs < 0 || !(s->gap_target >= 0) || s->shrinking_probability < 0 ||
-      s->shrinking_probability > 1 || s->shrink_eps < 0 || s->shrink_eps >= 1)
+      s->shrinking_probability > 1 || s->shrink_eps < 0 || s->shrink_eps >= 1 ||
+      s->precision < ACDC_PREC_AUTO || s->precision > ACDC_PREC_FP64 || !(s->polish_rel_gap >= 0))
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid settings value");
   p->s = *s;
   const double n = (double)p->d.n;
@@ -314,6 +330,8 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
   STEP(dalloc(&d.col_sq, n, &d.bytes));
   STEP(dalloc(&d.active, n, &d.bytes));
   STEP(dalloc(&d.xbuf, n, &d.bytes));
+  STEP(dalloc(&d.x64, n, &d.bytes));
+  STEP(dalloc(&d.rowcnt, m, &d.bytes));
   STEP(dalloc(&d.part, (int64_t)ACDC_RED_BLOCKS * ACDC_NPART, &d.bytes));
   STEP(dalloc(&d.eval_out, 16, &d.bytes));
   STEP(cudaMemsetAsync(d.part, 0, sizeof(double) * ACDC_RED_BLOCKS * ACDC_NPART, st));
@@ -327,10 +345,14 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
   unsigned long long* omega_slot = d.counters + CNT_GMAX_BITS;
   STEP(cudaMemsetAsync(omega_slot, 0, sizeof(unsigned long long), st));
   STEP(launch_max_i32(counts, m, omega_slot, st));
+  // Columns too long for the thread-per-column gap pass.
+  STEP(dalloc(&d.long_cols, n, &d.bytes));
+  STEP(launch_list_long(d, d.long_cols, d.counters + CNT_NLONG, st));
   rc = check_status_word(p);
   if (rc != ACDC_OK) return fail(rc);
   // The reference starts its running maximum at 1 (MultiCoreSolver.cpp:24).
   p->omega = std::max<int64_t>(1, (int64_t)p->h_counters[CNT_GMAX_BITS]);
+  d.n_long = (int64_t)p->h_counters[CNT_NLONG];
   STEP(cudaFree(s_colptr));
   s_colptr = nullptr;
   STEP(cudaFree(s_rows));
@@ -346,6 +368,15 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
   if (loss == ACDC_LOSS_SVM_DUAL) s.gap_relative = 0;
   rc = apply_settings(p, &s);
   if (rc != ACDC_OK) return fail(rc);
+  // The engine constructor refreshes the residual from x = 0
+  // (MulticoreEngineExecutor.h:59): r = -b (Lasso) or w = 0 (SVM).
+  {
+    EvalParams e = eval_params(p, false);
+    cudaError_t ce = launch_refresh(e, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) return fail(acdc_cuda_error(ctx, ce, "initial refresh"));
+  }
+  ctx->live_problems++;
   *out = p;
   return ACDC_OK;
 }
@@ -373,6 +404,7 @@ extern "C" int acdc_problem_destroy(acdc_problem* p) {
   free_problem_buffers(p->d);
   if (p->h_eval) cudaFreeHost(p->h_eval);
   if (p->h_counters) cudaFreeHost(p->h_counters);
+  p->ctx->live_problems--;
   delete p;
   return ACDC_OK;
 }
@@ -389,6 +421,26 @@ extern "C" int acdc_problem_info_get(acdc_problem* p, acdc_problem_info* info) {
   info->device_bytes = p->d.bytes;
   info->loss = p->loss;
   info->tau = p->s.tau;
+  info->omega_active = p->omega_active;
+  info->active_step_scale = p->li_scale_shrink;
+  info->long_columns = p->d.n_long;
+  return ACDC_OK;
+}
+
+extern "C" int acdc_problem_reset(acdc_problem* p) {
+  if (!p) return ACDC_EINVAL;
+  acdc_ctx* ctx = p->ctx;
+  ACDC_CK(ctx, cudaMemsetAsync(p->d.xbuf, 0, sizeof(double) * p->d.n, ctx->stream));
+  p->fp64_mode = false;
+  ACDC_CK(ctx, launch_set_x(p->d, false, ctx->stream));
+  p->k_next = 0;
+  p->epochs_done = 0;
+  p->updates_done = 0;
+  p->active_valid = false;
+  p->li_scale_shrink = 1.0;
+  p->omega_active = 1;
+  EvalParams e = eval_params(p, false);
+  ACDC_CK(ctx, launch_refresh(e, ctx->stream));
   return ACDC_OK;
 }
 
@@ -397,11 +449,34 @@ extern "C" int acdc_problem_set_settings(acdc_problem* p, const acdc_settings* s
   return apply_settings(p, s);
 }
 
+namespace {
+// Polish-mode transitions.  Entering copies x exactly (FP32 -> FP64); the FP64
+// residual of the last refresh already equals A x - b for that x.  Leaving
+// rounds x to FP32 and refreshes both residuals from it.
+int enter_fp64(acdc_problem* p) {
+  if (p->fp64_mode) return ACDC_OK;
+  ACDC_CK(p->ctx, launch_x32_to_x64(p->d, p->ctx->stream));
+  p->fp64_mode = true;
+  return ACDC_OK;
+}
+
+int leave_fp64(acdc_problem* p) {
+  if (!p->fp64_mode) return ACDC_OK;
+  ACDC_CK(p->ctx, launch_x64_to_x32(p->d, p->ctx->stream));
+  p->fp64_mode = false;
+  EvalParams e = eval_params(p, false);
+  ACDC_CK(p->ctx, launch_refresh(e, p->ctx->stream));
+  return ACDC_OK;
+}
+}  // namespace
+
 extern "C" int acdc_problem_set_lambda(acdc_problem* p, double lambda) {
   if (!p) return ACDC_EINVAL;
   if (!(lambda > 0)) return acdc_set_error(p->ctx, ACDC_EINVAL, "lambda must be positive");
   p->lambda = lambda;
   p->active_valid = false;
+  // A new lambda starts with the FP32 bulk again (AUTO precision).
+  if (p->s.precision == ACDC_PREC_AUTO) return leave_fp64(p);
   return ACDC_OK;
 }
 
@@ -411,6 +486,8 @@ extern "C" int acdc_run_updates(acdc_problem* p, uint64_t n_updates) {
   UpdateParams u = update_params(p, n_updates, shrink_now(p));
   ACDC_CK(ctx, launch_update(u, p->k_next, p->s.warps_per_block, ctx->stream));
   p->k_next += n_updates;
+  p->updates_done += n_updates;
+  p->epochs_done = (int64_t)(p->updates_done / (uint64_t)p->d.n);
   p->stats.update_launches++;
   return ACDC_OK;
 }
@@ -431,6 +508,7 @@ int evaluate_impl(acdc_problem* p, acdc_eval* out, float* ms) {
   ACDC_CK(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
   ACDC_CK(ctx, launch_refresh(e, ctx->stream));
   ACDC_CK(ctx, launch_gap(e, ctx->stream));
+  if (build_active) ACDC_CK(ctx, launch_active_omega(e, p->d.rowcnt, ctx->stream));
   ACDC_CK(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
   ACDC_CK(ctx, cudaMemcpyAsync(p->h_eval, p->d.eval_out, sizeof(double) * 16,
                                cudaMemcpyDeviceToHost, ctx->stream));
@@ -441,7 +519,18 @@ int evaluate_impl(acdc_problem* p, acdc_eval* out, float* ms) {
   p->stats.eval_ms += t;
   p->stats.eval_launches++;
   if (ms) *ms = t;
-  if (build_active) p->active_valid = true;
+  if (build_active) {
+    p->active_valid = true;
+    // ESO parameter of the active-set draws: q*tau of them land on the
+    // |A| active columns, whose rows hold at most omega_A of them.
+    const double a = p->h_eval[9];
+    p->omega_active = std::max<int64_t>(1, (int64_t)p->h_counters[CNT_OMEGA_ACTIVE]);
+    const double tau_shrink = p->s.tau_active > 0 ? p->s.tau_active : p->s.tau;
+    const double tau_a = std::max(1.0, p->s.shrinking_probability * tau_shrink);
+    const double beta_a =
+        a > 1 ? 1.0 + ((double)p->omega_active - 1.0) * (tau_a - 1.0) / (a - 1.0) : 1.0;
+    p->li_scale_shrink = p->beta / std::max(p->beta, beta_a);
+  }
   if (out) fill_eval(p->h_eval, out);
   if (!std::isfinite(p->h_eval[0]))
     return acdc_set_error(ctx, ACDC_EDEVICE, "objective is not finite (diverged or bad input)");
@@ -463,27 +552,67 @@ extern "C" int acdc_solve(acdc_problem* p, acdc_solve_result* out) {
   acdc_ctx* ctx = p->ctx;
   std::memset(out, 0, sizeof(*out));
   auto t0 = std::chrono::steady_clock::now();
-  acdc_eval ev;
-  int rc = evaluate_impl(p, &ev, nullptr);
+  ACDC_CK(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
+  int rc = ACDC_OK;
+  if (p->s.precision == ACDC_PREC_FP64) rc = enter_fp64(p);
+  if (p->s.precision == ACDC_PREC_FP32) rc = leave_fp64(p);
   if (rc != ACDC_OK) return rc;
-  int epochs = 0;
-  while (!converged(p->s, ev) && epochs < p->s.max_epochs) {
-    const int k = std::min(p->s.refresh_every, p->s.max_epochs - epochs);
-    const uint64_t count = (uint64_t)k * (uint64_t)p->d.n;
-    UpdateParams u = update_params(p, count, shrink_now(p));
+  acdc_eval ev;
+  rc = evaluate_impl(p, &ev, nullptr);
+  if (rc != ACDC_OK) return rc;
+  // Work is counted in updates; an epoch is n of them.
+  const uint64_t n = (uint64_t)p->d.n;
+  const uint64_t budget = (uint64_t)p->s.max_epochs * n;
+  uint64_t done = 0, done_fp64 = 0;
+  double best = ev.rel_gap;
+  uint64_t last_gain = 0;  // updates done when the gap last halved
+  while (!converged(p->s, ev) && done < budget) {
+    // AUTO: the FP32 iterate bounds the certificate near 1e-7 relative (higher
+    // for badly scaled columns); finish in FP64 once the gap is small or has
+    // not halved over ten epochs of updates.
+    const bool stalled = done - last_gain >= 10 * n && ev.rel_gap < 1e-2;
+    if (p->s.precision == ACDC_PREC_AUTO && !p->fp64_mode &&
+        (ev.rel_gap <= p->s.polish_rel_gap || stalled)) {
+      rc = enter_fp64(p);
+      if (rc != ACDC_OK) return rc;
+    }
+    const bool shrink = shrink_now(p);
+    uint64_t count = (uint64_t)p->s.refresh_every * n;
+    if (shrink && p->s.active_passes > 0 && ev.active > 0) {
+      // Passes over the active set: |A| / q updates each.
+      const double q = std::max(1e-3, p->s.shrinking_probability);
+      count = (uint64_t)((double)p->s.active_passes * (double)ev.active / q);
+      count = std::max<uint64_t>(count, 32u * (uint64_t)p->s.tau);
+      count = std::min<uint64_t>(count, (uint64_t)p->s.refresh_every * n);
+    }
+    count = std::min(count, budget - done);
+    UpdateParams u = update_params(p, count, shrink);
     ACDC_CK(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
     ACDC_CK(ctx, launch_update(u, p->k_next, p->s.warps_per_block, ctx->stream));
     ACDC_CK(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
     p->k_next += count;
     p->stats.update_launches++;
-    epochs += k;
-    p->epochs_done += k;
+    done += count;
+    if (p->fp64_mode) done_fp64 += count;
+    p->updates_done += count;
+    p->epochs_done = (int64_t)(p->updates_done / n);
     rc = evaluate_impl(p, &ev, nullptr);
     if (rc != ACDC_OK) return rc;
     float t = 0;
     ACDC_CK(ctx, cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]));
     p->stats.update_ms += t;
+    if (ev.rel_gap < 0.5 * best) {
+      best = ev.rel_gap;
+      last_gain = done;
+    }
   }
+  const int epochs = (int)((done + n - 1) / n);
+  out->fp64_epochs = (int32_t)((done_fp64 + n - 1) / n);
+  ACDC_CK(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
+  ACDC_CK(ctx, cudaEventSynchronize(ctx->ev[5]));
+  float dev_ms = 0;
+  ACDC_CK(ctx, cudaEventElapsedTime(&dev_ms, ctx->ev[4], ctx->ev[5]));
+  out->device_ms = dev_ms;
   out->eval = ev;
   out->converged = converged(p->s, ev) ? 1 : 0;
   out->epochs = epochs;
@@ -494,23 +623,19 @@ extern "C" int acdc_solve(acdc_problem* p, acdc_solve_result* out) {
 extern "C" int acdc_get_x(acdc_problem* p, double* x) {
   if (!p || !x) return ACDC_EINVAL;
   acdc_ctx* ctx = p->ctx;
-  std::vector<float> h((size_t)p->d.n);
-  ACDC_CK(ctx, launch_get_x(p->d, p->d.xbuf, ctx->stream));
-  ACDC_CK(ctx, cudaMemcpyAsync(h.data(), p->d.xbuf, sizeof(float) * p->d.n, cudaMemcpyDeviceToHost,
+  ACDC_CK(ctx, launch_get_x(p->d, p->fp64_mode, ctx->stream));
+  ACDC_CK(ctx, cudaMemcpyAsync(x, p->d.xbuf, sizeof(double) * p->d.n, cudaMemcpyDeviceToHost,
                                ctx->stream));
   ACDC_CK(ctx, cudaStreamSynchronize(ctx->stream));
-  for (int64_t j = 0; j < p->d.n; ++j) x[j] = (double)h[(size_t)j];
   return ACDC_OK;
 }
 
 extern "C" int acdc_set_x(acdc_problem* p, const double* x) {
   if (!p || !x) return ACDC_EINVAL;
   acdc_ctx* ctx = p->ctx;
-  std::vector<float> h((size_t)p->d.n);
-  for (int64_t j = 0; j < p->d.n; ++j) h[(size_t)j] = (float)x[j];
-  ACDC_CK(ctx, cudaMemcpyAsync(p->d.xbuf, h.data(), sizeof(float) * p->d.n, cudaMemcpyHostToDevice,
+  ACDC_CK(ctx, cudaMemcpyAsync(p->d.xbuf, x, sizeof(double) * p->d.n, cudaMemcpyHostToDevice,
                                ctx->stream));
-  ACDC_CK(ctx, launch_set_x(p->d, p->d.xbuf, ctx->stream));
+  ACDC_CK(ctx, launch_set_x(p->d, p->fp64_mode, ctx->stream));
   ACDC_CK(ctx, cudaStreamSynchronize(ctx->stream));
   p->active_valid = false;
   return acdc_recompute_residuals(p);

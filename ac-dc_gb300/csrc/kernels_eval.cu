@@ -171,16 +171,37 @@ __global__ void k_widen_i32(const int32_t* src, int64_t* dst, int64_t len) {
     dst[i] = (int64_t)src[i];
 }
 
-__global__ void k_set_x(DevProblem d, const float* x) {
+// xbuf (FP64, caller order) -> meta.w (FP32) and, in polish mode, x64.
+__global__ void k_set_x(DevProblem d, int fp64) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < d.n; j += stride)
-    d.meta[j].w = __float_as_int(x[j]);
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < d.n; j += stride) {
+    const double v = d.xbuf[j];
+    d.meta[j].w = __float_as_int((float)v);
+    if (fp64) d.x64[j] = v;
+  }
 }
 
-__global__ void k_get_x(DevProblem d, float* x) {
+__global__ void k_get_x(DevProblem d, int fp64) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < d.n; j += stride)
-    x[j] = __int_as_float(__ldcg(&d.meta[j].w));
+    d.xbuf[j] = fp64 ? __ldcg(d.x64 + j) : (double)__int_as_float(__ldcg(&d.meta[j].w));
+}
+
+__global__ void k_x32_to_x64(DevProblem d) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < d.n; j += stride)
+    d.x64[j] = (double)__int_as_float(d.meta[j].w);
+}
+
+__global__ void k_x64_to_x32(DevProblem d) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < d.n; j += stride)
+    d.meta[j].w = __float_as_int((float)d.x64[j]);
+}
+
+// Coordinate j as the evaluation sees it: FP64 in polish mode, else FP32 bits.
+__device__ __forceinline__ double coord(const EvalParams& p, int64_t j, int4 mt) {
+  return p.x64 ? p.x64[j] : (double)__int_as_float(mt.w);
 }
 
 // ---- refresh ----
@@ -206,13 +227,18 @@ __global__ void k_refresh_scatter(EvalParams p) {
     int4 mt = make_int4(0, 0, 0, 0);
     if (j < p.n) {
       mt = p.meta[j];
-      float xv = __int_as_float(mt.w);
+      const double xv = coord(p, j, mt);
       if (p.loss == ACDC_LOSS_SVM_DUAL) {
-        float c = xv > 1.f ? 1.f : (xv < 0.f ? 0.f : xv);
-        if (c != xv) p.meta[j].w = __float_as_int(c);
-        coef = (double)c * p.rhs64[j] * inv_ln;
+        const double c = xv > 1.0 ? 1.0 : (xv < 0.0 ? 0.0 : xv);
+        if (c != xv) {
+          if (p.x64)
+            p.x64[j] = c;
+          else
+            p.meta[j].w = __float_as_int((float)c);
+        }
+        coef = c * p.rhs64[j] * inv_ln;
       } else {
-        coef = (double)xv;
+        coef = xv;
       }
     }
     unsigned live = __ballot_sync(ACDC_FULL_MASK, coef != 0.0 && mt.y > 0);
@@ -262,62 +288,105 @@ __global__ void __launch_bounds__(ACDC_RED_THREADS) k_refresh_finish(EvalParams 
 
 // ---- gap ----
 
-// Lasso: groups of 8 lanes per column; slots 2: sum |x|, 3: max |a_j^T r|,
-// 4: support count.  Columns with x_j != 0 or |a_j^T r| > shrink_thresh join the
-// active set.
-__global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso(EvalParams p) {
+// Lasso gap, pass 1 (segment-parallel): a warp takes 32 consecutive columns.
+// Every column contributes |x_j| and the support count (slots 2 and 4).  The
+// padded entries of the columns with at most kShortLen entries are contiguous,
+// so the warp streams them as 4-entry units (one 128-bit load of values and one
+// of row indices per lane, coalesced), gathers r, and adds each column's units
+// with a segmented warp scan in a fixed order; these columns contribute
+// |a_j^T r| (slot 3) and may join the active set.  Longer columns are listed in
+// long_cols and handled by pass 2.
+constexpr int kShortLen = 32;
+constexpr int kShortUnits = kShortLen / 4;
+
+struct ShortWarp {
+  double colsum[32];
+  uint32_t ustart[32];  // first unit of each column in the padded arrays
+  int32_t uexcl[32];    // first unit of each column in the warp's unit stream
+  uint8_t owner[32 * kShortUnits];
+};
+
+__device__ __forceinline__ void append_active(const EvalParams& p, bool join, int64_t j,
+                                              int lane) {
+  // One counter increment per warp for its joining columns.
+  const unsigned joiners = __ballot_sync(ACDC_FULL_MASK, join);
+  if (!joiners) return;
+  const int leader = __ffs(joiners) - 1;
+  unsigned long long first = 0;
+  if (lane == leader) first = atomicAdd(p.counters + CNT_ACTIVE, (unsigned long long)__popc(joiners));
+  first = __shfl_sync(ACDC_FULL_MASK, first, leader);
+  if (join) {
+    const unsigned long long pos = first + __popc(joiners & ((1u << lane) - 1u));
+    if (pos < (unsigned long long)p.n) p.active[pos] = (int32_t)j;
+  }
+}
+
+__global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_short(EvalParams p) {
   __shared__ double s_l1[ACDC_RED_THREADS / 32], s_gm[ACDC_RED_THREADS / 32],
       s_sp[ACDC_RED_THREADS / 32];
+  __shared__ ShortWarp sw_all[ACDC_RED_THREADS / 32];
   const int lane = threadIdx.x & 31;
-  const int sub = lane & 7;
-  const int grp = lane >> 3;
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  ShortWarp& sw = sw_all[threadIdx.x >> 5];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;  // a multiple of 32
   double l1 = 0, gmax = 0, sp = 0;
-  for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 4; base < p.n;
-       base += warps * 4) {
-    const int64_t j = base + grp;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < p.n;
+       base += stride) {
+    const int64_t j = base + lane;
+    const bool valid = j < p.n;
     int4 mt = make_int4(0, 0, 0, 0);
-    if (j < p.n) mt = p.meta[j];
-    const int64_t start = (int64_t)(uint32_t)mt.x << 2;
-    const int32_t len = mt.y;
-    double g = 0;
-    // The four groups may have different lengths: loop to the longest.
-    int32_t lmax = len;
-    lmax = max(lmax, __shfl_xor_sync(ACDC_FULL_MASK, lmax, 8));
-    lmax = max(lmax, __shfl_xor_sync(ACDC_FULL_MASK, lmax, 16));
-    for (int32_t off = 4 * sub; off < lmax; off += 32) {
-      if (off < len) {
-        float4 v = __ldcs(reinterpret_cast<const float4*>(p.vals + start + off));
-        int4 id = __ldcs(reinterpret_cast<const int4*>(p.idx + start + off));
-        g += (double)v.x * p.r64[id.x];
-        g += (double)v.y * p.r64[id.y];
-        g += (double)v.z * p.r64[id.z];
-        g += (double)v.w * p.r64[id.w];
+    if (valid) mt = p.meta[j];
+    const double xv = valid ? coord(p, j, mt) : 0.0;
+    l1 += fabs(xv);
+    sp += xv != 0.0 ? 1.0 : 0.0;
+    const bool is_short = valid && mt.y <= kShortLen;
+    const int units = is_short ? (mt.y + 3) >> 2 : 0;
+    // Exclusive scan of the unit counts over the 32 columns.
+    int incl = units;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(ACDC_FULL_MASK, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int excl = incl - units;
+    const int total = __shfl_sync(ACDC_FULL_MASK, incl, 31);
+    sw.colsum[lane] = 0.0;
+    sw.ustart[lane] = (uint32_t)mt.x;
+    sw.uexcl[lane] = excl;
+    for (int u = 0; u < units; ++u) sw.owner[excl + u] = (uint8_t)lane;
+    __syncwarp();
+    for (int cb = 0; cb < total; cb += 32) {
+      const int u = cb + lane;
+      const bool live = u < total;
+      const int own = live ? sw.owner[u] : 31;
+      double v = 0.0;
+      if (live) {
+        const uint64_t e = ((uint64_t)sw.ustart[own] + (uint64_t)(u - sw.uexcl[own])) << 2;
+        const float4 a = __ldcs(reinterpret_cast<const float4*>(p.vals + e));
+        const int4 id = __ldcs(reinterpret_cast<const int4*>(p.idx + e));
+        if (a.x != 0.f) v += (double)a.x * p.r64[id.x];
+        if (a.y != 0.f) v += (double)a.y * p.r64[id.y];
+        if (a.z != 0.f) v += (double)a.z * p.r64[id.z];
+        if (a.w != 0.f) v += (double)a.w * p.r64[id.w];
       }
-    }
-    g += __shfl_xor_sync(ACDC_FULL_MASK, g, 4);
-    g += __shfl_xor_sync(ACDC_FULL_MASK, g, 2);
-    g += __shfl_xor_sync(ACDC_FULL_MASK, g, 1);
-    bool join = false;
-    if (sub == 0 && j < p.n) {
-      const float xv = __int_as_float(mt.w);
-      const double ag = fabs(g);
-      gmax = fmax(gmax, ag);
-      l1 += fabs((double)xv);
-      sp += xv != 0.f ? 1.0 : 0.0;
-      join = p.active && (xv != 0.f || ag > p.shrink_thresh);
-    }
-    // One counter increment per warp for the (up to four) joining columns.
-    const unsigned joiners = __ballot_sync(ACDC_FULL_MASK, join);
-    if (joiners) {
-      unsigned long long first = 0;
-      if (lane == __ffs(joiners) - 1) first = atomicAdd(p.counters + CNT_ACTIVE, (unsigned long long)__popc(joiners));
-      first = __shfl_sync(ACDC_FULL_MASK, first, __ffs(joiners) - 1);
-      if (join) {
-        unsigned long long pos = first + __popc(joiners & ((1u << lane) - 1u));
-        if (pos < (unsigned long long)p.n) p.active[pos] = (int32_t)j;
+      // Segmented inclusive scan: lanes of one column are contiguous.
+      const int prev_own = __shfl_up_sync(ACDC_FULL_MASK, own, 1);
+      const bool head = lane == 0 || prev_own != own;
+      const unsigned heads = __ballot_sync(ACDC_FULL_MASK, head);
+      const int seg0 = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double t = __shfl_up_sync(ACDC_FULL_MASK, v, o);
+        if (lane - o >= seg0) v += t;
       }
+      const int next_own = __shfl_down_sync(ACDC_FULL_MASK, own, 1);
+      const bool tail = live && (lane == 31 || u + 1 >= total || next_own != own);
+      if (tail) sw.colsum[own] += v;  // one tail per column per chunk
+      __syncwarp();
     }
+    const double ag = fabs(sw.colsum[lane]);
+    if (is_short) gmax = fmax(gmax, ag);
+    append_active(p, p.active && is_short && (xv != 0.0 || ag > p.shrink_thresh), j, lane);
+    __syncwarp();
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -341,6 +410,84 @@ __global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso(EvalParams p) {
     p.part[blockIdx.x * ACDC_NPART + 2] = t0;
     p.part[blockIdx.x * ACDC_NPART + 3] = t1;
     p.part[blockIdx.x * ACDC_NPART + 4] = t2;
+  }
+}
+
+// Lasso gap, pass 2: one warp per long column (slot 5: max |a_j^T r|).  The
+// metadata of the warp's next column is loaded while the current one is summed,
+// and each 128-entry chunk is loaded before the previous chunk's gathers.
+__global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_long(EvalParams p) {
+  __shared__ double s_gm[ACDC_RED_THREADS / 32];
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double gmax = 0;
+  int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int64_t j = t < p.n_long ? p.long_cols[t] : 0;
+  int4 mt = t < p.n_long ? p.meta[j] : make_int4(0, 0, 0, 0);
+  for (; t < p.n_long; t += warps) {
+    const int64_t tn = t + warps;
+    const int64_t jn = tn < p.n_long ? p.long_cols[tn] : 0;
+    const int4 mtn = tn < p.n_long ? p.meta[jn] : make_int4(0, 0, 0, 0);
+    const int64_t start = (int64_t)(uint32_t)mt.x << 2;
+    const int32_t len = mt.y;
+    double g = 0;
+    int32_t off = 4 * lane;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    int4 id = make_int4(0, 0, 0, 0);
+    if (off < len) {
+      v = __ldcs(reinterpret_cast<const float4*>(p.vals + start + off));
+      id = __ldcs(reinterpret_cast<const int4*>(p.idx + start + off));
+    }
+    for (; off < len; off += 128) {
+      float4 vn = make_float4(0.f, 0.f, 0.f, 0.f);
+      int4 idn = make_int4(0, 0, 0, 0);
+      if (off + 128 < len) {
+        vn = __ldcs(reinterpret_cast<const float4*>(p.vals + start + off + 128));
+        idn = __ldcs(reinterpret_cast<const int4*>(p.idx + start + off + 128));
+      }
+      g += (double)v.x * p.r64[id.x];
+      g += (double)v.y * p.r64[id.y];
+      g += (double)v.z * p.r64[id.z];
+      g += (double)v.w * p.r64[id.w];
+      v = vn;
+      id = idn;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(ACDC_FULL_MASK, g, o);
+    const double ag = fabs(g);
+    gmax = fmax(gmax, ag);
+    const double xv = coord(p, j, mt);
+    if (lane == 0 && p.active && (xv != 0.0 || ag > p.shrink_thresh)) {
+      const unsigned long long pos = atomicAdd(p.counters + CNT_ACTIVE, 1ull);
+      if (pos < (unsigned long long)p.n) p.active[pos] = (int32_t)j;
+    }
+    j = jn;
+    mt = mtn;
+  }
+  if (lane == 0) s_gm[threadIdx.x >> 5] = gmax;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t1 = 0;
+    for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) t1 = fmax(t1, s_gm[w]);
+    p.part[blockIdx.x * ACDC_NPART + 5] = t1;
+  }
+}
+
+// Columns with more than kShortLen entries, for pass 2 (order not significant).
+__global__ void k_list_long(const DevProblem d, int32_t* list, unsigned long long* count) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < d.n;
+       base += stride) {
+    const int64_t j = base + lane;
+    const bool is_long = j < d.n && d.meta[j].y > kShortLen;
+    const unsigned mask = __ballot_sync(ACDC_FULL_MASK, is_long);
+    if (!mask) continue;
+    const int leader = __ffs(mask) - 1;
+    unsigned long long first = 0;
+    if (lane == leader) first = atomicAdd(count, (unsigned long long)__popc(mask));
+    first = __shfl_sync(ACDC_FULL_MASK, first, leader);
+    if (is_long) list[first + __popc(mask & ((1u << lane) - 1u))] = (int32_t)j;
   }
 }
 
@@ -370,7 +517,7 @@ __global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_svm(EvalParams p) {
     for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(ACDC_FULL_MASK, g, o);
     if (lane == 0) {
       const double y = p.rhs64[j];
-      const double a = (double)__int_as_float(mt.w);
+      const double a = coord(p, j, mt);
       if (y * g > 0) ok += 1.0;
       double h = 1.0 - y * g;
       if (h < 0) h = 0;
@@ -408,20 +555,43 @@ __global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_svm(EvalParams p) {
 // Adds the per-block partials in block order and forms P, D and the gap.
 // eval_out: [0] P [1] D [2] gap [3] rel_gap [4] 0-1 accuracy [5] reg_norm
 //           [6] sq_norm [7] max_abs_grad [8] support [9] active
-__global__ void k_finalize(EvalParams p) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double rr = 0, br = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
-  for (int b = 0; b < ACDC_RED_BLOCKS; ++b) {
+constexpr int kFinThreads = 256;
+
+// Thread t adds blocks [t*S, (t+1)*S) in order; thread 0 then adds the stripes
+// in order, so the association is fixed and the result reproducible.
+__global__ void __launch_bounds__(kFinThreads) k_finalize(EvalParams p) {
+  __shared__ double st[kFinThreads][6];
+  constexpr int S = (ACDC_RED_BLOCKS + kFinThreads - 1) / kFinThreads;
+  const bool lasso = p.loss == ACDC_LOSS_L1_SQUARE;
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x * S; b < (int)(threadIdx.x + 1) * S && b < ACDC_RED_BLOCKS; ++b) {
     const double* q = p.part + b * ACDC_NPART;
-    rr += q[0];
-    br += q[1];
-    s2 += q[2];
-    s4 += q[4];
-    s5 += q[5];
-    if (p.loss == ACDC_LOSS_L1_SQUARE)
-      s3 = fmax(s3, q[3]);
-    else
-      s3 += q[3];
+    a[0] += q[0];
+    a[1] += q[1];
+    a[2] += q[2];
+    a[4] += q[4];
+    if (lasso) {
+      a[3] = fmax(a[3], fmax(q[3], q[5]));  // short and long columns
+    } else {
+      a[3] += q[3];
+      a[5] += q[5];
+    }
+  }
+  for (int k = 0; k < 6; ++k) st[threadIdx.x][k] = a[k];
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double rr = 0, br = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
+  for (int t = 0; t < kFinThreads; ++t) {
+    rr += st[t][0];
+    br += st[t][1];
+    s2 += st[t][2];
+    s4 += st[t][4];
+    if (lasso) {
+      s3 = fmax(s3, st[t][3]);
+    } else {
+      s3 += st[t][3];
+      s5 += st[t][5];
+    }
   }
   double P, D, acc = 0, gmax = 0;
   const double nn = (double)p.n;
@@ -517,13 +687,55 @@ cudaError_t launch_widen_i32(const int32_t* src, int64_t* dst, int64_t len, cuda
   return cudaGetLastError();
 }
 
-cudaError_t launch_set_x(const DevProblem& d, const float* x32, cudaStream_t st) {
-  k_set_x<<<grid_for(d.n, 256, 152 * 8), 256, 0, st>>>(d, x32);
+cudaError_t launch_set_x(const DevProblem& d, bool fp64, cudaStream_t st) {
+  k_set_x<<<grid_for(d.n, 256, 152 * 8), 256, 0, st>>>(d, fp64 ? 1 : 0);
   return cudaGetLastError();
 }
 
-cudaError_t launch_get_x(const DevProblem& d, float* x32, cudaStream_t st) {
-  k_get_x<<<grid_for(d.n, 256, 152 * 8), 256, 0, st>>>(d, x32);
+cudaError_t launch_get_x(const DevProblem& d, bool fp64, cudaStream_t st) {
+  k_get_x<<<grid_for(d.n, 256, 152 * 8), 256, 0, st>>>(d, fp64 ? 1 : 0);
+  return cudaGetLastError();
+}
+
+// One warp per active column: rowcnt[row] += 1 for each of its entries.
+__global__ void k_active_rowcount(EvalParams p, int32_t* rowcnt) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t cnt = (int64_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n);
+  for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < cnt; t += warps) {
+    const int4 mt = p.meta[p.active[t]];
+    const int64_t start = (int64_t)(uint32_t)mt.x << 2;
+    for (int32_t e = lane; e < mt.y; e += 32) atomicAdd(rowcnt + p.idx[start + e], 1);
+  }
+}
+
+cudaError_t launch_list_long(const DevProblem& d, int32_t* list, unsigned long long* count,
+                             cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  const int64_t blocks = std::min<int64_t>((d.n + 255) / 256, 152 * 8);
+  k_list_long<<<(unsigned)(blocks > 0 ? blocks : 1), 256, 0, st>>>(d, list, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_active_omega(const EvalParams& p, int32_t* rowcnt, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(rowcnt, 0, sizeof(int32_t) * p.m, st);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(p.counters + CNT_OMEGA_ACTIVE, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  k_active_rowcount<<<152 * 8, 256, 0, st>>>(p, rowcnt);
+  const int64_t blocks = std::min<int64_t>((p.m + 255) / 256, 152 * 8);
+  k_max_i32<<<(unsigned)blocks, 256, 0, st>>>(rowcnt, p.m, p.counters + CNT_OMEGA_ACTIVE);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_x32_to_x64(const DevProblem& d, cudaStream_t st) {
+  k_x32_to_x64<<<grid_for(d.n, 256, 152 * 8), 256, 0, st>>>(d);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_x64_to_x32(const DevProblem& d, cudaStream_t st) {
+  k_x64_to_x32<<<grid_for(d.n, 256, 152 * 8), 256, 0, st>>>(d);
   return cudaGetLastError();
 }
 
@@ -538,9 +750,12 @@ cudaError_t launch_gap(const EvalParams& p, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(p.counters + CNT_ACTIVE, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   if (p.loss == ACDC_LOSS_L1_SQUARE)
-    k_gap_lasso<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
+  {
+    k_gap_lasso_short<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
+    k_gap_lasso_long<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
+  }
   else
     k_gap_svm<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
-  k_finalize<<<1, 32, 0, st>>>(p);
+  k_finalize<<<1, kFinThreads, 0, st>>>(p);
   return cudaGetLastError();
 }

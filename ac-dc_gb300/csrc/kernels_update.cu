@@ -7,40 +7,84 @@
 // MulticoreSVMDualLoss::performOneCoordinateUpdate
 // (cpp/src/solver/lossFunctions/SVMDualLoss/MulticoreSVMDualLoss.h:119-141).
 //
-// tau warps run concurrently; each warp repeatedly takes 32 update numbers from
+// tau warps run concurrently; each warp takes 128 update numbers at a time from
 // a global work counter and performs those updates one after another:
 //   j      = sampler(seed, k)                         (Philox, see acdc_philox.h)
 //   g      = a_j^T r                                  (lanes gather, shuffle reduce)
 //   delta  = Lasso: S(lambda Li, x_j - Li g) - x_j    (treshhold_functions.h:27-33)
 //            SVM:   clip((1 - y_j g) lambda n Li, -a_j, 1 - a_j)
-//   x_j   += delta;  r += c delta a_j                 (red.global.add.f32)
-// with Li = 1/(beta ||a_j||^2), beta the ESO parameter for tau.  Reads of r and
-// x go to L2 (ld.global.cg) so they observe other warps' reductions; the column
-// entries are streamed with evict-first loads.  The column metadata of the
-// next two updates and the first 128 entries of the next column are loaded
-// while the current update waits on its gathers.
+//   x_j   += delta;  r += c delta a_j                 (red.global.add)
+// with Li = 1/(beta ||a_j||^2), beta the ESO parameter for tau.
+//
+// Memory pipeline.  The column metadata of update s + 2D and the first 128
+// entries (values and row indices) of update s + D are copied into the warp's
+// shared-memory ring with cp.async while update s runs: lane l copies entries
+// 4l..4l+3 as one 16-byte transfer of values and one of indices (the device
+// layout starts every column on a 16-byte boundary).  The warp waits only for
+// the copies of update s (cp.async.wait_group D-1), so D updates' worth of DRAM
+// traffic is in flight per warp while it waits on its L2 gathers of r.  x_j and
+// r are read when the update runs (ld.global.cg, L2), so the sequence of
+// updates a warp performs reads exactly the state its own previous updates left.
+// Entries beyond the first 128 of a long column are streamed with direct loads.
+//
+// Precision: T = float keeps x in the column metadata and r in FP32 (the bulk
+// mode); T = double keeps x and r in FP64 arrays (the polish mode).  Matrix
+// values are FP32 in both.
 #include "acdc_internal.cuh"
 
 namespace {
 
-constexpr int kChunk = 32;  // updates taken from the work counter at a time
+constexpr int kChunk = 128;          // updates taken from the work counter at a time
+constexpr int kD = 4;                // entry copies in flight per warp
+constexpr int kDS = kD + 1;          // entry slots (the slot being written is never the one read)
+constexpr int kDM = 2 * kD;          // metadata prefetch distance
+constexpr int kMS = kDM + 1;         // metadata slots
+constexpr int kMaxWarps = 8;         // warps per block
 
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(ACDC_FULL_MASK, v, o);
-  return v;  // identical in every lane: each butterfly step adds the same pair
+struct WarpRing {
+  float4 vals[kDS][32];
+  int4 idx[kDS][32];
+  int4 meta[kMS];
+  int32_t coords[kChunk];  // coordinates of the current chunk of updates
+};
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-__device__ __forceinline__ int64_t draw_coord(const UpdateParams& p, uint64_t k,
+// Sum over the lanes that hold entries of a column of len entries, returned
+// in every lane.  Only the lowest ceil(len/4) lanes carry nonzero partials, so
+// log2 of that many butterfly steps suffice before a broadcast from lane 0.
+template <typename T>
+__device__ __forceinline__ T column_sum(T v, uint32_t len) {
+  if (len > 64u) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(ACDC_FULL_MASK, v, o);
+    return v;  // every butterfly step adds the same pair in both lanes
+  }
+  const uint32_t lanes = (len + 3u) >> 2;  // 1..16
+  for (uint32_t o = 1; o < lanes; o <<= 1) v += __shfl_xor_sync(ACDC_FULL_MASK, v, (int)o);
+  return __shfl_sync(ACDC_FULL_MASK, v, 0);
+}
+
+__device__ __forceinline__ int32_t draw_coord(const UpdateParams& p, uint64_t k,
                                               int32_t active_cnt) {
   acdc_u32x4 o = acdc_philox4x32_10((uint32_t)k, (uint32_t)(k >> 32), ACDC_STREAM_SAMPLER, 0u,
                                     (uint32_t)p.seed, (uint32_t)(p.seed >> 32));
   if (active_cnt > 0 && o.v[2] < p.shrink_q32) {
     uint32_t t = __umulhi(o.v[3], (uint32_t)active_cnt);
-    return (int64_t)__ldg(p.active + t);
+    return __ldg(p.active + t);
   }
   uint64_t u = ((uint64_t)o.v[0] << 32) | (uint64_t)o.v[1];
-  return (int64_t)__umul64hi(u, (uint64_t)p.n);
+  return (int32_t)__umul64hi(u, (uint64_t)p.n);
 }
 
 struct Chunk {
@@ -62,31 +106,71 @@ __device__ __forceinline__ Chunk load_chunk(const UpdateParams& p, uint64_t star
   return c;
 }
 
-__device__ __forceinline__ float gather_dot(const float* r, const Chunk& c, bool live) {
-  if (!live) return 0.f;
-  float a = c.v.x * __ldcg(r + c.i.x);
-  a = fmaf(c.v.y, __ldcg(r + c.i.y), a);
-  a = fmaf(c.v.z, __ldcg(r + c.i.z), a);
-  a = fmaf(c.v.w, __ldcg(r + c.i.w), a);
+template <typename T>
+__device__ __forceinline__ T gather_dot(const T* r, const Chunk& c, bool live) {
+  if (!live) return T(0);
+  T a = (T)c.v.x * __ldcg(r + c.i.x);
+  a += (T)c.v.y * __ldcg(r + c.i.y);
+  a += (T)c.v.z * __ldcg(r + c.i.z);
+  a += (T)c.v.w * __ldcg(r + c.i.w);
   return a;
 }
 
-__device__ __forceinline__ void scatter(float* r, const Chunk& c, float coef, bool live) {
-  if (!live) return;
-  if (c.v.x != 0.f) atomicAdd(r + c.i.x, coef * c.v.x);
-  if (c.v.y != 0.f) atomicAdd(r + c.i.y, coef * c.v.y);
-  if (c.v.z != 0.f) atomicAdd(r + c.i.z, coef * c.v.z);
-  if (c.v.w != 0.f) atomicAdd(r + c.i.w, coef * c.v.w);
+// The same for the first chunk, skipping the pad entries of a column whose
+// length is not a multiple of 4 (most columns are short: one gather, not four).
+template <typename T>
+__device__ __forceinline__ T gather_dot_head(const T* r, const Chunk& c, uint32_t e0,
+                                             uint32_t len) {
+  T a = T(0);
+  if (e0 < len) a = (T)c.v.x * __ldcg(r + c.i.x);
+  if (e0 + 1u < len) a += (T)c.v.y * __ldcg(r + c.i.y);
+  if (e0 + 2u < len) a += (T)c.v.z * __ldcg(r + c.i.z);
+  if (e0 + 3u < len) a += (T)c.v.w * __ldcg(r + c.i.w);
+  return a;
 }
 
-template <int LOSS>
+template <typename T>
+__device__ __forceinline__ void scatter(T* r, const Chunk& c, T coef, bool live) {
+  if (!live) return;
+  if (c.v.x != 0.f) atomicAdd(r + c.i.x, coef * (T)c.v.x);
+  if (c.v.y != 0.f) atomicAdd(r + c.i.y, coef * (T)c.v.y);
+  if (c.v.z != 0.f) atomicAdd(r + c.i.z, coef * (T)c.v.z);
+  if (c.v.w != 0.f) atomicAdd(r + c.i.w, coef * (T)c.v.w);
+}
+
+__device__ __forceinline__ void issue_meta(WarpRing& w, const UpdateParams& p, int32_t j, int slot,
+                                           int lane) {
+  if (lane == 0) cp_async16(&w.meta[slot], p.meta + j);
+}
+
+__device__ __forceinline__ void issue_entries(WarpRing& w, const UpdateParams& p, int mslot,
+                                              int dslot, int lane) {
+  const int4 mt = w.meta[mslot];
+  const uint32_t len = (uint32_t)mt.y;
+  if (4u * (uint32_t)lane < len) {
+    const uint64_t src = ((uint64_t)(uint32_t)mt.x << 2) + 4u * (uint32_t)lane;
+    cp_async16(&w.vals[dslot][lane], p.vals + src);
+    cp_async16(&w.idx[dslot][lane], p.idx + src);
+  }
+}
+
+__device__ __forceinline__ int ring_next(int s, int size) { return s + 1 == size ? 0 : s + 1; }
+
+template <int LOSS, typename T>
 __global__ void __launch_bounds__(256, 4) k_pcdm_update(UpdateParams p, uint64_t k_base) {
+  __shared__ WarpRing rings[kMaxWarps];
   const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
   const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (gwarp >= p.n_warps) return;
+  WarpRing& w = rings[wib];
+  T* r = reinterpret_cast<T*>(sizeof(T) == 8 ? (void*)p.r64 : (void*)p.r);
   unsigned long long* work = p.counters + CNT_WORK;
   const int32_t active_cnt =
       p.shrink_q32 ? (int32_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n) : 0;
+  const T lam = (T)p.lambda_d;
+  const T inv_ln = (T)p.inv_lambda_n_d;
+  const T li_scale = (T)p.li_scale;
   unsigned long long n_upd = 0, n_nz = 0, n_read = 0, n_scat = 0;
 
   for (;;) {
@@ -95,81 +179,111 @@ __global__ void __launch_bounds__(256, 4) k_pcdm_update(UpdateParams p, uint64_t
     base = __shfl_sync(ACDC_FULL_MASK, base, 0);
     if (base >= p.count) break;
     const int cnt = (int)min((unsigned long long)kChunk, p.count - base);
-    int64_t my_j = 0;
-    if (lane < cnt) my_j = draw_coord(p, k_base + base + (uint64_t)lane, active_cnt);
+#pragma unroll
+    for (int q = 0; q < kChunk / 32; ++q) {
+      const int s = 32 * q + lane;
+      w.coords[s] = s < cnt ? draw_coord(p, k_base + base + (uint64_t)s, active_cnt) : 0;
+    }
+    __syncwarp();
 
-    // Pipeline prologue: meta of updates 0 and 1, entries of update 0.
-    int64_t j_c = __shfl_sync(ACDC_FULL_MASK, my_j, 0);
-    int4 mt_c = __ldcg(p.meta + j_c);
-    int64_t j_n = __shfl_sync(ACDC_FULL_MASK, my_j, 1 & 31);
-    int4 mt_n = make_int4(0, 0, 0, 0);
-    if (cnt > 1) mt_n = __ldcg(p.meta + j_n);
-    Chunk c_c = load_chunk(p, (uint64_t)(uint32_t)mt_c.x << 2, (uint32_t)mt_c.y, 0u, lane);
+    // Prologue: metadata of updates 0..2D-1, then entries of updates 0..D-1,
+    // one commit group per update so that wait_group(D-1) below always means
+    // "the copies of update s have landed".
+    for (int t = 0; t < kDM && t < cnt; ++t) issue_meta(w, p, w.coords[t], t, lane);
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < kD; ++t) {
+      if (t < cnt) issue_entries(w, p, t, t, lane);
+      cp_async_commit();
+    }
 
-    for (int u = 0; u < cnt; ++u) {
-      // Prefetch: entries of update u+1, meta of update u+2.
-      Chunk c_n = {make_float4(0.f, 0.f, 0.f, 0.f), make_int4(0, 0, 0, 0)};
-      if (u + 1 < cnt)
-        c_n = load_chunk(p, (uint64_t)(uint32_t)mt_n.x << 2, (uint32_t)mt_n.y, 0u, lane);
-      const int64_t j_nn = __shfl_sync(ACDC_FULL_MASK, my_j, (u + 2) & 31);
-      int4 mt_nn = make_int4(0, 0, 0, 0);
-      if (u + 2 < cnt) mt_nn = __ldcg(p.meta + j_nn);
+    // Ring positions: update s reads meta slot ms and entry slot ds; the refill
+    // writes entries of s+D into slot (s+D) mod kDS and meta of s+2D into slot
+    // (s+2D) mod kMS, which are the slots update s-1 used.
+    int ms = 0, ds = 0, ms_d = kD % kMS, ds_d = kD % kDS, ms_2d = kDM % kMS;
+    uint32_t chunk_read = 0, chunk_nz = 0, chunk_scat = 0;
+    for (int s = 0; s < cnt; ++s) {
+      cp_async_wait<kD - 1>();
+      __syncwarp();  // copies of update s visible; every lane is done with update s-1
+      const int32_t j = w.coords[s];
+      const int4 mt = w.meta[ms];
+      T xj;
+      if constexpr (sizeof(T) == 8)
+        xj = __ldcg(p.x64 + j);
+      else
+        xj = __int_as_float(__ldcg(&p.meta[j].w));
+      const uint64_t start = (uint64_t)(uint32_t)mt.x << 2;
+      const uint32_t len = (uint32_t)mt.y;
+      const uint32_t e0 = 4u * (uint32_t)lane;
+      const bool live0 = e0 < len;
+      Chunk c0;
+      c0.v = live0 ? w.vals[ds][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+      c0.i = live0 ? w.idx[ds][lane] : make_int4(0, 0, 0, 0);
+      // Refill: entries of update s + D, metadata of update s + 2D.
+      if (s + kD < cnt) issue_entries(w, p, ms_d, ds_d, lane);
+      if (s + kDM < cnt) issue_meta(w, p, w.coords[s + kDM], ms_2d, lane);
+      cp_async_commit();
+      ms = ring_next(ms, kMS);
+      ds = ring_next(ds, kDS);
+      ms_d = ring_next(ms_d, kMS);
+      ds_d = ring_next(ds_d, kDS);
+      ms_2d = ring_next(ms_2d, kMS);
 
-      // Update u: g = a_j^T r.
-      const uint64_t start = (uint64_t)(uint32_t)mt_c.x << 2;
-      const uint32_t len = (uint32_t)mt_c.y;
-      float acc = gather_dot(p.r, c_c, 4u * (uint32_t)lane < len);
+      // g = a_j^T r.
+      T acc = gather_dot_head<T>(r, c0, e0, len);
       if (len > 128u) {
         Chunk a = load_chunk(p, start, len, 128u, lane);
         for (uint32_t off = 128u; off < len; off += 128u) {
           Chunk b = load_chunk(p, start, len, off + 128u, lane);
-          acc += gather_dot(p.r, a, off + 4u * (uint32_t)lane < len);
+          acc += gather_dot<T>(r, a, off + e0 < len);
           a = b;
         }
       }
-      const float g = warp_sum(acc);
+      const T g = column_sum<T>(acc, len);
 
-      const float li = __int_as_float(mt_c.z);
-      const float xj = __int_as_float(mt_c.w);
-      float delta, coef;
+      const T li = (T)__int_as_float(mt.z) * li_scale;
+      T delta, coef;
       if (LOSS == ACDC_LOSS_L1_SQUARE) {
-        const float z = xj - li * g;
-        float a = fabsf(z) - p.lambda * li;
-        a = a < 0.f ? 0.f : a;
-        const float xn = z > 0.f ? a : (z < 0.f ? -a : 0.f);
+        const T z = xj - li * g;
+        T a = fabs(z) - lam * li;
+        a = a < T(0) ? T(0) : a;
+        const T xn = z > T(0) ? a : (z < T(0) ? -a : T(0));
         delta = xn - xj;
         coef = delta;
       } else {
-        const float y = li < 0.f ? -1.f : 1.f;
-        delta = (1.f - g * y) * p.lambda * fabsf(li);
+        const T y = li < T(0) ? T(-1) : T(1);
+        delta = (T(1) - g * y) * lam * fabs(li);
         if (delta < -xj)
           delta = -xj;
-        else if (delta > 1.f - xj)
-          delta = 1.f - xj;
-        coef = delta * y * p.inv_lambda_n;
+        else if (delta > T(1) - xj)
+          delta = T(1) - xj;
+        coef = delta * y * inv_ln;
       }
-      n_upd++;
-      n_read += len;
-      if (delta != 0.f) {
-        n_nz++;
-        n_scat += len;
-        scatter(p.r, c_c, coef, 4u * (uint32_t)lane < len);
+      chunk_read += len;
+      if (delta != T(0)) {
+        chunk_nz++;
+        chunk_scat += len;
+        scatter<T>(r, c0, coef, live0);
         for (uint32_t off = 128u; off < len; off += 128u) {
           Chunk a = load_chunk(p, start, len, off, lane);
-          scatter(p.r, a, coef, off + 4u * (uint32_t)lane < len);
+          scatter<T>(r, a, coef, off + e0 < len);
         }
-        if (lane == 0) atomicAdd(reinterpret_cast<float*>(&p.meta[j_c].w), delta);
-        // The prefetched meta of the next two updates predates this write.
-        const int xn_bits = __float_as_int(xj + delta);
-        if (j_n == j_c) mt_n.w = xn_bits;
-        if (j_nn == j_c) mt_nn.w = xn_bits;
+        if (lane == 0) {
+          if constexpr (sizeof(T) == 8)
+            atomicAdd(p.x64 + j, delta);
+          else
+            atomicAdd(reinterpret_cast<float*>(&p.meta[j].w), delta);
+        }
       }
-      j_c = j_n;
-      mt_c = mt_n;
-      c_c = c_n;
-      j_n = j_nn;
-      mt_n = mt_nn;
     }
+    cp_async_wait<0>();
+    __syncwarp();
+    n_upd += (unsigned)cnt;
+    n_read += chunk_read;
+    n_nz += chunk_nz;
+    n_scat += chunk_scat;
   }
   if (lane == 0) {
     atomicAdd(p.counters + CNT_UPDATES, n_upd);
@@ -179,16 +293,18 @@ __global__ void __launch_bounds__(256, 4) k_pcdm_update(UpdateParams p, uint64_t
   }
 }
 
+// The sampler's uniform draw with a 64-bit result, so the stream can be checked
+// for any n (problems themselves hold fewer than 2^31 coordinates).
 __global__ void k_debug_sample(uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
                                int64_t* out) {
-  UpdateParams p;
-  p.seed = seed;
-  p.n = n;
-  p.shrink_q32 = 0;
-  p.active = nullptr;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride)
-    out[i] = draw_coord(p, k0 + i, 0);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const uint64_t k = k0 + i;
+    acdc_u32x4 o = acdc_philox4x32_10((uint32_t)k, (uint32_t)(k >> 32), ACDC_STREAM_SAMPLER, 0u,
+                                      (uint32_t)seed, (uint32_t)(seed >> 32));
+    const uint64_t u = ((uint64_t)o.v[0] << 32) | (uint64_t)o.v[1];
+    out[i] = (int64_t)__umul64hi(u, (uint64_t)n);
+  }
 }
 
 }  // namespace
@@ -205,14 +321,35 @@ cudaError_t launch_update(const UpdateParams& p, uint64_t k_base, int warps_per_
                           cudaStream_t st) {
   if (p.count == 0 || p.n_warps <= 0) return cudaSuccess;
   if (warps_per_block < 1) warps_per_block = 1;
-  if (warps_per_block > 8) warps_per_block = 8;
+  if (warps_per_block > kMaxWarps) warps_per_block = kMaxWarps;
   cudaError_t e = cudaMemsetAsync(p.counters + CNT_WORK, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   const int blocks = (p.n_warps + warps_per_block - 1) / warps_per_block;
   dim3 grid(blocks), block(warps_per_block * 32);
-  if (p.loss == ACDC_LOSS_SVM_DUAL)
-    k_pcdm_update<ACDC_LOSS_SVM_DUAL><<<grid, block, 0, st>>>(p, k_base);
-  else
-    k_pcdm_update<ACDC_LOSS_L1_SQUARE><<<grid, block, 0, st>>>(p, k_base);
+  const bool svm = p.loss == ACDC_LOSS_SVM_DUAL;
+  // Four 42 KB blocks per SM need the shared-memory side of the L1 carveout.
+  static bool carveout_set = false;
+  if (!carveout_set) {
+    cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_SVM_DUAL, double>,
+                         cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L1_SQUARE, double>,
+                         cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_SVM_DUAL, float>,
+                         cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L1_SQUARE, float>,
+                         cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    carveout_set = true;
+  }
+  if (p.fp64) {
+    if (svm)
+      k_pcdm_update<ACDC_LOSS_SVM_DUAL, double><<<grid, block, 0, st>>>(p, k_base);
+    else
+      k_pcdm_update<ACDC_LOSS_L1_SQUARE, double><<<grid, block, 0, st>>>(p, k_base);
+  } else {
+    if (svm)
+      k_pcdm_update<ACDC_LOSS_SVM_DUAL, float><<<grid, block, 0, st>>>(p, k_base);
+    else
+      k_pcdm_update<ACDC_LOSS_L1_SQUARE, float><<<grid, block, 0, st>>>(p, k_base);
+  }
   return cudaGetLastError();
 }

@@ -1,0 +1,386 @@
+#!/usr/bin/env python3
+"""Lasso time-to-gap benchmark of the GB300 PCDM library.
+
+Workload (default): the large single Lasso of the reference's headline metric:
+A is 1,000,000 x 10,000,000 with Zipf(1.5) column lengths clipped to [1, 2000]
+and rescaled to mean 20 (about 2.0e8 nonzeros), uniform distinct rows, N(0,1)
+values scaled to unit columns; x* has 10,000 entries +-1; b = A x* + N(0, 0.01^2);
+lambda = 0.05 ||A^T b||_inf.  Seeded synthetic data (no dataset is shipped).
+PCDM with tau = 4096, FP32 bulk with FP64 refresh and duality gap every 5 epochs,
+q-shrinking after 5 epochs, FP64 polish below a relative gap of 1e-5; target
+relative duality gap 1e-6.
+
+A step is one solve from x = 0 to the target gap with the matrix resident in
+HBM; value is the mean time-to-gap in seconds (lower is better), timed with
+CUDA events on the library's stream.  e2e repeats the same metric through the
+C-ABI from pinned host buffers (upload, device layout build, solve, x read back).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs N independent replicas (one per GPU, no collective on the data
+path); value is the slowest replica's time-to-gap.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "ac-dc_gb300")
+ORACLE = os.path.join(ROOT, "oracle")
+sys.path.insert(0, PKG)
+
+WORKLOADS = {
+    "lasso_m1e6_n1e7_zipf": dict(m=1_000_000, n=10_000_000, nnz_mode=1, zipf_s=1.5, nnz_min=1,
+                                 nnz_max=2000, nnz_mean=20.0, n_star=10_000, noise_sigma=0.01,
+                                 lambda_frac=0.05, seed=0xACDC0001, tau=4096, refresh_every=5,
+                                 gap=1e-6, max_epochs=3000),
+    # the reference's CPU-sized case (2,000 x 10,000, 20 per column), for quick checks
+    "lasso_m2e3_n1e4": dict(m=2000, n=10000, nnz_mode=0, nnz_per_col=20, n_star=100,
+                            noise_sigma=0.01, lambda_frac=0.1, seed=0xACDC0000, tau=64,
+                            refresh_every=2, gap=1e-6, max_epochs=3000),
+}
+METRIC = "lasso_time_to_gap_1e-6"
+# Kernels launched per evaluation (refresh: init, scatter, finish; gap: short,
+# long, finalize; active-set omega: row count, max) and per reset (set_x + refresh).
+KERNELS_PER_EVAL = 6
+KERNELS_PER_EVAL_SHRINK = 8
+KERNELS_PER_RESET = 4
+# Columns of the update kernel's algorithmic bytes (FP32 values and state, int32
+# indices): every update reads 12 bytes per entry (value, row index, residual
+# gather) and 16 bytes of column record (start, length, Li, x); a nonzero step
+# adds 4 bytes per entry (residual scatter) and 4 bytes (x write).
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "k_pcdm_update_traffic.json")
+
+
+def epochs_file(workload):
+    """Epochs-to-gap measured by the GPU solver on a workload (written from bench runs)."""
+    return os.path.join(ROOT, "profiles", workload + "_epochs.json")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="lasso_m1e6_n1e7_zipf", choices=sorted(WORKLOADS))
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--cpu-sample-updates", type=float, default=0,
+                    help="updates timed for the CPU baseline (default: one epoch)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def dist_init(world, backend):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def max_over_ranks(dist, value, device=None):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(self.NAMES, parts[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_json(path, default=None):
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return default
+
+
+def generate(w, pinned):
+    import acdc
+    if w["nnz_mode"] == 1:
+        return acdc.gen_lasso(w["m"], w["n"], nnz_mode=acdc.NNZ_ZIPF, zipf_s=w["zipf_s"],
+                              nnz_min=w["nnz_min"], nnz_max=w["nnz_max"], nnz_mean=w["nnz_mean"],
+                              n_star=w["n_star"], noise_sigma=w["noise_sigma"],
+                              lambda_frac=w["lambda_frac"], seed=w["seed"], pinned=pinned)
+    return acdc.gen_lasso(w["m"], w["n"], nnz_per_col=w["nnz_per_col"], n_star=w["n_star"],
+                          noise_sigma=w["noise_sigma"], lambda_frac=w["lambda_frac"],
+                          seed=w["seed"], pinned=pinned)
+
+
+def settings_for(w):
+    import acdc
+    return acdc.default_settings(acdc.LOSS_L1_SQUARE, tau=w["tau"], warps_per_block=8,
+                                 refresh_every=w["refresh_every"], gap_target=w["gap"],
+                                 gap_relative=1, max_epochs=w["max_epochs"], use_shrinking=1,
+                                 shrinking_probability=0.9, shrinking_starting_iter=5, seed=1,
+                                 precision=acdc.PREC_AUTO, polish_rel_gap=1e-5)
+
+
+def cpu_time_per_epoch(inst, threads, updates):
+    """The reference's asynchronous multicore engine, restated (oracle port), timed
+    on the host cores for a bounded number of updates from x = 0."""
+    sys.path.insert(0, ORACLE)
+    import oracle
+    L = oracle.Lasso(inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals, inst.rhs, inst.lam)
+    secs = L.hogwild(updates, 1, threads)
+    return secs * inst.n / updates, secs
+
+
+def run_reference(args, w):
+    """--impl reference: the reference's CPU algorithm on all host cores."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    inst = generate(w, pinned=False)
+    upd = int(args.cpu_sample_updates) if args.cpu_sample_updates > 0 else inst.n
+    rec = load_json(epochs_file(args.workload), {})
+    epochs = rec.get("epochs_to_gap")
+    samples = []
+    for i in range(args.warmup + args.steps):
+        per_epoch, secs = cpu_time_per_epoch(inst, threads, upd)
+        if i >= args.warmup:
+            samples.append(per_epoch)
+    per_epoch = statistics.mean(samples)
+    if not epochs:
+        print(json.dumps({"impl": "reference", "unavailable":
+                          "epochs-to-gap record missing (profiles/%s)"
+                          % os.path.basename(epochs_file(args.workload))}))
+        return 0
+    value = per_epoch * epochs
+    sample = ("%d updates (%.2f epochs) of the asynchronous multicore engine from x=0 per step, "
+              "%d threads; time-to-gap = s/epoch x %d epochs (the epochs the GPU solver needs "
+              "with q-shrinking; the reference samples uniformly, so this is a lower bound)"
+              % (upd, upd / inst.n, threads, epochs))
+    line = {"metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Zipf Lasso generator)", "impl": "reference",
+            "config": {"workload": args.workload, "m": w["m"], "n": w["n"], "nnz": inst.nnz,
+                       "threads": threads, "seconds_per_epoch": per_epoch},
+            "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, w):
+    import numpy as np
+    import torch
+    import acdc
+
+    rank, world, local = dist_env()
+    if world > 1:
+        torch.cuda.set_device(local)
+    dist = dist_init(world, "nccl" if torch.cuda.is_available() else "gloo")
+    dev = torch.device("cuda", local) if torch.cuda.is_available() else None
+
+    t_gen = time.time()
+    inst = generate(w, pinned=True)
+    t_gen = time.time() - t_gen
+    s = settings_for(w)
+    ctx = acdc.Context(local)
+    p = acdc.Problem(ctx, inst, s)
+    info = p.info()
+
+    def one_solve():
+        p.reset()
+        p.reset_stats()
+        r = p.solve()
+        return r
+
+    for _ in range(args.warmup):
+        one_solve()
+    p.synchronize()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    results = []
+    for _ in range(args.steps):
+        results.append(one_solve())
+    p.synchronize()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if dist is not None:
+        dist.barrier()
+    clk = clocks.stop()
+
+    dev_ms = [r.device_ms for r in results]
+    ms_per_step = max_over_ranks(dist, statistics.mean(dev_ms), dev)
+    value = ms_per_step / 1e3
+    converged = all(r.converged for r in results)
+    epochs = [r.epochs for r in results]
+
+    # Roofline of the update kernel (algorithmic bytes over its event-timed duration).
+    upd_ms = sum(r.stats.update_ms for r in results)
+    launches = sum(r.stats.update_launches for r in results)
+    updates = sum(r.stats.updates for r in results)
+    nnz_read = sum(r.stats.nnz_read for r in results)
+    nnz_sc = sum(r.stats.nnz_scattered for r in results)
+    nonzero = sum(r.stats.nonzero_updates for r in results)
+    alg_bytes = 12 * nnz_read + 16 * updates + 4 * nnz_sc + 4 * nonzero
+    achieved = alg_bytes / (upd_ms * 1e-3) / 1e9 if upd_ms > 0 else 0.0
+    peaks = load_json(PEAKS_FILE, {})
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured"
+    if not peak:
+        peak, peak_src = 6800.0, "fallback"
+    traffic_rec = load_json(TRAFFIC_FILE, {})
+    traffic = None
+    if traffic_rec.get("dram_bytes_per_update") and launches:
+        traffic = traffic_rec["dram_bytes_per_update"] * updates / launches
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if peak else None, "traffic": traffic,
+                "peak_source": peak_src, "kernel": "k_pcdm_update",
+                "alg_bytes_per_launch": alg_bytes / launches if launches else 0,
+                "avg_launch_ms": upd_ms / launches if launches else 0}
+
+    kpe = KERNELS_PER_EVAL_SHRINK if s.use_shrinking else KERNELS_PER_EVAL
+    gpu_launches = sum(r.stats.update_launches + kpe * r.stats.eval_launches + KERNELS_PER_RESET +
+                       (1 if r.fp64_epochs else 0) for r in results)
+
+    # e2e: the same metric through the C-ABI from pinned host buffers.
+    h2d = inst.col_ptr.nbytes + inst.row_idx.nbytes + inst.vals.nbytes + inst.rhs.nbytes
+    d2h = inst.n * 8
+    e2e_times = []
+    x_last = None
+    for i in range(args.e2e_steps + 1):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        q = acdc.Problem(ctx, inst, s)
+        rq = q.solve()
+        x_last = q.get_x()
+        q.close()
+        torch.cuda.synchronize()
+        if i > 0:
+            e2e_times.append(time.perf_counter() - t)
+    e2e_value = max_over_ranks(dist, statistics.mean(e2e_times), dev)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        upd = int(args.cpu_sample_updates) if args.cpu_sample_updates > 0 else inst.n
+        per_epoch, secs = cpu_time_per_epoch(inst, threads, upd)
+        ep = statistics.mean(epochs)
+        cpu = {"value": per_epoch * ep, "unit": "s", "cores": threads, "kind": "port",
+               "sample": ("%d updates of the asynchronous multicore engine (oracle port) from x=0 "
+                          "in %.2f s on %d threads; scaled to %.0f epochs, the epochs the GPU "
+                          "solve needed (the reference samples uniformly: a lower bound)"
+                          % (upd, secs, threads, ep))}
+
+    p.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Zipf Lasso generator; inputs larger than L2)",
+            "config": {"workload": args.workload, "m": w["m"], "n": w["n"], "nnz": inst.nnz,
+                       "tau": w["tau"], "refresh_every": w["refresh_every"],
+                       "gap_target_relative": w["gap"], "q_shrinking": 0.9,
+                       "precision": "fp32 bulk, fp64 refresh/gap, fp64 polish below 1e-5",
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (no flush)", "omega": info.omega,
+                       "beta": info.sigma, "epochs": epochs,
+                       "fp64_epochs": [r.fp64_epochs for r in results],
+                       "converged": converged, "final_rel_gap": [r.eval.rel_gap for r in results],
+                       "objective": results[-1].eval.primal, "support": results[-1].eval.support,
+                       "host_wall_s": wall / args.steps, "generate_s": t_gen},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(gpu_launches),
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    ctx.close()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, w)
+    return run_ours(args, w)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -71,8 +71,22 @@ typedef struct acdc_settings {
   int32_t shrinking_starting_iter;/* epochs before shrinking starts                */
   double shrinking_probability;   /* q: probability of drawing from the active set */
   double shrink_eps;              /* Lasso active test |a_j^T r| > (1-eps) lambda   */
-  int32_t reserved[8];
+  int32_t precision;              /* ACDC_PREC_*: arithmetic of x and the residual  */
+  int32_t tau_active;             /* updates in flight while shrinking (0 = tau)   */
+  double polish_rel_gap;          /* AUTO: switch to FP64 below this relative gap  */
+  int32_t active_passes;          /* > 0: while shrinking, each bulk is this many
+                                     passes over the active set (|A|/q updates each)
+                                     instead of refresh_every epochs               */
+  int32_t reserved[3];
 } acdc_settings;
+
+/* precision: FP32 x and residual with FP64 refresh and gap (FP32), the same
+ * with the updates switched to FP64 x and residual once the relative gap falls
+ * below polish_rel_gap (AUTO, the default), or FP64 throughout (FP64).  The
+ * matrix values are stored in FP32 in every mode. */
+#define ACDC_PREC_AUTO 0
+#define ACDC_PREC_FP32 1
+#define ACDC_PREC_FP64 2
 
 /* FP64 evaluation of the current iterate (after an FP64 refresh). */
 typedef struct acdc_eval {
@@ -106,6 +120,10 @@ typedef struct acdc_solve_result {
   int32_t epochs;
   double seconds;           /* host wall time of the call                         */
   acdc_stats stats;
+  double device_ms;         /* CUDA-event time on the context stream, first launch
+                               to the last gap read-back (includes host decisions) */
+  int32_t fp64_epochs;      /* epochs run in the FP64 polish stage                */
+  int32_t reserved;
 } acdc_solve_result;
 
 typedef struct acdc_problem_info {
@@ -116,6 +134,9 @@ typedef struct acdc_problem_info {
   int64_t device_bytes;
   int32_t loss;
   int32_t tau;
+  int64_t omega_active;     /* omega over the last active set                     */
+  double active_step_scale; /* step scale while drawing from the active set       */
+  int64_t long_columns;     /* columns with more than 32 entries                  */
 } acdc_problem_info;
 
 /* ---- context ---------------------------------------------------------- */
@@ -163,6 +184,11 @@ int acdc_evaluate(acdc_problem* p, acdc_eval* out);
 /* Bulks of refresh_every epochs, each followed by refresh + gap, until the gap
  * target or max_epochs. */
 int acdc_solve(acdc_problem* p, acdc_solve_result* out);
+
+/* Restarts the solve on the resident data: x = 0, residual refreshed, sampler
+ * counter 0, FP32 stage, active set cleared (the state the engine constructor
+ * leaves, MulticoreEngineExecutor.h:25-66). */
+int acdc_problem_reset(acdc_problem* p);
 
 int acdc_get_x(acdc_problem* p, double* x);        /* n entries (alpha for loss 2) */
 int acdc_set_x(acdc_problem* p, const double* x);  /* warm start; refreshes r      */

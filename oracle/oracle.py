@@ -53,6 +53,9 @@ def lib():
         L.orc_lasso_solve.argtypes = [I64, I64, i64p, i32p, f64p, f64p, D, D, U64, D, I, I64, I64,
                                       f64p, f64p, f64p]
         L.orc_lasso_solve.restype = I64
+        L.orc_lasso_solve_shrink.argtypes = [I64, I64, i64p, i32p, f64p, f64p, D, D, U64, D, I,
+                                             I64, I64, D, D, I64, D, f64p, f64p, f64p, f64p]
+        L.orc_lasso_solve_shrink.restype = I64
         L.orc_svm_lipschitz.argtypes = [I64, i64p, f64p, D, f64p]
         L.orc_svm_residuals.argtypes = [I64, I64, i64p, i32p, f64p, f64p, D, f64p, f64p]
         L.orc_svm_updates.argtypes = [I64, i64p, i32p, f64p, f64p, D, f64p, f64p, f64p, U64, U64,
@@ -159,6 +162,23 @@ def lasso_solve(m, n, col_ptr, row_idx, vals, b, lam, beta=1.0, seed=1, target=1
                                np.ascontiguousarray(b, np.float64), lam, beta, seed, target,
                                int(rel), max_epochs, check_every, x, r, out)
     return x, r, _eval_dict(out), int(ep)
+
+
+def lasso_solve_shrink(m, n, col_ptr, row_idx, vals, b, lam, beta=1.0, seed=1, target=1e-9,
+                       rel=False, max_epochs=100000, check_every=1, q=0.9, eps=0.1,
+                       start_epoch=2, step_scale=1.0, x0=None):
+    """Serial FP64 q-shrinking solve (the build's shrinking rule; unpinned)."""
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64)
+    r = np.zeros(m)
+    out = np.zeros(9)
+    trace = np.zeros(max_epochs // max(1, check_every) + 2)
+    ep = lib().orc_lasso_solve_shrink(m, n, np.ascontiguousarray(col_ptr, np.int64),
+                                      np.ascontiguousarray(row_idx, np.int32),
+                                      np.ascontiguousarray(vals, np.float64),
+                                      np.ascontiguousarray(b, np.float64), lam, beta, seed, target,
+                                      int(rel), max_epochs, check_every, q, eps, start_epoch,
+                                      step_scale, x, r, out, trace)
+    return x, r, _eval_dict(out), int(ep), trace[:max(0, int(ep) // max(1, check_every))]
 
 
 class SVM:

@@ -171,6 +171,70 @@ int64_t orc_lasso_solve(int64_t m, int64_t n, const int64_t* col_ptr, const int3
   return epochs;
 }
 
+/* Active list in column order: x_j != 0 or |a_j^T r| > (1 - eps) lambda. */
+static int64_t build_active(int64_t n, const int64_t* col_ptr, const int32_t* row_idx,
+                            const double* vals, double lambda, double eps, const double* x,
+                            const double* r, int32_t* active) {
+  int64_t cnt = 0;
+  for (int64_t j = 0; j < n; ++j) {
+    double g = 0;
+    for (int64_t e = col_ptr[j]; e < col_ptr[j + 1]; ++e) g += vals[e] * r[row_idx[e]];
+    if (x[j] != 0 || fabs(g) > (1 - eps) * lambda) active[cnt++] = (int32_t)j;
+  }
+  return cnt;
+}
+
+int64_t orc_lasso_solve_shrink(int64_t m, int64_t n, const int64_t* col_ptr,
+                               const int32_t* row_idx, const double* vals, const double* b,
+                               double lambda, double beta, uint64_t seed, double target, int rel,
+                               int64_t max_epochs, int64_t check_every, double q, double eps,
+                               int64_t start_epoch, double step_scale, double* x, double* r,
+                               double* out, double* gap_trace) {
+  double* Li = (double*)malloc(sizeof(double) * (size_t)n);
+  int32_t* active = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+  orc_lasso_lipschitz(n, col_ptr, vals, beta, Li);
+  orc_lasso_residuals(m, n, col_ptr, row_idx, vals, b, x, r);
+  orc_lasso_eval(m, n, col_ptr, row_idx, vals, b, lambda, x, r, 0, out);
+  int64_t n_active = 0;
+  int64_t epochs = 0, checks = 0;
+  uint64_t k = 0;
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  const uint32_t q32 = q >= 1 ? 0xffffffffu : (uint32_t)(q * 4294967296.0);
+  if (check_every < 1) check_every = 1;
+  while ((rel ? out[3] : out[2]) > target && epochs < max_epochs) {
+    const int shrink = epochs >= start_epoch && n_active > 0 && q > 0;
+    for (uint64_t t = 0; t < (uint64_t)(check_every * n); ++t, ++k) {
+      uint32_t ctr[4] = {(uint32_t)k, (uint32_t)(k >> 32), 0x5A3D0001u, 0u}, o[4];
+      orc_philox4x32_10(ctr, key, o);
+      int64_t idx;
+      double scale = 1.0;
+      if (shrink && o[2] < q32) {
+        idx = active[(uint32_t)(((uint64_t)o[3] * (uint64_t)n_active) >> 32)];
+        scale = step_scale;
+      } else {
+        uint64_t u = ((uint64_t)o[0] << 32) | o[1];
+        idx = (int64_t)(((unsigned __int128)u * (uint64_t)n) >> 64);
+      }
+      double tmp = 0;
+      for (int64_t j = col_ptr[idx]; j < col_ptr[idx + 1]; ++j) tmp += vals[j] * r[row_idx[j]];
+      const double li = Li[idx] * scale;
+      tmp = soft_threshold(li * lambda, x[idx] - li * tmp) - x[idx];
+      x[idx] = x[idx] + tmp;
+      for (int64_t j = col_ptr[idx]; j < col_ptr[idx + 1]; ++j)
+        r[row_idx[j]] = r[row_idx[j]] + tmp * vals[j];
+    }
+    epochs += check_every;
+    orc_lasso_residuals(m, n, col_ptr, row_idx, vals, b, x, r);
+    orc_lasso_eval(m, n, col_ptr, row_idx, vals, b, lambda, x, r, 0, out);
+    n_active = build_active(n, col_ptr, row_idx, vals, lambda, eps, x, r, active);
+    if (gap_trace) gap_trace[checks] = out[3];
+    checks++;
+  }
+  free(Li);
+  free(active);
+  return epochs;
+}
+
 /* ---- SVM dual ---- */
 
 /* MulticoreSVMDualLoss::computeReciprocalLipConstants (MulticoreSVMDualLoss.h:48-61). */

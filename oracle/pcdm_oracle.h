@@ -51,6 +51,21 @@ int64_t orc_lasso_solve(int64_t m, int64_t n, const int64_t* col_ptr, const int3
                         uint64_t seed, double target, int rel, int64_t max_epochs,
                         int64_t check_every, double* x, double* r, double* out);
 
+/* q-shrinking (the build's definition; the reference has only the settings
+ * fields use_shrinking / shrinking_probability / shrinking_starting_iter,
+ * cpp/src/solver/settingsAndStatistics.h:60-62): after start_epoch epochs,
+ * update k draws from the active list with probability q (Philox word 2 below
+ * q * 2^32; index umulhi(word 3, |A|)), else uniformly (words 0-1).  The list
+ * {j : x_j != 0 or |a_j^T r| > (1 - eps) lambda} is rebuilt in column order at
+ * every check.  Serial, FP64; the step uses Li * step_scale while drawing from
+ * the list.  Parity of this rule is unpinned: the reference has no shrinking. */
+int64_t orc_lasso_solve_shrink(int64_t m, int64_t n, const int64_t* col_ptr,
+                               const int32_t* row_idx, const double* vals, const double* b,
+                               double lambda, double beta, uint64_t seed, double target, int rel,
+                               int64_t max_epochs, int64_t check_every, double q, double eps,
+                               int64_t start_epoch, double step_scale, double* x, double* r,
+                               double* out, double* gap_trace);
+
 /* ---- SVM dual (loss 2); the matrix is CSR by sample, m = features ---- */
 void orc_svm_lipschitz(int64_t n, const int64_t* row_ptr, const double* vals, double sigma,
                        double* Li);

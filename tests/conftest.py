@@ -33,4 +33,6 @@ def ctx():
     import acdc
     c = acdc.Context(0)
     yield c
+    import gc
+    gc.collect()  # problems hold the context; destroy it after they are gone
     c.close()

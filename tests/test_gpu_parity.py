@@ -124,7 +124,7 @@ def test_nesterov_known_optimum_on_gpu(ctx):
     p = acdc.Problem(ctx, inst, tau=64, warps_per_block=8, gap_target=1e-8, gap_relative=1,
                      refresh_every=2, max_epochs=4000, seed=3)
     r = p.solve()
-    assert r.converged
+    assert r.converged, (r.eval.rel_gap, r.epochs, r.fp64_epochs)
     assert abs(r.eval.primal - inst.f_star) <= 1e-6 * inst.f_star
     x = p.get_x()
     assert set(np.nonzero(x)[0]) == set(np.nonzero(inst.x_star)[0])
@@ -165,7 +165,7 @@ def test_long_and_empty_columns(ctx):
     p = acdc.Problem(ctx, inst, tau=16, warps_per_block=8, gap_target=1e-8, gap_relative=1,
                      refresh_every=5, max_epochs=20000, seed=2)
     r = p.solve()
-    assert r.converged
+    assert r.converged, (r.eval.rel_gap, r.epochs, r.fp64_epochs)
     assert abs(r.eval.primal - ev_o["primal"]) <= 1e-6 * abs(ev_o["primal"])
     x = p.get_x()
     assert set(np.nonzero(x)[0]) == set(np.nonzero(x_o)[0])
@@ -194,7 +194,7 @@ def test_shrinking_keeps_the_solution(ctx):
                      max_epochs=3000, use_shrinking=1, shrinking_probability=0.9,
                      shrinking_starting_iter=2, seed=4)
     r = p.solve()
-    assert r.converged
+    assert r.converged, (r.eval.rel_gap, r.epochs, r.fp64_epochs)
     assert r.eval.active > 0
     assert abs(r.eval.primal - ev_o["primal"]) <= 1e-6 * abs(ev_o["primal"])
     assert set(np.nonzero(p.get_x())[0]) == set(np.nonzero(x_o)[0])
