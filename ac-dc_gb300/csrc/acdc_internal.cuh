@@ -70,6 +70,7 @@ struct UpdateParams {
   int32_t n_warps;      // tau
   int32_t loss;
   int32_t fp64;         // 1: x and r in FP64 (x64, r64)
+  uint64_t k_base;      // sampler counter of the launch's first update (batched launches)
 };
 
 // Parameters of the evaluation kernels.
@@ -91,6 +92,40 @@ struct EvalParams {
   double lambda;
   double shrink_thresh; // Lasso: (1-eps) lambda
   int32_t loss;
+};
+
+// ---- batched solves: many problems ("slots") served by one launch per kernel ----
+
+// Control state of one slot, owned by the device between rounds.
+struct SlotCtl {
+  int32_t live;          // 1 while the slot still has lambdas to solve
+  int32_t k;             // index of the current lambda on the path
+  int32_t path_len;
+  int32_t to_fp64;       // set by the control kernel for its own block
+  uint64_t updates_here; // updates spent on the current lambda
+  uint64_t max_updates;  // per-lambda budget
+  uint64_t round_updates;// updates per round
+  double gap_target;     // relative gap per lambda
+  double polish_rel_gap;
+  const double* lambdas; // path_len values
+  double* results;       // path_len rows of kBatchResultLen doubles
+};
+
+// Row of a per-lambda result: eval_out[0..9], lambda, converged, epochs, tau.
+#define ACDC_BATCH_RESULT_LEN 14
+
+// Device view of a batch: per-slot parameters and block -> slot maps.
+struct BatchDev {
+  UpdateParams* up;
+  EvalParams* ep;
+  SlotCtl* ctl;
+  const int32_t* ublk_slot;   // update grid: slot of each block
+  const int32_t* ublk_first;  // first update block of each slot
+  const int32_t* eblk_slot;   // evaluation grid: slot of each block
+  const int32_t* eblk_first;  // first evaluation block of each slot
+  const int32_t* eblk_count;  // evaluation blocks of each slot
+  int32_t* live_count;        // slots still running
+  int32_t n_slots;
 };
 
 struct DevProblem {
@@ -185,3 +220,8 @@ cudaError_t launch_active_omega(const EvalParams& p, int32_t* rowcnt, cudaStream
 cudaError_t launch_gap(const EvalParams& p, cudaStream_t st);
 cudaError_t launch_debug_sample(uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
                                 int64_t* out, cudaStream_t st);
+// Batched round: update, refresh, gap and control kernels over every live slot.
+cudaError_t launch_batch_update(const BatchDev& b, int update_blocks, cudaStream_t st);
+cudaError_t launch_batch_eval(const BatchDev& b, int eval_blocks, cudaStream_t st);
+// One-time kernel attributes (shared-memory carveout), set at context creation.
+cudaError_t update_kernels_init();

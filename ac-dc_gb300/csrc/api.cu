@@ -75,6 +75,7 @@ extern "C" int acdc_ctx_create(int device, acdc_ctx** out) {
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
+  if (e == cudaSuccess) e = update_kernels_init();
   if (e != cudaSuccess) {
     delete ctx;
     return ACDC_ECUDA;

@@ -207,20 +207,24 @@ __device__ __forceinline__ double coord(const EvalParams& p, int64_t j, int4 mt)
 // ---- refresh ----
 
 // r64 = -b (Lasso) or 0 (SVM).
-__global__ void k_refresh_init(EvalParams p) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.m; i += stride)
+__device__ __forceinline__ void k_refresh_init_body(const EvalParams& p, const int64_t rank,
+                                                const int64_t nb) {
+  const int64_t stride = (int64_t)nb * blockDim.x;
+  for (int64_t i = (int64_t)rank * blockDim.x + threadIdx.x; i < p.m; i += stride)
     p.r64[i] = p.loss == ACDC_LOSS_L1_SQUARE ? -p.rhs64[i] : 0.0;
 }
+
+__global__ void k_refresh_init(EvalParams p) { k_refresh_init_body(p, blockIdx.x, gridDim.x); }
 
 // Each warp reads 32 consecutive coordinates, then scatters the nonzero ones
 // cooperatively: r64 += coef_j a_j with coef = x_j (Lasso) or
 // alpha_j y_j / (lambda n) after clipping alpha_j into [0, 1] (SVM).
-__global__ void k_refresh_scatter(EvalParams p) {
+__device__ __forceinline__ void k_refresh_scatter_body(const EvalParams& p, const int64_t rank,
+                                                const int64_t nb) {
   const int lane = threadIdx.x & 31;
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t warps = ((int64_t)nb * blockDim.x) >> 5;
   const double inv_ln = 1.0 / (p.lambda * (double)p.n);
-  for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < p.n;
+  for (int64_t base = (((int64_t)rank * blockDim.x + threadIdx.x) >> 5) * 32; base < p.n;
        base += warps * 32) {
     const int64_t j = base + lane;
     double coef = 0;
@@ -254,12 +258,15 @@ __global__ void k_refresh_scatter(EvalParams p) {
   }
 }
 
+__global__ void k_refresh_scatter(EvalParams p) { k_refresh_scatter_body(p, blockIdx.x, gridDim.x); }
+
 // r32 = (float) r64 and the partial sums sum r^2 (slot 0), sum b r (slot 1).
-__global__ void __launch_bounds__(ACDC_RED_THREADS) k_refresh_finish(EvalParams p) {
+__device__ __forceinline__ void k_refresh_finish_body(const EvalParams& p, const int64_t rank,
+                                                const int64_t nb) {
   __shared__ double s0[ACDC_RED_THREADS / 32], s1[ACDC_RED_THREADS / 32];
   double a0 = 0, a1 = 0;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.m; i += stride) {
+  const int64_t stride = (int64_t)nb * blockDim.x;
+  for (int64_t i = (int64_t)rank * blockDim.x + threadIdx.x; i < p.m; i += stride) {
     double v = p.r64[i];
     p.r32[i] = (float)v;
     a0 += v * v;
@@ -281,10 +288,12 @@ __global__ void __launch_bounds__(ACDC_RED_THREADS) k_refresh_finish(EvalParams 
       t0 += s0[w];
       t1 += s1[w];
     }
-    p.part[blockIdx.x * ACDC_NPART + 0] = t0;
-    p.part[blockIdx.x * ACDC_NPART + 1] = t1;
+    p.part[rank * ACDC_NPART + 0] = t0;
+    p.part[rank * ACDC_NPART + 1] = t1;
   }
 }
+
+__global__ void __launch_bounds__(ACDC_RED_THREADS) k_refresh_finish(EvalParams p) { k_refresh_finish_body(p, blockIdx.x, gridDim.x); }
 
 // ---- gap ----
 
@@ -321,15 +330,16 @@ __device__ __forceinline__ void append_active(const EvalParams& p, bool join, in
   }
 }
 
-__global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_short(EvalParams p) {
+__device__ __forceinline__ void k_gap_lasso_short_body(const EvalParams& p, const int64_t rank,
+                                                const int64_t nb) {
   __shared__ double s_l1[ACDC_RED_THREADS / 32], s_gm[ACDC_RED_THREADS / 32],
       s_sp[ACDC_RED_THREADS / 32];
   __shared__ ShortWarp sw_all[ACDC_RED_THREADS / 32];
   const int lane = threadIdx.x & 31;
   ShortWarp& sw = sw_all[threadIdx.x >> 5];
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;  // a multiple of 32
+  const int64_t stride = (int64_t)nb * blockDim.x;  // a multiple of 32
   double l1 = 0, gmax = 0, sp = 0;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < p.n;
+  for (int64_t base = (int64_t)rank * blockDim.x + (threadIdx.x & ~31); base < p.n;
        base += stride) {
     const int64_t j = base + lane;
     const bool valid = j < p.n;
@@ -407,21 +417,24 @@ __global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_short(EvalParams
       t1 = fmax(t1, s_gm[w]);
       t2 += s_sp[w];
     }
-    p.part[blockIdx.x * ACDC_NPART + 2] = t0;
-    p.part[blockIdx.x * ACDC_NPART + 3] = t1;
-    p.part[blockIdx.x * ACDC_NPART + 4] = t2;
+    p.part[rank * ACDC_NPART + 2] = t0;
+    p.part[rank * ACDC_NPART + 3] = t1;
+    p.part[rank * ACDC_NPART + 4] = t2;
   }
 }
+
+__global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_short(EvalParams p) { k_gap_lasso_short_body(p, blockIdx.x, gridDim.x); }
 
 // Lasso gap, pass 2: one warp per long column (slot 5: max |a_j^T r|).  The
 // metadata of the warp's next column is loaded while the current one is summed,
 // and each 128-entry chunk is loaded before the previous chunk's gathers.
-__global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_long(EvalParams p) {
+__device__ __forceinline__ void k_gap_lasso_long_body(const EvalParams& p, const int64_t rank,
+                                                const int64_t nb) {
   __shared__ double s_gm[ACDC_RED_THREADS / 32];
   const int lane = threadIdx.x & 31;
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t warps = ((int64_t)nb * blockDim.x) >> 5;
   double gmax = 0;
-  int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int64_t t = ((int64_t)rank * blockDim.x + threadIdx.x) >> 5;
   int64_t j = t < p.n_long ? p.long_cols[t] : 0;
   int4 mt = t < p.n_long ? p.meta[j] : make_int4(0, 0, 0, 0);
   for (; t < p.n_long; t += warps) {
@@ -469,9 +482,11 @@ __global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_long(EvalParams 
   if (threadIdx.x == 0) {
     double t1 = 0;
     for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) t1 = fmax(t1, s_gm[w]);
-    p.part[blockIdx.x * ACDC_NPART + 5] = t1;
+    p.part[rank * ACDC_NPART + 5] = t1;
   }
 }
+
+__global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_long(EvalParams p) { k_gap_lasso_long_body(p, blockIdx.x, gridDim.x); }
 
 // Columns with more than kShortLen entries, for pass 2 (order not significant).
 __global__ void k_list_long(const DevProblem d, int32_t* list, unsigned long long* count) {
@@ -494,13 +509,14 @@ __global__ void k_list_long(const DevProblem d, int32_t* list, unsigned long lon
 // SVM: one warp per sample; slots 2: sum alpha, 3: sum hinge, 4: support,
 // 5: correctly classified count.  Samples that are margin-violating or have
 // 0 < alpha < 1 join the active set.
-__global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_svm(EvalParams p) {
+__device__ __forceinline__ void k_gap_svm_body(const EvalParams& p, const int64_t rank,
+                                                const int64_t nb) {
   __shared__ double s_a[ACDC_RED_THREADS / 32], s_h[ACDC_RED_THREADS / 32],
       s_sp[ACDC_RED_THREADS / 32], s_ok[ACDC_RED_THREADS / 32];
   const int lane = threadIdx.x & 31;
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t warps = ((int64_t)nb * blockDim.x) >> 5;
   double sa = 0, sh = 0, sp = 0, ok = 0;
-  for (int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < p.n; j += warps) {
+  for (int64_t j = ((int64_t)rank * blockDim.x + threadIdx.x) >> 5; j < p.n; j += warps) {
     const int4 mt = p.meta[j];
     const int64_t start = (int64_t)(uint32_t)mt.x << 2;
     const int32_t len = mt.y;
@@ -545,12 +561,14 @@ __global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_svm(EvalParams p) {
       t2 += s_sp[w];
       t3 += s_ok[w];
     }
-    p.part[blockIdx.x * ACDC_NPART + 2] = t0;
-    p.part[blockIdx.x * ACDC_NPART + 3] = t1;
-    p.part[blockIdx.x * ACDC_NPART + 4] = t2;
-    p.part[blockIdx.x * ACDC_NPART + 5] = t3;
+    p.part[rank * ACDC_NPART + 2] = t0;
+    p.part[rank * ACDC_NPART + 3] = t1;
+    p.part[rank * ACDC_NPART + 4] = t2;
+    p.part[rank * ACDC_NPART + 5] = t3;
   }
 }
+
+__global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_svm(EvalParams p) { k_gap_svm_body(p, blockIdx.x, gridDim.x); }
 
 // Adds the per-block partials in block order and forms P, D and the gap.
 // eval_out: [0] P [1] D [2] gap [3] rel_gap [4] 0-1 accuracy [5] reg_norm
@@ -559,12 +577,12 @@ constexpr int kFinThreads = 256;
 
 // Thread t adds blocks [t*S, (t+1)*S) in order; thread 0 then adds the stripes
 // in order, so the association is fixed and the result reproducible.
-__global__ void __launch_bounds__(kFinThreads) k_finalize(EvalParams p) {
+__device__ __forceinline__ void k_finalize_body(const EvalParams& p, const int64_t nparts) {
   __shared__ double st[kFinThreads][6];
-  constexpr int S = (ACDC_RED_BLOCKS + kFinThreads - 1) / kFinThreads;
+  const int S = (int)((nparts + kFinThreads - 1) / kFinThreads);
   const bool lasso = p.loss == ACDC_LOSS_L1_SQUARE;
   double a[6] = {0, 0, 0, 0, 0, 0};
-  for (int b = threadIdx.x * S; b < (int)(threadIdx.x + 1) * S && b < ACDC_RED_BLOCKS; ++b) {
+  for (int b = threadIdx.x * S; b < (int)(threadIdx.x + 1) * S && b < nparts; ++b) {
     const double* q = p.part + b * ACDC_NPART;
     a[0] += q[0];
     a[1] += q[1];
@@ -617,6 +635,10 @@ __global__ void __launch_bounds__(kFinThreads) k_finalize(EvalParams p) {
   o[7] = gmax;
   o[8] = s4;
   o[9] = (double)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n);
+}
+
+__global__ void __launch_bounds__(kFinThreads) k_finalize(EvalParams p) {
+  k_finalize_body(p, ACDC_RED_BLOCKS);
 }
 
 }  // namespace
@@ -757,5 +779,114 @@ cudaError_t launch_gap(const EvalParams& p, cudaStream_t st) {
   else
     k_gap_svm<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
   k_finalize<<<1, kFinThreads, 0, st>>>(p);
+  return cudaGetLastError();
+}
+
+// ---- batched rounds ----
+namespace {
+
+enum { EV_REFRESH_INIT, EV_REFRESH_SCATTER, EV_REFRESH_FINISH, EV_GAP_SHORT, EV_GAP_LONG, EV_GAP_SVM };
+
+// One evaluation kernel over every live slot; a block serves its slot at rank
+// blockIdx.x - first block of the slot, out of that slot's block count.
+template <int KIND>
+__global__ void __launch_bounds__(ACDC_RED_THREADS) k_eval_batch(BatchDev b) {
+  const int s = b.eblk_slot[blockIdx.x];
+  if (!b.ctl[s].live) return;
+  const EvalParams p = b.ep[s];
+  if ((KIND == EV_GAP_SHORT || KIND == EV_GAP_LONG) && p.loss != ACDC_LOSS_L1_SQUARE) return;
+  if (KIND == EV_GAP_SVM && p.loss != ACDC_LOSS_SVM_DUAL) return;
+  const int64_t rank = (int64_t)blockIdx.x - b.eblk_first[s];
+  const int64_t nb = b.eblk_count[s];
+  if (KIND == EV_REFRESH_INIT) k_refresh_init_body(p, rank, nb);
+  if (KIND == EV_REFRESH_SCATTER) k_refresh_scatter_body(p, rank, nb);
+  if (KIND == EV_REFRESH_FINISH) k_refresh_finish_body(p, rank, nb);
+  if (KIND == EV_GAP_SHORT) k_gap_lasso_short_body(p, rank, nb);
+  if (KIND == EV_GAP_LONG) k_gap_lasso_long_body(p, rank, nb);
+  if (KIND == EV_GAP_SVM) k_gap_svm_body(p, rank, nb);
+}
+
+// One block per slot: form the gap from the slot's partials, then decide.
+//  * converged (relative gap <= target) or the lambda's update budget spent:
+//    record the result row, move to the next lambda (warm start: x and the
+//    residual carry over; FP64 coordinates are rounded back to FP32 for the next
+//    bulk) or retire the slot after the last lambda;
+//  * otherwise, below polish_rel_gap in FP32: continue in FP64 (x64 = x).
+__global__ void __launch_bounds__(kFinThreads) k_batch_control(BatchDev b) {
+  __shared__ int s_action;
+  const int s = blockIdx.x;
+  SlotCtl& c = b.ctl[s];
+  if (!c.live) return;
+  UpdateParams& up = b.up[s];
+  EvalParams& ep = b.ep[s];
+  const EvalParams epc = ep;
+  k_finalize_body(epc, b.eblk_count[s]);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double* o = epc.eval_out;
+    up.k_base += up.count;
+    c.updates_here += up.count;
+    const bool conv = o[3] <= c.gap_target;
+    int action = 0;
+    if (conv || c.updates_here >= c.max_updates) {
+      double* row = c.results + (int64_t)c.k * ACDC_BATCH_RESULT_LEN;
+      for (int i = 0; i < 10; ++i) row[i] = o[i];
+      row[10] = epc.lambda;
+      row[11] = conv ? 1.0 : 0.0;
+      row[12] = (double)((c.updates_here + (uint64_t)epc.n - 1) / (uint64_t)epc.n);
+      row[13] = (double)up.n_warps;
+      c.k++;
+      c.updates_here = 0;
+      if (c.k >= c.path_len) {
+        c.live = 0;
+        atomicSub(b.live_count, 1);
+      } else {
+        const double lam = c.lambdas[c.k];
+        ep.lambda = lam;
+        ep.shrink_thresh = 0.9 * lam;
+        if (up.loss == ACDC_LOSS_SVM_DUAL) {
+          up.lambda_d = lam * (double)up.n;
+          up.inv_lambda_n_d = 1.0 / (lam * (double)up.n);
+        } else {
+          up.lambda_d = lam;
+        }
+        if (up.fp64) action = 2;
+      }
+    } else if (!up.fp64 && o[3] <= c.polish_rel_gap) {
+      action = 1;
+    }
+    up.counters[CNT_WORK] = 0;
+    s_action = action;
+  }
+  __syncthreads();
+  const int action = s_action;
+  if (action == 1) {
+    for (int64_t j = threadIdx.x; j < epc.n; j += blockDim.x)
+      up.x64[j] = (double)__int_as_float(epc.meta[j].w);
+  } else if (action == 2) {
+    for (int64_t j = threadIdx.x; j < epc.n; j += blockDim.x)
+      epc.meta[j].w = __float_as_int((float)up.x64[j]);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && action == 1) {
+    up.fp64 = 1;
+    ep.x64 = up.x64;
+  } else if (threadIdx.x == 0 && action == 2) {
+    up.fp64 = 0;
+    ep.x64 = nullptr;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_batch_eval(const BatchDev& b, int eval_blocks, cudaStream_t st) {
+  if (eval_blocks <= 0) return cudaSuccess;
+  k_eval_batch<EV_REFRESH_INIT><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
+  k_eval_batch<EV_REFRESH_SCATTER><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
+  k_eval_batch<EV_REFRESH_FINISH><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
+  k_eval_batch<EV_GAP_SHORT><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
+  k_eval_batch<EV_GAP_LONG><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
+  k_eval_batch<EV_GAP_SVM><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
+  k_batch_control<<<b.n_slots, kFinThreads, 0, st>>>(b);
   return cudaGetLastError();
 }

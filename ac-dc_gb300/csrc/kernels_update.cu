@@ -156,12 +156,15 @@ __device__ __forceinline__ void issue_entries(WarpRing& w, const UpdateParams& p
 
 __device__ __forceinline__ int ring_next(int s, int size) { return s + 1 == size ? 0 : s + 1; }
 
+// One warp's share of an update launch; rank is the block's position among the
+// blocks serving this problem (the grid for one problem, a block range for one
+// slot of a batch).
 template <int LOSS, typename T>
-__global__ void __launch_bounds__(256, 4) k_pcdm_update(UpdateParams p, uint64_t k_base) {
-  __shared__ WarpRing rings[kMaxWarps];
+__device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t k_base,
+                                                 int64_t rank, WarpRing* rings) {
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t gwarp = (rank * blockDim.x + threadIdx.x) >> 5;
   if (gwarp >= p.n_warps) return;
   WarpRing& w = rings[wib];
   T* r = reinterpret_cast<T*>(sizeof(T) == 8 ? (void*)p.r64 : (void*)p.r);
@@ -293,6 +296,27 @@ __global__ void __launch_bounds__(256, 4) k_pcdm_update(UpdateParams p, uint64_t
   }
 }
 
+template <int LOSS, typename T>
+__global__ void __launch_bounds__(256, 4) k_pcdm_update(UpdateParams p, uint64_t k_base) {
+  __shared__ WarpRing rings[kMaxWarps];
+  pcdm_update_body<LOSS, T>(p, k_base, blockIdx.x, rings);
+}
+
+// Batched launch: each block serves one slot at rank blockIdx.x - first block
+// of that slot.  One instantiation per loss and precision; a block whose slot
+// is of another kind (or finished) returns at once.
+template <int LOSS, typename T>
+__global__ void __launch_bounds__(256, 4) k_pcdm_update_batch(BatchDev b) {
+  __shared__ WarpRing rings[kMaxWarps];
+  const int s = b.ublk_slot[blockIdx.x];
+  if (!b.ctl[s].live) return;
+  const UpdateParams p = b.up[s];
+  const bool mine = (p.loss == ACDC_LOSS_SVM_DUAL) == (LOSS == ACDC_LOSS_SVM_DUAL) &&
+                    (p.fp64 != 0) == (sizeof(T) == 8);
+  if (!mine || p.count == 0) return;
+  pcdm_update_body<LOSS, T>(p, p.k_base, (int64_t)blockIdx.x - b.ublk_first[s], rings);
+}
+
 // The sampler's uniform draw with a 64-bit result, so the stream can be checked
 // for any n (problems themselves hold fewer than 2^31 coordinates).
 __global__ void k_debug_sample(uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
@@ -327,19 +351,6 @@ cudaError_t launch_update(const UpdateParams& p, uint64_t k_base, int warps_per_
   const int blocks = (p.n_warps + warps_per_block - 1) / warps_per_block;
   dim3 grid(blocks), block(warps_per_block * 32);
   const bool svm = p.loss == ACDC_LOSS_SVM_DUAL;
-  // Four 42 KB blocks per SM need the shared-memory side of the L1 carveout.
-  static bool carveout_set = false;
-  if (!carveout_set) {
-    cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_SVM_DUAL, double>,
-                         cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L1_SQUARE, double>,
-                         cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_SVM_DUAL, float>,
-                         cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L1_SQUARE, float>,
-                         cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-    carveout_set = true;
-  }
   if (p.fp64) {
     if (svm)
       k_pcdm_update<ACDC_LOSS_SVM_DUAL, double><<<grid, block, 0, st>>>(p, k_base);
@@ -352,4 +363,29 @@ cudaError_t launch_update(const UpdateParams& p, uint64_t k_base, int warps_per_
       k_pcdm_update<ACDC_LOSS_L1_SQUARE, float><<<grid, block, 0, st>>>(p, k_base);
   }
   return cudaGetLastError();
+}
+
+cudaError_t launch_batch_update(const BatchDev& b, int update_blocks, cudaStream_t st) {
+  if (update_blocks <= 0) return cudaSuccess;
+  const dim3 grid(update_blocks), block(kMaxWarps * 32);
+  k_pcdm_update_batch<ACDC_LOSS_L1_SQUARE, float><<<grid, block, 0, st>>>(b);
+  k_pcdm_update_batch<ACDC_LOSS_L1_SQUARE, double><<<grid, block, 0, st>>>(b);
+  k_pcdm_update_batch<ACDC_LOSS_SVM_DUAL, float><<<grid, block, 0, st>>>(b);
+  k_pcdm_update_batch<ACDC_LOSS_SVM_DUAL, double><<<grid, block, 0, st>>>(b);
+  return cudaGetLastError();
+}
+
+// Four 46 KB blocks per SM need the shared-memory side of the L1 carveout.
+cudaError_t update_kernels_init() {
+  const int carve = cudaSharedmemCarveoutMaxShared;
+  const cudaFuncAttribute a = cudaFuncAttributePreferredSharedMemoryCarveout;
+  cudaError_t e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L1_SQUARE, float>, a, carve);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L1_SQUARE, double>, a, carve);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_SVM_DUAL, float>, a, carve);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_SVM_DUAL, double>, a, carve);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_L1_SQUARE, float>, a, carve);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_L1_SQUARE, double>, a, carve);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_SVM_DUAL, float>, a, carve);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_SVM_DUAL, double>, a, carve);
+  return e;
 }
