@@ -457,6 +457,59 @@ class Problem:
             pass
 
 
+class Server:
+    """Continuous batching of solve requests on one context (acdc_server_*)."""
+
+    STATES = ("queued", "running", "done", "failed")
+
+    def __init__(self, ctx, memory_budget_bytes=120 << 30, max_slots=256, quantum_rounds=4,
+                 max_epochs=2000):
+        self.ctx, self.L = ctx, ctx.L
+        opt = ServerOptions(int(memory_budget_bytes), max_slots, quantum_rounds, max_epochs)
+        h = VP()
+        ctx.check(self.L.acdc_server_create(ctx.h, C.byref(opt), C.byref(h)))
+        self.h = h
+        self.n_of = {}
+
+    def submit(self, inst, lam=None, gap_target=1e-6, seed=1):
+        cp = np.ascontiguousarray(inst.col_ptr, np.int64)
+        ri = np.ascontiguousarray(inst.row_idx, np.int32)
+        va = np.ascontiguousarray(inst.vals, np.float64)
+        rh = np.ascontiguousarray(inst.rhs, np.float64)
+        req = Request(inst.loss, 0, inst.m, inst.n, cp.ctypes.data, ri.ctypes.data if ri.size else None,
+                      va.ctypes.data if va.size else None, rh.ctypes.data,
+                      float(inst.lam if lam is None else lam), gap_target, seed)
+        t = I64()
+        self.ctx.check(self.L.acdc_server_submit(self.h, C.byref(req), C.byref(t)))
+        self.n_of[t.value] = inst.n
+        return t.value
+
+    def step(self):
+        pend = I32()
+        self.ctx.check(self.L.acdc_server_step(self.h, C.byref(pend)))
+        return pend.value
+
+    def poll(self, ticket, want_x=False):
+        res = RequestResult()
+        x = np.zeros(self.n_of[ticket]) if want_x else None
+        self.ctx.check(self.L.acdc_server_poll(self.h, ticket, C.byref(res), _ptr(x)))
+        return res, x
+
+    def release(self, ticket):
+        self.ctx.check(self.L.acdc_server_release(self.h, ticket))
+
+    def close(self):
+        if self.h:
+            self.L.acdc_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def batch_solve_path(ctx, problems, lambdas, gap_target=1e-6, max_epochs=1000, refresh_every=5,
                      autotune=1, tau_override=0, plain=0, want_x=False):
     """Solve every problem along its lambda row; returns (results[count][path], xs)."""

@@ -6,11 +6,15 @@
 // at once.  One round is: the update kernel over every live slot, the FP64
 // refresh and gap kernels over every live slot, and a control kernel with one
 // block per slot that records converged lambdas and advances the path.  The
-// round is captured once in a CUDA graph and replayed until every slot is done.
+// path solver captures one round in a CUDA graph and replays it until every
+// slot is done; the server runs rounds between admissions and retirements.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
 #include <vector>
 
 #include "acdc_internal.cuh"
@@ -37,22 +41,292 @@ int eval_blocks_for(const acdc_problem* p) {
   return (int)std::min<int64_t>(ACDC_RED_BLOCKS, std::max<int64_t>(1, work));
 }
 
+double now_seconds() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+template <typename T>
+cudaError_t upload(T** dst, const std::vector<T>& src, cudaStream_t st) {
+  cudaError_t e = cudaMalloc((void**)dst, sizeof(T) * std::max<size_t>(1, src.size()));
+  if (e == cudaSuccess && !src.empty())
+    e = cudaMemcpyAsync(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice, st);
+  return e;
+}
+
+struct SolveOpts {
+  double gap_target;
+  int32_t max_epochs;
+  int32_t refresh_every;
+  int32_t autotune;
+  int32_t tau_override;
+};
+
+// Settings of one problem for batched or plain solving: tau from the
+// autotuner (or the override), no shrinking, relative gap.
+int prepare(acdc_problem* p, const SolveOpts& o, int wpb_cap) {
+  acdc_settings s = p->s;
+  s.gap_target = o.gap_target;
+  s.gap_relative = 1;
+  s.max_epochs = o.max_epochs;
+  s.refresh_every = o.refresh_every;
+  s.use_shrinking = 0;
+  if (o.tau_override > 0)
+    s.tau = o.tau_override;
+  else if (o.autotune)
+    s.tau = autotune_tau(p->d.n, p->omega, 1.3);
+  s.warps_per_block = std::min(wpb_cap, s.tau);
+  return acdc_problem_set_settings(p, &s);
+}
+
+// Device tables and per-slot state of one set of problems solved together.
+class BatchEngine {
+ public:
+  explicit BatchEngine(acdc_ctx* ctx) : ctx_(ctx) {}
+  ~BatchEngine() { release(); }
+
+  // Slot i solves problems[i] along lambdas[i*path .. i*path+path-1].
+  int build(const std::vector<acdc_problem*>& probs, const std::vector<double>& lambdas, int path,
+            const SolveOpts& o, const std::vector<double>* gap_targets = nullptr) {
+    release();
+    cudaStream_t st = ctx_->stream;
+    const int count = (int)probs.size();
+    path_ = path;
+    count_ = count;
+    up_.assign((size_t)count, UpdateParams());
+    std::vector<EvalParams> ep((size_t)count);
+    std::vector<SlotCtl> ctl((size_t)count);
+    std::vector<int32_t> ublk_slot, ublk_first((size_t)count), eblk_slot, eblk_first((size_t)count),
+        eblk_count((size_t)count);
+    ACDC_CK(ctx_, upload(&lambdas_, lambdas, st));
+    const size_t rows = (size_t)count * path * ACDC_BATCH_RESULT_LEN;
+    ACDC_CK(ctx_, cudaMalloc((void**)&results_, sizeof(double) * std::max<size_t>(1, rows)));
+    ACDC_CK(ctx_, cudaMemsetAsync(results_, 0, sizeof(double) * std::max<size_t>(1, rows), st));
+    for (int i = 0; i < count; ++i) {
+      acdc_problem* p = probs[(size_t)i];
+      int rc = prepare(p, o, 8);
+      if (rc) return rc;
+      p->lambda = lambdas[(size_t)i * path];
+      p->active_valid = false;
+      UpdateParams& u = up_[(size_t)i];
+      std::memset(&u, 0, sizeof(u));
+      u.meta = p->d.meta;
+      u.vals = p->d.vals;
+      u.idx = p->d.idx;
+      u.r = p->d.r32;
+      u.active = p->d.active;
+      u.counters = p->d.counters;
+      u.x64 = p->d.x64;
+      u.r64 = p->d.r64;
+      u.n = p->d.n;
+      u.count = (uint64_t)o.refresh_every * (uint64_t)p->d.n;
+      u.seed = p->s.seed;
+      if (p->loss == ACDC_LOSS_SVM_DUAL) {
+        u.lambda_d = p->lambda * (double)p->d.n;
+        u.inv_lambda_n_d = 1.0 / (p->lambda * (double)p->d.n);
+      } else {
+        u.lambda_d = p->lambda;
+      }
+      u.li_scale = 1.0;
+      u.n_warps = p->s.tau;
+      u.loss = p->loss;
+      u.fp64 = p->fp64_mode ? 1 : 0;
+      u.k_base = p->k_next;
+      EvalParams& e = ep[(size_t)i];
+      std::memset(&e, 0, sizeof(e));
+      e.meta = p->d.meta;
+      e.vals = p->d.vals;
+      e.idx = p->d.idx;
+      e.r32 = p->d.r32;
+      e.r64 = p->d.r64;
+      e.rhs64 = p->d.rhs64;
+      e.active = nullptr;
+      e.counters = p->d.counters;
+      e.part = p->d.part;
+      e.eval_out = p->d.eval_out;
+      e.x64 = p->fp64_mode ? p->d.x64 : nullptr;
+      e.long_cols = p->d.long_cols;
+      e.n_long = p->d.n_long;
+      e.m = p->d.m;
+      e.n = p->d.n;
+      e.lambda = p->lambda;
+      e.shrink_thresh = 0.9 * p->lambda;
+      e.loss = p->loss;
+      SlotCtl& c = ctl[(size_t)i];
+      std::memset(&c, 0, sizeof(c));
+      c.live = 1;
+      c.path_len = path;
+      c.max_updates = (uint64_t)o.max_epochs * (uint64_t)p->d.n;
+      c.round_updates = u.count;
+      c.gap_target = gap_targets ? (*gap_targets)[(size_t)i] : o.gap_target;
+      c.polish_rel_gap = p->s.polish_rel_gap;
+      c.lambdas = lambdas_ + (size_t)i * path;
+      c.results = results_ + (size_t)i * path * ACDC_BATCH_RESULT_LEN;
+      ublk_first[(size_t)i] = (int32_t)ublk_slot.size();
+      for (int b = 0; b < (p->s.tau + 7) / 8; ++b) ublk_slot.push_back(i);
+      eblk_first[(size_t)i] = (int32_t)eblk_slot.size();
+      eblk_count[(size_t)i] = eval_blocks_for(p);
+      for (int b = 0; b < eblk_count[(size_t)i]; ++b) eblk_slot.push_back(i);
+      ACDC_CK(ctx_, cudaMemsetAsync(p->d.counters + CNT_WORK, 0, sizeof(unsigned long long), st));
+    }
+    ACDC_CK(ctx_, upload(&up_dev_, up_, st));
+    ACDC_CK(ctx_, upload(&ep_dev_, ep, st));
+    ACDC_CK(ctx_, upload(&ctl_dev_, ctl, st));
+    ACDC_CK(ctx_, upload(&ublk_slot_, ublk_slot, st));
+    ACDC_CK(ctx_, upload(&ublk_first_, ublk_first, st));
+    ACDC_CK(ctx_, upload(&eblk_slot_, eblk_slot, st));
+    ACDC_CK(ctx_, upload(&eblk_first_, eblk_first, st));
+    ACDC_CK(ctx_, upload(&eblk_count_, eblk_count, st));
+    ACDC_CK(ctx_, upload(&live_, std::vector<int32_t>{count}, st));
+    if (!h_live_) ACDC_CK(ctx_, cudaMallocHost((void**)&h_live_, sizeof(int32_t)));
+    *h_live_ = count;
+    bd_.up = up_dev_;
+    bd_.ep = ep_dev_;
+    bd_.ctl = ctl_dev_;
+    bd_.ublk_slot = ublk_slot_;
+    bd_.ublk_first = ublk_first_;
+    bd_.eblk_slot = eblk_slot_;
+    bd_.eblk_first = eblk_first_;
+    bd_.eblk_count = eblk_count_;
+    bd_.live_count = live_;
+    bd_.n_slots = count;
+    ublocks_ = (int)ublk_slot.size();
+    eblocks_ = (int)eblk_slot.size();
+    ACDC_CK(ctx_, cudaStreamSynchronize(st));
+    return ACDC_OK;
+  }
+
+  // One round on the stream, ending with the live count copied to the host.
+  cudaError_t enqueue_round() {
+    cudaStream_t st = ctx_->stream;
+    cudaError_t e = launch_batch_update(bd_, ublocks_, st);
+    if (e == cudaSuccess) e = launch_batch_eval(bd_, eblocks_, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h_live_, live_, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    return e;
+  }
+
+  // Replays one captured round until no slot is live or max_rounds is reached.
+  int run_graph(int64_t max_rounds) {
+    cudaStream_t st = ctx_->stream;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ACDC_CK(ctx_, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ce = enqueue_round();
+    cudaError_t ce2 = cudaStreamEndCapture(st, &graph);
+    if (ce != cudaSuccess || ce2 != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return acdc_cuda_error(ctx_, ce != cudaSuccess ? ce : ce2, "batch graph capture");
+    }
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return acdc_cuda_error(ctx_, ce, "cudaGraphInstantiate");
+    for (int64_t r = 0; r < max_rounds && *h_live_ > 0; ++r) {
+      ce = cudaGraphLaunch(exec, st);
+      if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+      if (ce != cudaSuccess) break;
+    }
+    cudaGraphExecDestroy(exec);
+    if (ce != cudaSuccess) return acdc_cuda_error(ctx_, ce, "batch round");
+    return ACDC_OK;
+  }
+
+  // Runs rounds without a graph (the slot set changes between calls).
+  int run_rounds(int rounds) {
+    for (int r = 0; r < rounds && *h_live_ > 0; ++r) {
+      ACDC_CK(ctx_, enqueue_round());
+      ACDC_CK(ctx_, cudaStreamSynchronize(ctx_->stream));
+    }
+    return ACDC_OK;
+  }
+
+  int32_t live() const { return h_live_ ? *h_live_ : 0; }
+
+  // Result rows and per-slot control state; also writes the device-side
+  // sampler counter and precision back into the problems.
+  int collect(const std::vector<acdc_problem*>& probs, std::vector<double>& rows,
+              std::vector<SlotCtl>& ctl) {
+    cudaStream_t st = ctx_->stream;
+    rows.assign((size_t)count_ * path_ * ACDC_BATCH_RESULT_LEN, 0.0);
+    ctl.assign((size_t)count_, SlotCtl());
+    ACDC_CK(ctx_, cudaMemcpyAsync(rows.data(), results_, sizeof(double) * rows.size(),
+                                  cudaMemcpyDeviceToHost, st));
+    ACDC_CK(ctx_, cudaMemcpyAsync(ctl.data(), ctl_dev_, sizeof(SlotCtl) * ctl.size(),
+                                  cudaMemcpyDeviceToHost, st));
+    ACDC_CK(ctx_, cudaMemcpyAsync(up_.data(), up_dev_, sizeof(UpdateParams) * up_.size(),
+                                  cudaMemcpyDeviceToHost, st));
+    ACDC_CK(ctx_, cudaStreamSynchronize(st));
+    for (int i = 0; i < count_; ++i) {
+      acdc_problem* p = probs[(size_t)i];
+      p->k_next = up_[(size_t)i].k_base;
+      p->fp64_mode = up_[(size_t)i].fp64 != 0;
+    }
+    return ACDC_OK;
+  }
+
+  void release() {
+    cudaFree(up_dev_);
+    cudaFree(ep_dev_);
+    cudaFree(ctl_dev_);
+    cudaFree(ublk_slot_);
+    cudaFree(ublk_first_);
+    cudaFree(eblk_slot_);
+    cudaFree(eblk_first_);
+    cudaFree(eblk_count_);
+    cudaFree(live_);
+    cudaFree(lambdas_);
+    cudaFree(results_);
+    up_dev_ = nullptr;
+    ep_dev_ = nullptr;
+    ctl_dev_ = nullptr;
+    ublk_slot_ = ublk_first_ = eblk_slot_ = eblk_first_ = eblk_count_ = live_ = nullptr;
+    lambdas_ = results_ = nullptr;
+    if (h_live_) {
+      cudaFreeHost(h_live_);
+      h_live_ = nullptr;
+    }
+    count_ = 0;
+  }
+
+ private:
+  acdc_ctx* ctx_;
+  std::vector<UpdateParams> up_;
+  UpdateParams* up_dev_ = nullptr;
+  EvalParams* ep_dev_ = nullptr;
+  SlotCtl* ctl_dev_ = nullptr;
+  int32_t *ublk_slot_ = nullptr, *ublk_first_ = nullptr, *eblk_slot_ = nullptr,
+          *eblk_first_ = nullptr, *eblk_count_ = nullptr, *live_ = nullptr;
+  double *lambdas_ = nullptr, *results_ = nullptr;
+  int32_t* h_live_ = nullptr;
+  BatchDev bd_{};
+  int ublocks_ = 0, eblocks_ = 0, count_ = 0, path_ = 1;
+};
+
+void row_to_result(const double* row, acdc_batch_result* out) {
+  std::memset(out, 0, sizeof(*out));
+  out->eval.primal = row[0];
+  out->eval.dual = row[1];
+  out->eval.gap = row[2];
+  out->eval.rel_gap = row[3];
+  out->eval.zero_one_accuracy = row[4];
+  out->eval.reg_norm = row[5];
+  out->eval.sq_norm = row[6];
+  out->eval.max_abs_grad = row[7];
+  out->eval.support = (int64_t)row[8];
+  out->eval.active = (int64_t)row[9];
+  out->lambda = row[10];
+  out->converged = row[11] != 0.0;
+  out->epochs = (int32_t)row[12];
+  out->tau = (int32_t)row[13];
+}
+
 int plain_path(acdc_ctx* ctx, int32_t count, acdc_problem* const* problems, const double* lambdas,
                const acdc_batch_options* opt, acdc_batch_result* results, double* const* x_out) {
+  (void)ctx;
+  const SolveOpts o{opt->gap_target, opt->max_epochs, opt->refresh_every, opt->autotune,
+                    opt->tau_override};
   for (int32_t i = 0; i < count; ++i) {
     acdc_problem* p = problems[i];
-    acdc_settings s = p->s;
-    s.gap_target = opt->gap_target;
-    s.gap_relative = 1;
-    s.max_epochs = opt->max_epochs;
-    s.refresh_every = opt->refresh_every;
-    s.use_shrinking = 0;
-    if (opt->tau_override > 0)
-      s.tau = opt->tau_override;
-    else if (opt->autotune)
-      s.tau = autotune_tau(p->d.n, p->omega, 1.3);
-    s.warps_per_block = std::min(8, s.tau);
-    int rc = acdc_problem_set_settings(p, &s);
+    int rc = prepare(p, o, 8);
     if (rc) return rc;
     for (int32_t k = 0; k < opt->path_len; ++k) {
       const double lam = lambdas[(size_t)i * opt->path_len + k];
@@ -67,7 +341,7 @@ int plain_path(acdc_ctx* ctx, int32_t count, acdc_problem* const* problems, cons
       out.lambda = lam;
       out.converged = r.converged;
       out.epochs = r.epochs;
-      out.tau = s.tau;
+      out.tau = p->s.tau;
     }
     if (x_out && x_out[i]) {
       rc = acdc_get_x(p, x_out[i]);
@@ -77,232 +351,33 @@ int plain_path(acdc_ctx* ctx, int32_t count, acdc_problem* const* problems, cons
   return ACDC_OK;
 }
 
-template <typename T>
-cudaError_t upload(T** dst, const std::vector<T>& src, cudaStream_t st) {
-  cudaError_t e = cudaMalloc((void**)dst, sizeof(T) * std::max<size_t>(1, src.size()));
-  if (e == cudaSuccess && !src.empty())
-    e = cudaMemcpyAsync(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice, st);
-  return e;
-}
-
-struct BatchBuffers {
-  UpdateParams* up = nullptr;
-  EvalParams* ep = nullptr;
-  SlotCtl* ctl = nullptr;
-  int32_t* ublk_slot = nullptr;
-  int32_t* ublk_first = nullptr;
-  int32_t* eblk_slot = nullptr;
-  int32_t* eblk_first = nullptr;
-  int32_t* eblk_count = nullptr;
-  int32_t* live = nullptr;
-  double* lambdas = nullptr;
-  double* results = nullptr;
-  int32_t* h_live = nullptr;
-  ~BatchBuffers() {
-    cudaFree(up);
-    cudaFree(ep);
-    cudaFree(ctl);
-    cudaFree(ublk_slot);
-    cudaFree(ublk_first);
-    cudaFree(eblk_slot);
-    cudaFree(eblk_first);
-    cudaFree(eblk_count);
-    cudaFree(live);
-    cudaFree(lambdas);
-    cudaFree(results);
-    if (h_live) cudaFreeHost(h_live);
-  }
-};
-
 int batched_path(acdc_ctx* ctx, int32_t count, acdc_problem* const* problems,
                  const double* lambdas, const acdc_batch_options* opt,
                  acdc_batch_result* results, double* const* x_out) {
-  cudaStream_t st = ctx->stream;
   const int path = opt->path_len;
-  std::vector<UpdateParams> up((size_t)count);
-  std::vector<EvalParams> ep((size_t)count);
-  std::vector<SlotCtl> ctl((size_t)count);
-  std::vector<int32_t> ublk_slot, ublk_first((size_t)count), eblk_slot, eblk_first((size_t)count),
-      eblk_count((size_t)count);
-  BatchBuffers bb;
-  ACDC_CK(ctx, upload(&bb.lambdas, std::vector<double>(lambdas, lambdas + (size_t)count * path), st));
-  ACDC_CK(ctx, cudaMalloc((void**)&bb.results,
-                          sizeof(double) * (size_t)count * path * ACDC_BATCH_RESULT_LEN));
-  ACDC_CK(ctx, cudaMemsetAsync(bb.results, 0,
-                               sizeof(double) * (size_t)count * path * ACDC_BATCH_RESULT_LEN, st));
-  for (int32_t i = 0; i < count; ++i) {
-    acdc_problem* p = problems[i];
-    // Settings: tau per instance from the autotuner (or the override), no shrinking.
-    acdc_settings s = p->s;
-    s.gap_target = opt->gap_target;
-    s.gap_relative = 1;
-    s.max_epochs = opt->max_epochs;
-    s.refresh_every = opt->refresh_every;
-    s.use_shrinking = 0;
-    s.tau = opt->tau_override > 0 ? opt->tau_override
-                                  : (opt->autotune ? autotune_tau(p->d.n, p->omega, 1.3) : s.tau);
-    s.warps_per_block = 8;
-    int rc = acdc_problem_set_settings(p, &s);
-    if (rc) return rc;
-    p->lambda = lambdas[(size_t)i * path];
-    p->active_valid = false;
-    // The slot's parameters (the control kernel keeps them current on the device).
-    UpdateParams u;
-    std::memset(&u, 0, sizeof(u));
-    u.meta = p->d.meta;
-    u.vals = p->d.vals;
-    u.idx = p->d.idx;
-    u.r = p->d.r32;
-    u.active = p->d.active;
-    u.counters = p->d.counters;
-    u.x64 = p->d.x64;
-    u.r64 = p->d.r64;
-    u.n = p->d.n;
-    u.count = (uint64_t)opt->refresh_every * (uint64_t)p->d.n;
-    u.seed = p->s.seed;
-    if (p->loss == ACDC_LOSS_SVM_DUAL) {
-      u.lambda_d = p->lambda * (double)p->d.n;
-      u.inv_lambda_n_d = 1.0 / (p->lambda * (double)p->d.n);
-    } else {
-      u.lambda_d = p->lambda;
-    }
-    u.li_scale = 1.0;
-    u.n_warps = s.tau;
-    u.loss = p->loss;
-    u.fp64 = p->fp64_mode ? 1 : 0;
-    u.k_base = p->k_next;
-    up[(size_t)i] = u;
-    EvalParams e;
-    std::memset(&e, 0, sizeof(e));
-    e.meta = p->d.meta;
-    e.vals = p->d.vals;
-    e.idx = p->d.idx;
-    e.r32 = p->d.r32;
-    e.r64 = p->d.r64;
-    e.rhs64 = p->d.rhs64;
-    e.active = nullptr;
-    e.counters = p->d.counters;
-    e.part = p->d.part;
-    e.eval_out = p->d.eval_out;
-    e.x64 = p->fp64_mode ? p->d.x64 : nullptr;
-    e.long_cols = p->d.long_cols;
-    e.n_long = p->d.n_long;
-    e.m = p->d.m;
-    e.n = p->d.n;
-    e.lambda = p->lambda;
-    e.shrink_thresh = 0.9 * p->lambda;
-    e.loss = p->loss;
-    ep[(size_t)i] = e;
-    SlotCtl c;
-    std::memset(&c, 0, sizeof(c));
-    c.live = 1;
-    c.k = 0;
-    c.path_len = path;
-    c.max_updates = (uint64_t)opt->max_epochs * (uint64_t)p->d.n;
-    c.round_updates = u.count;
-    c.gap_target = opt->gap_target;
-    c.polish_rel_gap = p->s.polish_rel_gap;
-    c.lambdas = bb.lambdas + (size_t)i * path;
-    c.results = bb.results + (size_t)i * path * ACDC_BATCH_RESULT_LEN;
-    ctl[(size_t)i] = c;
-    // Blocks: tau/8 update blocks and a size-proportional share of evaluation blocks.
-    ublk_first[(size_t)i] = (int32_t)ublk_slot.size();
-    for (int b = 0; b < (s.tau + 7) / 8; ++b) ublk_slot.push_back(i);
-    eblk_first[(size_t)i] = (int32_t)eblk_slot.size();
-    eblk_count[(size_t)i] = eval_blocks_for(p);
-    for (int b = 0; b < eblk_count[(size_t)i]; ++b) eblk_slot.push_back(i);
-    ACDC_CK(ctx, cudaMemsetAsync(p->d.counters + CNT_WORK, 0, sizeof(unsigned long long), st));
-  }
-  ACDC_CK(ctx, upload(&bb.up, up, st));
-  ACDC_CK(ctx, upload(&bb.ep, ep, st));
-  ACDC_CK(ctx, upload(&bb.ctl, ctl, st));
-  ACDC_CK(ctx, upload(&bb.ublk_slot, ublk_slot, st));
-  ACDC_CK(ctx, upload(&bb.ublk_first, ublk_first, st));
-  ACDC_CK(ctx, upload(&bb.eblk_slot, eblk_slot, st));
-  ACDC_CK(ctx, upload(&bb.eblk_first, eblk_first, st));
-  ACDC_CK(ctx, upload(&bb.eblk_count, eblk_count, st));
-  ACDC_CK(ctx, upload(&bb.live, std::vector<int32_t>{count}, st));
-  ACDC_CK(ctx, cudaMallocHost((void**)&bb.h_live, sizeof(int32_t)));
-  BatchDev bd;
-  bd.up = bb.up;
-  bd.ep = bb.ep;
-  bd.ctl = bb.ctl;
-  bd.ublk_slot = bb.ublk_slot;
-  bd.ublk_first = bb.ublk_first;
-  bd.eblk_slot = bb.eblk_slot;
-  bd.eblk_first = bb.eblk_first;
-  bd.eblk_count = bb.eblk_count;
-  bd.live_count = bb.live;
-  bd.n_slots = count;
-  const int ublocks = (int)ublk_slot.size();
-  const int eblocks = (int)eblk_slot.size();
-
-  // Refresh every slot's residual for its first lambda, then capture one round.
-  ACDC_CK(ctx, cudaStreamSynchronize(st));
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  ACDC_CK(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  cudaError_t ce = launch_batch_update(bd, ublocks, st);
-  if (ce == cudaSuccess) ce = launch_batch_eval(bd, eblocks, st);
-  if (ce == cudaSuccess)
-    ce = cudaMemcpyAsync(bb.h_live, bb.live, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
-  cudaError_t ce2 = cudaStreamEndCapture(st, &graph);
-  if (ce != cudaSuccess || ce2 != cudaSuccess) {
-    if (graph) cudaGraphDestroy(graph);
-    return acdc_cuda_error(ctx, ce != cudaSuccess ? ce : ce2, "batch graph capture");
-  }
-  ce = cudaGraphInstantiate(&exec, graph, 0);
-  cudaGraphDestroy(graph);
-  if (ce != cudaSuccess) return acdc_cuda_error(ctx, ce, "cudaGraphInstantiate");
-  // Rounds: each slot advances refresh_every epochs per round; a slot can take
-  // at most path_len * ceil(max_epochs / refresh_every) rounds.
+  const SolveOpts o{opt->gap_target, opt->max_epochs, opt->refresh_every, opt->autotune,
+                    opt->tau_override};
+  std::vector<acdc_problem*> probs(problems, problems + count);
+  BatchEngine eng(ctx);
+  int rc = eng.build(probs, std::vector<double>(lambdas, lambdas + (size_t)count * path), path, o);
+  if (rc) return rc;
+  // Each slot advances refresh_every epochs per round and spends at most
+  // max_epochs per lambda.
   const int64_t max_rounds =
       (int64_t)path * ((opt->max_epochs + opt->refresh_every - 1) / opt->refresh_every) + path + 1;
-  int rc = ACDC_OK;
-  *bb.h_live = count;
-  for (int64_t round = 0; round < max_rounds && *bb.h_live > 0; ++round) {
-    ce = cudaGraphLaunch(exec, st);
-    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
-    if (ce != cudaSuccess) {
-      rc = acdc_cuda_error(ctx, ce, "batch round");
-      break;
-    }
-  }
-  cudaGraphExecDestroy(exec);
-  if (rc != ACDC_OK) return rc;
-  // Results and the per-problem host state.
-  std::vector<double> rows((size_t)count * path * ACDC_BATCH_RESULT_LEN);
-  ACDC_CK(ctx, cudaMemcpyAsync(rows.data(), bb.results, sizeof(double) * rows.size(),
-                               cudaMemcpyDeviceToHost, st));
-  ACDC_CK(ctx, cudaMemcpyAsync(up.data(), bb.up, sizeof(UpdateParams) * up.size(),
-                               cudaMemcpyDeviceToHost, st));
-  ACDC_CK(ctx, cudaStreamSynchronize(st));
+  rc = eng.run_graph(max_rounds);
+  if (rc) return rc;
+  std::vector<double> rows;
+  std::vector<SlotCtl> ctl;
+  rc = eng.collect(probs, rows, ctl);
+  if (rc) return rc;
   for (int32_t i = 0; i < count; ++i) {
-    acdc_problem* p = problems[i];
-    p->k_next = up[(size_t)i].k_base;
-    p->fp64_mode = up[(size_t)i].fp64 != 0;
-    p->lambda = lambdas[(size_t)i * path + path - 1];
-    for (int k = 0; k < path; ++k) {
-      const double* row = rows.data() + ((size_t)i * path + k) * ACDC_BATCH_RESULT_LEN;
-      acdc_batch_result& out = results[(size_t)i * path + k];
-      std::memset(&out, 0, sizeof(out));
-      out.eval.primal = row[0];
-      out.eval.dual = row[1];
-      out.eval.gap = row[2];
-      out.eval.rel_gap = row[3];
-      out.eval.zero_one_accuracy = row[4];
-      out.eval.reg_norm = row[5];
-      out.eval.sq_norm = row[6];
-      out.eval.max_abs_grad = row[7];
-      out.eval.support = (int64_t)row[8];
-      out.eval.active = (int64_t)row[9];
-      out.lambda = row[10];
-      out.converged = row[11] != 0.0;
-      out.epochs = (int32_t)row[12];
-      out.tau = (int32_t)row[13];
-    }
+    problems[i]->lambda = lambdas[(size_t)i * path + path - 1];
+    for (int k = 0; k < path; ++k)
+      row_to_result(rows.data() + ((size_t)i * path + k) * ACDC_BATCH_RESULT_LEN,
+                    &results[(size_t)i * path + k]);
     if (x_out && x_out[i]) {
-      rc = acdc_get_x(p, x_out[i]);
+      rc = acdc_get_x(problems[i], x_out[i]);
       if (rc) return rc;
     }
   }
@@ -328,32 +403,214 @@ extern "C" int acdc_batch_solve_path(acdc_ctx* ctx, int32_t count, acdc_problem*
   return batched_path(ctx, count, problems, lambdas, opt, results, x_out);
 }
 
+// ---- serving ----
+
+namespace {
+struct Request {
+  int64_t ticket = 0;
+  int32_t loss = 0;
+  int64_t m = 0, n = 0;
+  std::vector<int64_t> col_ptr;
+  std::vector<int32_t> row_idx;
+  std::vector<double> vals, rhs;
+  double lambda = 0, gap_target = 1e-6;
+  uint64_t seed = 0;
+  int64_t footprint = 0;
+  acdc_problem* prob = nullptr;
+  acdc_request_result res{};
+  std::vector<double> x;
+};
+
+// Device bytes a request holds while resident, including its upload staging.
+int64_t footprint_of(int64_t m, int64_t n, int64_t nnz) {
+  const int64_t nnz_pad = nnz + 3 * n;
+  return 8 * nnz_pad + 12 * nnz + 112 * n + 32 * m + (1 << 20);
+}
+}  // namespace
+
 struct acdc_server {
-  acdc_ctx* ctx;
+  acdc_ctx* ctx = nullptr;
+  acdc_server_options opt{};
+  int64_t next_ticket = 1;
+  int64_t used_bytes = 0;
+  std::deque<Request*> queue;               // submitted, not yet admitted
+  std::vector<Request*> resident;           // on the device
+  std::map<int64_t, std::unique_ptr<Request>> all;
+  BatchEngine* engine = nullptr;
+  bool dirty = true;                        // resident set changed since the last build
 };
 
 extern "C" int acdc_server_create(acdc_ctx* ctx, const acdc_server_options* opt, acdc_server** out) {
-  (void)opt;
-  if (!ctx || !out) return ACDC_EINVAL;
-  return acdc_set_error(ctx, ACDC_EUNSUPPORTED, "server not built yet");
+  if (!ctx || !opt || !out) return ACDC_EINVAL;
+  if (opt->memory_budget_bytes <= 0 || opt->max_slots < 1 || opt->quantum_epochs < 1 ||
+      opt->max_epochs < 1)
+    return acdc_set_error(ctx, ACDC_EINVAL, "invalid server options");
+  acdc_server* s = new acdc_server();
+  s->ctx = ctx;
+  s->opt = *opt;
+  s->engine = new BatchEngine(ctx);
+  ctx->live_problems++;
+  *out = s;
+  return ACDC_OK;
 }
+
 extern "C" int acdc_server_submit(acdc_server* s, const acdc_request* req, int64_t* ticket) {
-  (void)s; (void)req; (void)ticket;
-  return ACDC_EUNSUPPORTED;
+  if (!s || !req || !ticket) return ACDC_EINVAL;
+  acdc_ctx* ctx = s->ctx;
+  if ((req->loss != ACDC_LOSS_L1_SQUARE && req->loss != ACDC_LOSS_SVM_DUAL) || req->m <= 0 ||
+      req->n <= 0 || !req->col_ptr || !req->rhs || !(req->lambda > 0) || !(req->gap_target >= 0))
+    return acdc_set_error(ctx, ACDC_EINVAL, "invalid request");
+  const int64_t nnz = req->col_ptr[req->n];
+  if (req->col_ptr[0] != 0 || nnz < 0 || (nnz > 0 && (!req->row_idx || !req->vals)))
+    return acdc_set_error(ctx, ACDC_EINVAL, "invalid request matrix");
+  const int64_t fp = footprint_of(req->m, req->n, nnz);
+  if (fp > s->opt.memory_budget_bytes)
+    return acdc_set_error(ctx, ACDC_EBUSY, "request larger than the memory budget");
+  auto r = std::make_unique<Request>();
+  r->ticket = s->next_ticket++;
+  r->loss = req->loss;
+  r->m = req->m;
+  r->n = req->n;
+  r->col_ptr.assign(req->col_ptr, req->col_ptr + req->n + 1);
+  r->row_idx.assign(req->row_idx, req->row_idx + nnz);
+  r->vals.assign(req->vals, req->vals + nnz);
+  const int64_t rhs_len = req->loss == ACDC_LOSS_L1_SQUARE ? req->m : req->n;
+  r->rhs.assign(req->rhs, req->rhs + rhs_len);
+  r->lambda = req->lambda;
+  r->gap_target = req->gap_target;
+  r->seed = req->seed;
+  r->footprint = fp;
+  r->res.state = 0;
+  r->res.submit_time = now_seconds();
+  *ticket = r->ticket;
+  s->queue.push_back(r.get());
+  s->all[r->ticket] = std::move(r);
+  return ACDC_OK;
 }
+
+namespace {
+// Retires the resident requests whose slot finished (their only lambda done):
+// records the result, reads x back and frees the device buffers.
+int retire_finished(acdc_server* s) {
+  if (s->resident.empty()) return ACDC_OK;
+  std::vector<acdc_problem*> probs;
+  for (Request* r : s->resident) probs.push_back(r->prob);
+  std::vector<double> rows;
+  std::vector<SlotCtl> ctl;
+  int rc = s->engine->collect(probs, rows, ctl);
+  if (rc) return rc;
+  std::vector<Request*> keep;
+  bool changed = false;
+  for (size_t i = 0; i < s->resident.size(); ++i) {
+    Request* r = s->resident[i];
+    if (ctl[i].live) {
+      keep.push_back(r);
+      continue;
+    }
+    acdc_batch_result br;
+    row_to_result(rows.data() + i * ACDC_BATCH_RESULT_LEN, &br);
+    r->res.eval = br.eval;
+    r->res.converged = br.converged;
+    r->res.epochs = br.epochs;
+    r->res.status = ACDC_OK;
+    r->x.assign((size_t)r->n, 0.0);
+    rc = acdc_get_x(r->prob, r->x.data());
+    if (rc) r->res.status = rc;
+    acdc_problem_destroy(r->prob);
+    r->prob = nullptr;
+    s->used_bytes -= r->footprint;
+    r->res.finish_time = now_seconds();
+    r->res.state = r->res.status == ACDC_OK ? 2 : 3;
+    changed = true;
+  }
+  s->resident.swap(keep);
+  if (changed) s->dirty = true;
+  return ACDC_OK;
+}
+
+// Admits queued requests in arrival order while slots and memory allow.
+void admit(acdc_server* s) {
+  while (!s->queue.empty() && (int32_t)s->resident.size() < s->opt.max_slots) {
+    Request* r = s->queue.front();
+    if (s->used_bytes + r->footprint > s->opt.memory_budget_bytes) break;
+    s->queue.pop_front();
+    acdc_problem* p = nullptr;
+    int rc = acdc_problem_create(s->ctx, r->loss, r->m, r->n, r->col_ptr.data(),
+                                 r->row_idx.empty() ? nullptr : r->row_idx.data(),
+                                 r->vals.empty() ? nullptr : r->vals.data(), r->rhs.data(),
+                                 r->lambda, &p);
+    r->res.start_time = now_seconds();
+    if (rc != ACDC_OK) {
+      r->res.state = 3;
+      r->res.status = rc;
+      r->res.finish_time = r->res.start_time;
+      continue;
+    }
+    p->s.seed = r->seed;
+    r->prob = p;
+    r->res.state = 1;
+    s->used_bytes += r->footprint;
+    s->resident.push_back(r);
+    s->dirty = true;
+  }
+}
+}  // namespace
+
 extern "C" int acdc_server_step(acdc_server* s, int32_t* pending) {
-  (void)s; (void)pending;
-  return ACDC_EUNSUPPORTED;
+  if (!s) return ACDC_EINVAL;
+  acdc_ctx* ctx = s->ctx;
+  ACDC_CK(ctx, cudaSetDevice(ctx->device));
+  admit(s);
+  if (!s->resident.empty()) {
+    if (s->dirty) {
+      // Rebuild the slot tables over the resident set: running slots keep their
+      // x, residual and sampler state; new ones start from x = 0.
+      std::vector<acdc_problem*> probs;
+      std::vector<double> lams, targets;
+      const SolveOpts o{1e-6, s->opt.max_epochs, 1, 1, 0};
+      for (Request* r : s->resident) {
+        probs.push_back(r->prob);
+        lams.push_back(r->lambda);
+        targets.push_back(r->gap_target);
+      }
+      int rc = s->engine->build(probs, lams, 1, o, &targets);
+      if (rc) return rc;
+      s->dirty = false;
+    }
+    int rc = s->engine->run_rounds(s->opt.quantum_epochs);
+    if (rc) return rc;
+    rc = retire_finished(s);
+    if (rc) return rc;
+  }
+  if (pending) *pending = (int32_t)(s->queue.size() + s->resident.size());
+  return ACDC_OK;
 }
+
 extern "C" int acdc_server_poll(acdc_server* s, int64_t ticket, acdc_request_result* res, double* x) {
-  (void)s; (void)ticket; (void)res; (void)x;
-  return ACDC_EUNSUPPORTED;
+  if (!s || !res) return ACDC_EINVAL;
+  auto it = s->all.find(ticket);
+  if (it == s->all.end()) return ACDC_ENOTFOUND;
+  Request* r = it->second.get();
+  *res = r->res;
+  if (x && r->res.state == 2) std::memcpy(x, r->x.data(), sizeof(double) * r->x.size());
+  return ACDC_OK;
 }
+
 extern "C" int acdc_server_release(acdc_server* s, int64_t ticket) {
-  (void)s; (void)ticket;
-  return ACDC_EUNSUPPORTED;
+  if (!s) return ACDC_EINVAL;
+  auto it = s->all.find(ticket);
+  if (it == s->all.end()) return ACDC_ENOTFOUND;
+  if (it->second->res.state < 2) return acdc_set_error(s->ctx, ACDC_EBUSY, "request still pending");
+  s->all.erase(it);
+  return ACDC_OK;
 }
+
 extern "C" int acdc_server_destroy(acdc_server* s) {
-  (void)s;
-  return ACDC_EUNSUPPORTED;
+  if (!s) return ACDC_EINVAL;
+  for (Request* r : s->resident)
+    if (r->prob) acdc_problem_destroy(r->prob);
+  delete s->engine;
+  s->ctx->live_problems--;
+  delete s;
+  return ACDC_OK;
 }

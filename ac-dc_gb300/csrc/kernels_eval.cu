@@ -435,22 +435,39 @@ __device__ __forceinline__ void k_gap_lasso_long_body(const EvalParams& p, const
   const int64_t warps = ((int64_t)nb * blockDim.x) >> 5;
   double gmax = 0;
   int64_t t = ((int64_t)rank * blockDim.x + threadIdx.x) >> 5;
+  auto first_chunk = [&](const int4& m, float4& v, int4& id) {
+    const int32_t off = 4 * lane;
+    if (off < m.y) {
+      const int64_t s = ((int64_t)(uint32_t)m.x << 2) + off;
+      v = __ldcs(reinterpret_cast<const float4*>(p.vals + s));
+      id = __ldcs(reinterpret_cast<const int4*>(p.idx + s));
+    } else {
+      v = make_float4(0.f, 0.f, 0.f, 0.f);
+      id = make_int4(0, 0, 0, 0);
+    }
+  };
+  // Two-deep pipeline: the first chunk of the next column and the record of
+  // the column after it are in flight while the current column is summed.
   int64_t j = t < p.n_long ? p.long_cols[t] : 0;
   int4 mt = t < p.n_long ? p.meta[j] : make_int4(0, 0, 0, 0);
+  float4 v0;
+  int4 id0;
+  first_chunk(mt, v0, id0);
+  int64_t jn = t + warps < p.n_long ? p.long_cols[t + warps] : 0;
+  int4 mtn = t + warps < p.n_long ? p.meta[jn] : make_int4(0, 0, 0, 0);
   for (; t < p.n_long; t += warps) {
-    const int64_t tn = t + warps;
-    const int64_t jn = tn < p.n_long ? p.long_cols[tn] : 0;
-    const int4 mtn = tn < p.n_long ? p.meta[jn] : make_int4(0, 0, 0, 0);
+    float4 v1;
+    int4 id1;
+    first_chunk(mtn, v1, id1);
+    const int64_t tnn = t + 2 * warps;
+    const int64_t jnn = tnn < p.n_long ? p.long_cols[tnn] : 0;
+    const int4 mtnn = tnn < p.n_long ? p.meta[jnn] : make_int4(0, 0, 0, 0);
     const int64_t start = (int64_t)(uint32_t)mt.x << 2;
     const int32_t len = mt.y;
     double g = 0;
     int32_t off = 4 * lane;
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    int4 id = make_int4(0, 0, 0, 0);
-    if (off < len) {
-      v = __ldcs(reinterpret_cast<const float4*>(p.vals + start + off));
-      id = __ldcs(reinterpret_cast<const int4*>(p.idx + start + off));
-    }
+    float4 v = v0;
+    int4 id = id0;
     for (; off < len; off += 128) {
       float4 vn = make_float4(0.f, 0.f, 0.f, 0.f);
       int4 idn = make_int4(0, 0, 0, 0);
@@ -476,6 +493,10 @@ __device__ __forceinline__ void k_gap_lasso_long_body(const EvalParams& p, const
     }
     j = jn;
     mt = mtn;
+    v0 = v1;
+    id0 = id1;
+    jn = jnn;
+    mtn = mtnn;
   }
   if (lane == 0) s_gm[threadIdx.x >> 5] = gmax;
   __syncthreads();

@@ -39,6 +39,12 @@ WORKLOADS = {
                                  nnz_max=2000, nnz_mean=20.0, n_star=10_000, noise_sigma=0.01,
                                  lambda_frac=0.05, seed=0xACDC0001, tau=4096, refresh_every=5,
                                  gap=1e-6, max_epochs=3000),
+    # the same generator at 3e5 x 3e6 (about 6e7 nonzeros): small enough for full
+    # profiler captures
+    "lasso_m3e5_n3e6_zipf": dict(m=300_000, n=3_000_000, nnz_mode=1, zipf_s=1.5, nnz_min=1,
+                                 nnz_max=2000, nnz_mean=20.0, n_star=3_000, noise_sigma=0.01,
+                                 lambda_frac=0.05, seed=0xACDC0001, tau=4096, refresh_every=5,
+                                 gap=1e-6, max_epochs=3000),
     # the reference's CPU-sized case (2,000 x 10,000, 20 per column), for quick checks
     "lasso_m2e3_n1e4": dict(m=2000, n=10000, nnz_mode=0, nnz_per_col=20, n_star=100,
                             noise_sigma=0.01, lambda_frac=0.1, seed=0xACDC0000, tau=64,
@@ -74,6 +80,8 @@ def parse_args():
     ap.add_argument("--cpu-sample-updates", type=float, default=0,
                     help="updates timed for the CPU baseline (default: one epoch)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--max-epochs", type=int, default=0,
+                    help="cap each solve (profiling runs; the line then reports converged=false)")
     return ap.parse_args()
 
 
@@ -376,7 +384,9 @@ def main():
     args = parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.max_epochs > 0:
+        w["max_epochs"] = args.max_epochs
     if args.impl == "reference":
         return run_reference(args, w)
     return run_ours(args, w)
