@@ -30,7 +30,7 @@ class Settings(C.Structure):
                 ("max_epochs", I32), ("use_shrinking", I32), ("shrinking_starting_iter", I32),
                 ("shrinking_probability", D), ("shrink_eps", D), ("precision", I32),
                 ("tau_active", I32), ("polish_rel_gap", D), ("active_passes", I32),
-                ("reserved", I32 * 3)]
+                ("screened_eval", I32), ("reserved", I32 * 2)]
 
 
 class Eval(C.Structure):
@@ -45,7 +45,7 @@ class Eval(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("updates", U64), ("nonzero_updates", U64), ("nnz_read", U64),
                 ("nnz_scattered", U64), ("update_ms", D), ("eval_ms", D),
-                ("update_launches", I64), ("eval_launches", I64)]
+                ("update_launches", I64), ("eval_launches", I64), ("screened_evals", I64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -15,6 +15,8 @@
 //   rhs64[]   FP64 b (m entries, Lasso) or y (n entries, SVM).
 //   col_sq[n] FP64 ||a_j||^2.
 //   active[n] q-shrinking active set (int32 coordinate list).
+//   r_ref[m]  FP64 residual of the last full evaluation (screened evaluations
+//             bound the inactive columns by their distance from it).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -40,6 +42,7 @@ enum {
   CNT_GMAX_BITS = 8,   // max |a_j^T r| as FP64 bits (non-negative, so integer max works)
   CNT_OMEGA_ACTIVE = 9,// max entries per residual row over the active columns
   CNT_NLONG = 10,      // number of columns with more than 32 entries
+  CNT_COLSQ_BITS = 11, // max ||a_j||^2 as FP64 bits
   CNT_SLOTS = 16
 };
 
@@ -48,7 +51,12 @@ enum { DEV_ERR_BAD_INDEX = 1, DEV_ERR_BAD_LAYOUT = 2, DEV_ERR_BAD_STATE = 4 };
 // Fixed grid for the reductions, so partial sums are combined in a fixed order.
 #define ACDC_RED_BLOCKS 1216
 #define ACDC_RED_THREADS 256
-#define ACDC_NPART 8  // partial slots per block
+#define ACDC_NPART 10  // partial slots per block
+// Partial slots: 0 sum r^2, 1 sum b r, 2 sum |x|, 3 max |a_j^T r| (short columns;
+// screened: active columns), 4 support, 5 max |a_j^T r| (long columns), 6 sum
+// (r - r_ref)^2 (screened), 7 and 8 max |a_j^T r| over the columns left out of
+// the active set (short, long).  SVM: 2 sum alpha, 3 sum hinge, 4 support,
+// 5 correct signs.
 
 // Parameters of one launch of the update kernel.
 struct UpdateParams {
@@ -92,6 +100,13 @@ struct EvalParams {
   double lambda;
   double shrink_thresh; // Lasso: (1-eps) lambda
   int32_t loss;
+  // Lasso with an active set: a full evaluation copies r64 into r_ref and
+  // reports the largest |a_j^T r| outside the active set (eval_out[10]); a
+  // screened one (screened = 1) gathers only the active columns and bounds
+  // the rest by eval_out[10] + col_norm_max ||r64 - r_ref|| (eval_out[11]).
+  double* r_ref = nullptr;
+  double col_norm_max = 0;
+  int32_t screened = 0;
 };
 
 // ---- batched solves: many problems ("slots") served by one launch per kernel ----
@@ -143,6 +158,7 @@ struct DevProblem {
   int32_t* long_cols = nullptr;  // columns with more than 32 entries (n_long of them)
   int64_t n_long = 0;
   double* xbuf = nullptr;   // n doubles: staging for x up/downloads
+  double* r_ref = nullptr;  // m doubles: residual of the last full evaluation (Lasso)
   double* part = nullptr;
   double* eval_out = nullptr;
   unsigned long long* counters = nullptr;
@@ -175,6 +191,10 @@ struct acdc_problem {
   // beta_A the ESO parameter of q*tau draws over the active columns.
   double li_scale_shrink = 1.0;
   int64_t omega_active = 1;
+  // Screened evaluations: valid after a full evaluation that built the active
+  // set; stale once the bound of the inactive columns reaches (1 - eps/2) lambda.
+  bool screen_valid = false;
+  double col_norm_max = 0;  // max ||a_j|| (from col_sq)
   acdc_stats stats;
   double* h_eval = nullptr;               // pinned, 16 doubles
   unsigned long long* h_counters = nullptr;  // pinned, CNT_SLOTS

@@ -59,6 +59,7 @@ extern "C" void acdc_settings_default(acdc_settings* s) {
   s->shrink_eps = 0.1;
   s->precision = ACDC_PREC_AUTO;
   s->polish_rel_gap = 1e-5;
+  s->screened_eval = 1;
 }
 
 // ---- context ----
@@ -120,6 +121,7 @@ void free_problem_buffers(DevProblem& d) {
   cudaFree(d.x64);
   cudaFree(d.rowcnt);
   cudaFree(d.long_cols);
+  cudaFree(d.r_ref);
   cudaFree(d.part);
   cudaFree(d.eval_out);
   cudaFree(d.counters);
@@ -163,6 +165,8 @@ EvalParams eval_params(acdc_problem* p, bool build_active) {
   e.x64 = p->fp64_mode ? p->d.x64 : nullptr;
   e.long_cols = p->d.long_cols;
   e.n_long = p->d.n_long;
+  if (build_active && p->loss == ACDC_LOSS_L1_SQUARE) e.r_ref = p->d.r_ref;
+  e.col_norm_max = p->col_norm_max;
   return e;
 }
 
@@ -227,6 +231,7 @@ int apply_settings(acdc_problem* p, const acdc_settings* s) {
       s->precision < ACDC_PREC_AUTO || s->precision > ACDC_PREC_FP64 || !(s->polish_rel_gap >= 0))
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid settings value");
   p->s = *s;
+  p->screen_valid = false;
   const double n = (double)p->d.n;
   if (s->sigma > 0)
     p->beta = s->sigma;
@@ -333,6 +338,7 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
   STEP(dalloc(&d.xbuf, n, &d.bytes));
   STEP(dalloc(&d.x64, n, &d.bytes));
   STEP(dalloc(&d.rowcnt, m, &d.bytes));
+  if (loss == ACDC_LOSS_L1_SQUARE) STEP(dalloc(&d.r_ref, m, &d.bytes));
   STEP(dalloc(&d.part, (int64_t)ACDC_RED_BLOCKS * ACDC_NPART, &d.bytes));
   STEP(dalloc(&d.eval_out, 16, &d.bytes));
   STEP(cudaMemsetAsync(d.part, 0, sizeof(double) * ACDC_RED_BLOCKS * ACDC_NPART, st));
@@ -376,6 +382,14 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
     cudaError_t ce = launch_refresh(e, st);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     if (ce != cudaSuccess) return fail(acdc_cuda_error(ctx, ce, "initial refresh"));
+  }
+  rc = check_status_word(p);
+  if (rc != ACDC_OK) return fail(rc);
+  {
+    const unsigned long long bits = p->h_counters[CNT_COLSQ_BITS];
+    double sq;
+    std::memcpy(&sq, &bits, sizeof(sq));
+    p->col_norm_max = std::sqrt(sq);
   }
   ctx->live_problems++;
   *out = p;
@@ -438,6 +452,7 @@ extern "C" int acdc_problem_reset(acdc_problem* p) {
   p->epochs_done = 0;
   p->updates_done = 0;
   p->active_valid = false;
+  p->screen_valid = false;
   p->li_scale_shrink = 1.0;
   p->omega_active = 1;
   EvalParams e = eval_params(p, false);
@@ -476,6 +491,7 @@ extern "C" int acdc_problem_set_lambda(acdc_problem* p, double lambda) {
   if (!(lambda > 0)) return acdc_set_error(p->ctx, ACDC_EINVAL, "lambda must be positive");
   p->lambda = lambda;
   p->active_valid = false;
+  p->screen_valid = false;
   // A new lambda starts with the FP32 bulk again (AUTO precision).
   if (p->s.precision == ACDC_PREC_AUTO) return leave_fp64(p);
   return ACDC_OK;
@@ -501,11 +517,15 @@ extern "C" int acdc_recompute_residuals(acdc_problem* p) {
 }
 
 namespace {
-// Refresh + gap; copies the result to the pinned host buffer and waits.
-int evaluate_impl(acdc_problem* p, acdc_eval* out, float* ms) {
+// Refresh + gap; copies the result to the pinned host buffer and waits.  A
+// screened evaluation (Lasso, after a full one that built the active set)
+// gathers only the active columns and bounds the others.
+int evaluate_impl(acdc_problem* p, acdc_eval* out, float* ms, bool screened = false) {
   acdc_ctx* ctx = p->ctx;
-  const bool build_active = p->s.use_shrinking != 0;
-  EvalParams e = eval_params(p, build_active);
+  screened = screened && p->screen_valid;
+  const bool build_active = p->s.use_shrinking != 0 && !screened;
+  EvalParams e = eval_params(p, p->s.use_shrinking != 0);
+  e.screened = screened ? 1 : 0;
   ACDC_CK(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
   ACDC_CK(ctx, launch_refresh(e, ctx->stream));
   ACDC_CK(ctx, launch_gap(e, ctx->stream));
@@ -519,7 +539,9 @@ int evaluate_impl(acdc_problem* p, acdc_eval* out, float* ms) {
   ACDC_CK(ctx, cudaEventElapsedTime(&t, ctx->ev[2], ctx->ev[3]));
   p->stats.eval_ms += t;
   p->stats.eval_launches++;
+  if (screened) p->stats.screened_evals++;
   if (ms) *ms = t;
+  if (!screened) p->screen_valid = build_active && e.r_ref != nullptr;
   if (build_active) {
     p->active_valid = true;
     // ESO parameter of the active-set draws: q*tau of them land on the
@@ -587,6 +609,7 @@ extern "C" int acdc_solve(acdc_problem* p, acdc_solve_result* out) {
       count = std::min<uint64_t>(count, (uint64_t)p->s.refresh_every * n);
     }
     count = std::min(count, budget - done);
+    const bool screen = shrink && p->s.screened_eval != 0 && p->screen_valid;
     UpdateParams u = update_params(p, count, shrink);
     ACDC_CK(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
     ACDC_CK(ctx, launch_update(u, p->k_next, p->s.warps_per_block, ctx->stream));
@@ -597,8 +620,19 @@ extern "C" int acdc_solve(acdc_problem* p, acdc_solve_result* out) {
     if (p->fp64_mode) done_fp64 += count;
     p->updates_done += count;
     p->epochs_done = (int64_t)(p->updates_done / n);
-    rc = evaluate_impl(p, &ev, nullptr);
+    rc = evaluate_impl(p, &ev, nullptr, screen);
     if (rc != ACDC_OK) return rc;
+    if (screen) {
+      // The bound of the inactive columns: past (1 - eps/2) lambda the next
+      // evaluation is a full one (new reference residual and active set); past
+      // lambda it may inflate this certificate, so run the full one now.
+      const double bound = p->h_eval[11];
+      if (bound >= (1.0 - 0.5 * p->s.shrink_eps) * p->lambda) p->screen_valid = false;
+      if (bound >= p->lambda && !converged(p->s, ev)) {
+        rc = evaluate_impl(p, &ev, nullptr);
+        if (rc != ACDC_OK) return rc;
+      }
+    }
     float t = 0;
     ACDC_CK(ctx, cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]));
     p->stats.update_ms += t;
@@ -639,6 +673,7 @@ extern "C" int acdc_set_x(acdc_problem* p, const double* x) {
   ACDC_CK(ctx, launch_set_x(p->d, p->fp64_mode, ctx->stream));
   ACDC_CK(ctx, cudaStreamSynchronize(ctx->stream));
   p->active_valid = false;
+  p->screen_valid = false;
   return acdc_recompute_residuals(p);
 }
 

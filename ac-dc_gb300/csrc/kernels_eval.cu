@@ -155,14 +155,22 @@ __global__ void k_max_i32(const int32_t* v, int64_t len, unsigned long long* out
 }
 
 // Li = 1/(beta ||a_j||^2) (0 for an empty column); the SVM stores y_j Li.
+// Li of every column, and the largest ||a_j||^2 (CNT_COLSQ_BITS; non-negative
+// doubles order like their bit patterns).
 __global__ void k_set_li(DevProblem d, int32_t loss, double beta) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  double sq_max = 0;
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < d.n; j += stride) {
     double sq = d.col_sq[j];
+    sq_max = fmax(sq_max, sq);
     double li = sq > 0 ? 1.0 / (beta * sq) : 0.0;
     if (loss == ACDC_LOSS_SVM_DUAL && d.rhs64[j] < 0) li = -li;
     d.meta[j].z = __float_as_int((float)li);
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sq_max = fmax(sq_max, __shfl_xor_sync(ACDC_FULL_MASK, sq_max, o));
+  if ((threadIdx.x & 31) == 0 && sq_max > 0)
+    atomicMax(d.counters + CNT_COLSQ_BITS, (unsigned long long)__double_as_longlong(sq_max));
 }
 
 __global__ void k_widen_i32(const int32_t* src, int64_t* dst, int64_t len) {
@@ -261,35 +269,50 @@ __device__ __forceinline__ void k_refresh_scatter_body(const EvalParams& p, cons
 __global__ void k_refresh_scatter(EvalParams p) { k_refresh_scatter_body(p, blockIdx.x, gridDim.x); }
 
 // r32 = (float) r64 and the partial sums sum r^2 (slot 0), sum b r (slot 1).
+// With r_ref: a screened evaluation adds sum (r - r_ref)^2 (slot 6); a full one
+// stores r64 into r_ref.
 __device__ __forceinline__ void k_refresh_finish_body(const EvalParams& p, const int64_t rank,
                                                 const int64_t nb) {
-  __shared__ double s0[ACDC_RED_THREADS / 32], s1[ACDC_RED_THREADS / 32];
-  double a0 = 0, a1 = 0;
+  __shared__ double s0[ACDC_RED_THREADS / 32], s1[ACDC_RED_THREADS / 32],
+      s2[ACDC_RED_THREADS / 32];
+  double a0 = 0, a1 = 0, a2 = 0;
   const int64_t stride = (int64_t)nb * blockDim.x;
   for (int64_t i = (int64_t)rank * blockDim.x + threadIdx.x; i < p.m; i += stride) {
     double v = p.r64[i];
     p.r32[i] = (float)v;
     a0 += v * v;
     if (p.loss == ACDC_LOSS_L1_SQUARE) a1 += p.rhs64[i] * v;
+    if (p.r_ref) {
+      if (p.screened) {
+        const double dv = v - p.r_ref[i];
+        a2 += dv * dv;
+      } else {
+        p.r_ref[i] = v;
+      }
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     a0 += __shfl_down_sync(ACDC_FULL_MASK, a0, o);
     a1 += __shfl_down_sync(ACDC_FULL_MASK, a1, o);
+    a2 += __shfl_down_sync(ACDC_FULL_MASK, a2, o);
   }
   if ((threadIdx.x & 31) == 0) {
     s0[threadIdx.x >> 5] = a0;
     s1[threadIdx.x >> 5] = a1;
+    s2[threadIdx.x >> 5] = a2;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t0 = 0, t1 = 0;
+    double t0 = 0, t1 = 0, t2 = 0;
     for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) {
       t0 += s0[w];
       t1 += s1[w];
+      t2 += s2[w];
     }
     p.part[rank * ACDC_NPART + 0] = t0;
     p.part[rank * ACDC_NPART + 1] = t1;
+    p.part[rank * ACDC_NPART + 6] = t2;
   }
 }
 
@@ -333,12 +356,12 @@ __device__ __forceinline__ void append_active(const EvalParams& p, bool join, in
 __device__ __forceinline__ void k_gap_lasso_short_body(const EvalParams& p, const int64_t rank,
                                                 const int64_t nb) {
   __shared__ double s_l1[ACDC_RED_THREADS / 32], s_gm[ACDC_RED_THREADS / 32],
-      s_sp[ACDC_RED_THREADS / 32];
+      s_sp[ACDC_RED_THREADS / 32], s_go[ACDC_RED_THREADS / 32];
   __shared__ ShortWarp sw_all[ACDC_RED_THREADS / 32];
   const int lane = threadIdx.x & 31;
   ShortWarp& sw = sw_all[threadIdx.x >> 5];
   const int64_t stride = (int64_t)nb * blockDim.x;  // a multiple of 32
-  double l1 = 0, gmax = 0, sp = 0;
+  double l1 = 0, gmax = 0, sp = 0, gout = 0;
   for (int64_t base = (int64_t)rank * blockDim.x + (threadIdx.x & ~31); base < p.n;
        base += stride) {
     const int64_t j = base + lane;
@@ -395,7 +418,9 @@ __device__ __forceinline__ void k_gap_lasso_short_body(const EvalParams& p, cons
     }
     const double ag = fabs(sw.colsum[lane]);
     if (is_short) gmax = fmax(gmax, ag);
-    append_active(p, p.active && is_short && (xv != 0.0 || ag > p.shrink_thresh), j, lane);
+    const bool join = p.active && is_short && (xv != 0.0 || ag > p.shrink_thresh);
+    if (p.active && is_short && !join) gout = fmax(gout, ag);
+    append_active(p, join, j, lane);
     __syncwarp();
   }
 #pragma unroll
@@ -403,23 +428,27 @@ __device__ __forceinline__ void k_gap_lasso_short_body(const EvalParams& p, cons
     l1 += __shfl_down_sync(ACDC_FULL_MASK, l1, o);
     gmax = fmax(gmax, __shfl_down_sync(ACDC_FULL_MASK, gmax, o));
     sp += __shfl_down_sync(ACDC_FULL_MASK, sp, o);
+    gout = fmax(gout, __shfl_down_sync(ACDC_FULL_MASK, gout, o));
   }
   if (lane == 0) {
     s_l1[threadIdx.x >> 5] = l1;
     s_gm[threadIdx.x >> 5] = gmax;
     s_sp[threadIdx.x >> 5] = sp;
+    s_go[threadIdx.x >> 5] = gout;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t0 = 0, t1 = 0, t2 = 0;
+    double t0 = 0, t1 = 0, t2 = 0, t3 = 0;
     for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) {
       t0 += s_l1[w];
       t1 = fmax(t1, s_gm[w]);
       t2 += s_sp[w];
+      t3 = fmax(t3, s_go[w]);
     }
     p.part[rank * ACDC_NPART + 2] = t0;
     p.part[rank * ACDC_NPART + 3] = t1;
     p.part[rank * ACDC_NPART + 4] = t2;
+    p.part[rank * ACDC_NPART + 7] = t3;
   }
 }
 
@@ -430,10 +459,10 @@ __global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_short(EvalParams
 // and each 128-entry chunk is loaded before the previous chunk's gathers.
 __device__ __forceinline__ void k_gap_lasso_long_body(const EvalParams& p, const int64_t rank,
                                                 const int64_t nb) {
-  __shared__ double s_gm[ACDC_RED_THREADS / 32];
+  __shared__ double s_gm[ACDC_RED_THREADS / 32], s_go[ACDC_RED_THREADS / 32];
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)nb * blockDim.x) >> 5;
-  double gmax = 0;
+  double gmax = 0, gout = 0;
   int64_t t = ((int64_t)rank * blockDim.x + threadIdx.x) >> 5;
   auto first_chunk = [&](const int4& m, float4& v, int4& id) {
     const int32_t off = 4 * lane;
@@ -487,9 +516,15 @@ __device__ __forceinline__ void k_gap_lasso_long_body(const EvalParams& p, const
     const double ag = fabs(g);
     gmax = fmax(gmax, ag);
     const double xv = coord(p, j, mt);
-    if (lane == 0 && p.active && (xv != 0.0 || ag > p.shrink_thresh)) {
-      const unsigned long long pos = atomicAdd(p.counters + CNT_ACTIVE, 1ull);
-      if (pos < (unsigned long long)p.n) p.active[pos] = (int32_t)j;
+    if (p.active) {
+      if (xv != 0.0 || ag > p.shrink_thresh) {
+        if (lane == 0) {
+          const unsigned long long pos = atomicAdd(p.counters + CNT_ACTIVE, 1ull);
+          if (pos < (unsigned long long)p.n) p.active[pos] = (int32_t)j;
+        }
+      } else {
+        gout = fmax(gout, ag);
+      }
     }
     j = jn;
     mt = mtn;
@@ -498,16 +533,91 @@ __device__ __forceinline__ void k_gap_lasso_long_body(const EvalParams& p, const
     jn = jnn;
     mtn = mtnn;
   }
-  if (lane == 0) s_gm[threadIdx.x >> 5] = gmax;
+  if (lane == 0) {
+    s_gm[threadIdx.x >> 5] = gmax;
+    s_go[threadIdx.x >> 5] = gout;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t1 = 0;
-    for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) t1 = fmax(t1, s_gm[w]);
+    double t1 = 0, t2 = 0;
+    for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) {
+      t1 = fmax(t1, s_gm[w]);
+      t2 = fmax(t2, s_go[w]);
+    }
     p.part[rank * ACDC_NPART + 5] = t1;
+    p.part[rank * ACDC_NPART + 8] = t2;
   }
 }
 
 __global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_long(EvalParams p) { k_gap_lasso_long_body(p, blockIdx.x, gridDim.x); }
+
+// Screened Lasso gap: |x|_1 and the support over every coordinate (4 bytes of
+// each column record, or the FP64 coordinate), and |a_j^T r| over the active
+// list only, one warp per active column in 128-entry chunks (slots 2-4; the
+// inactive columns are bounded in the finalize step).
+__device__ __forceinline__ void k_gap_lasso_screened_body(const EvalParams& p, const int64_t rank,
+                                                         const int64_t nb) {
+  __shared__ double s_l1[ACDC_RED_THREADS / 32], s_gm[ACDC_RED_THREADS / 32],
+      s_sp[ACDC_RED_THREADS / 32];
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)nb * blockDim.x;
+  const int32_t* xbits = reinterpret_cast<const int32_t*>(p.meta) + 3;
+  double l1 = 0, sp = 0, gmax = 0;
+  for (int64_t j = (int64_t)rank * blockDim.x + threadIdx.x; j < p.n; j += stride) {
+    const double xv = p.x64 ? p.x64[j] : (double)__int_as_float(xbits[4 * j]);
+    l1 += fabs(xv);
+    sp += xv != 0.0 ? 1.0 : 0.0;
+  }
+  const int64_t cnt = (int64_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n);
+  const int64_t warps = stride >> 5;
+  for (int64_t t = ((int64_t)rank * blockDim.x + threadIdx.x) >> 5; t < cnt; t += warps) {
+    const int4 mt = p.meta[p.active[t]];
+    const int64_t start = (int64_t)(uint32_t)mt.x << 2;
+    double g = 0;
+    for (int32_t off = 4 * lane; off < mt.y; off += 128) {
+      const float4 v = __ldcs(reinterpret_cast<const float4*>(p.vals + start + off));
+      const int4 id = __ldcs(reinterpret_cast<const int4*>(p.idx + start + off));
+      g += (double)v.x * p.r64[id.x];
+      g += (double)v.y * p.r64[id.y];
+      g += (double)v.z * p.r64[id.z];
+      g += (double)v.w * p.r64[id.w];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(ACDC_FULL_MASK, g, o);
+    gmax = fmax(gmax, fabs(g));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    l1 += __shfl_down_sync(ACDC_FULL_MASK, l1, o);
+    sp += __shfl_down_sync(ACDC_FULL_MASK, sp, o);
+    gmax = fmax(gmax, __shfl_down_sync(ACDC_FULL_MASK, gmax, o));
+  }
+  if (lane == 0) {
+    s_l1[threadIdx.x >> 5] = l1;
+    s_gm[threadIdx.x >> 5] = gmax;
+    s_sp[threadIdx.x >> 5] = sp;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0, t1 = 0, t2 = 0;
+    for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) {
+      t0 += s_l1[w];
+      t1 = fmax(t1, s_gm[w]);
+      t2 += s_sp[w];
+    }
+    double* q = p.part + rank * ACDC_NPART;
+    q[2] = t0;
+    q[3] = t1;
+    q[4] = t2;
+    q[5] = 0;
+    q[7] = 0;
+    q[8] = 0;
+  }
+}
+
+__global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_screened(EvalParams p) {
+  k_gap_lasso_screened_body(p, blockIdx.x, gridDim.x);
+}
 
 // Columns with more than kShortLen entries, for pass 2 (order not significant).
 __global__ void k_list_long(const DevProblem d, int32_t* list, unsigned long long* count) {
@@ -599,10 +709,10 @@ constexpr int kFinThreads = 256;
 // Thread t adds blocks [t*S, (t+1)*S) in order; thread 0 then adds the stripes
 // in order, so the association is fixed and the result reproducible.
 __device__ __forceinline__ void k_finalize_body(const EvalParams& p, const int64_t nparts) {
-  __shared__ double st[kFinThreads][6];
+  __shared__ double st[kFinThreads][8];
   const int S = (int)((nparts + kFinThreads - 1) / kFinThreads);
   const bool lasso = p.loss == ACDC_LOSS_L1_SQUARE;
-  double a[6] = {0, 0, 0, 0, 0, 0};
+  double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (int b = threadIdx.x * S; b < (int)(threadIdx.x + 1) * S && b < nparts; ++b) {
     const double* q = p.part + b * ACDC_NPART;
     a[0] += q[0];
@@ -611,15 +721,17 @@ __device__ __forceinline__ void k_finalize_body(const EvalParams& p, const int64
     a[4] += q[4];
     if (lasso) {
       a[3] = fmax(a[3], fmax(q[3], q[5]));  // short and long columns
+      a[6] += q[6];
+      a[7] = fmax(a[7], fmax(q[7], q[8]));
     } else {
       a[3] += q[3];
       a[5] += q[5];
     }
   }
-  for (int k = 0; k < 6; ++k) st[threadIdx.x][k] = a[k];
+  for (int k = 0; k < 8; ++k) st[threadIdx.x][k] = a[k];
   __syncthreads();
   if (threadIdx.x != 0) return;
-  double rr = 0, br = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
+  double rr = 0, br = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0, s6 = 0, s7 = 0;
   for (int t = 0; t < kFinThreads; ++t) {
     rr += st[t][0];
     br += st[t][1];
@@ -627,6 +739,8 @@ __device__ __forceinline__ void k_finalize_body(const EvalParams& p, const int64
     s4 += st[t][4];
     if (lasso) {
       s3 = fmax(s3, st[t][3]);
+      s6 += st[t][6];
+      s7 = fmax(s7, st[t][7]);
     } else {
       s3 += st[t][3];
       s5 += st[t][5];
@@ -634,8 +748,18 @@ __device__ __forceinline__ void k_finalize_body(const EvalParams& p, const int64
   }
   double P, D, acc = 0, gmax = 0;
   const double nn = (double)p.n;
+  double* o = p.eval_out;
   if (p.loss == ACDC_LOSS_L1_SQUARE) {
     gmax = s3;
+    if (p.screened) {
+      // Inactive columns: |a_j^T r| <= |a_j^T r_ref| + ||a_j|| ||r - r_ref||.
+      const double bound = o[10] + p.col_norm_max * sqrt(s6);
+      o[11] = bound;
+      gmax = fmax(gmax, bound);
+    } else {
+      o[10] = s7;
+      o[11] = 0;
+    }
     P = 0.5 * rr + p.lambda * s2;
     const double s = gmax > p.lambda ? p.lambda / gmax : 1.0;
     D = -s * br - 0.5 * s * s * rr;
@@ -645,7 +769,6 @@ __device__ __forceinline__ void k_finalize_body(const EvalParams& p, const int64
     acc = s5 / nn;
   }
   const double gap = P - D;
-  double* o = p.eval_out;
   o[0] = P;
   o[1] = D;
   o[2] = gap;
@@ -790,6 +913,11 @@ cudaError_t launch_refresh(const EvalParams& p, cudaStream_t st) {
 }
 
 cudaError_t launch_gap(const EvalParams& p, cudaStream_t st) {
+  if (p.loss == ACDC_LOSS_L1_SQUARE && p.screened) {
+    k_gap_lasso_screened<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
+    k_finalize<<<1, kFinThreads, 0, st>>>(p);
+    return cudaGetLastError();
+  }
   cudaError_t e = cudaMemsetAsync(p.counters + CNT_ACTIVE, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   if (p.loss == ACDC_LOSS_L1_SQUARE)

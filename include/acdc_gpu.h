@@ -77,7 +77,15 @@ typedef struct acdc_settings {
   int32_t active_passes;          /* > 0: while shrinking, each bulk is this many
                                      passes over the active set (|A|/q updates each)
                                      instead of refresh_every epochs               */
-  int32_t reserved[3];
+  int32_t screened_eval;          /* Lasso with shrinking, 1 (default): between
+                                     full passes, solve evaluates only the active
+                                     columns and bounds the others by
+                                     |a_j^T r| <= |a_j^T r0| + ||a_j|| ||r - r0||
+                                     (r0 = residual of the last full pass); a full
+                                     pass (and active-set rebuild) runs whenever
+                                     that bound reaches (1 - eps/2) lambda.  The
+                                     certificate stays a valid duality gap.       */
+  int32_t reserved[2];
 } acdc_settings;
 
 /* precision: FP32 x and residual with FP64 refresh and gap (FP32), the same
@@ -97,7 +105,8 @@ typedef struct acdc_eval {
   double zero_one_accuracy; /* SVM: fraction of y_i x_i^T w > 0; Lasso: 0         */
   double reg_norm;          /* Lasso ||x||_1; SVM sum alpha_i                     */
   double sq_norm;           /* Lasso ||Ax-b||^2; SVM ||w||^2                      */
-  double max_abs_grad;      /* Lasso ||A^T r||_inf; SVM 0                         */
+  double max_abs_grad;      /* Lasso ||A^T r||_inf (an upper bound of it after a
+                               screened evaluation); SVM 0                        */
   int64_t support;          /* nonzeros of x (alpha)                              */
   int64_t active;           /* size of the q-shrinking active set                 */
 } acdc_eval;
@@ -112,6 +121,7 @@ typedef struct acdc_stats {
   double eval_ms;           /* device time of refresh + gap kernels               */
   int64_t update_launches;
   int64_t eval_launches;
+  int64_t screened_evals;   /* evaluations that read only the active columns      */
 } acdc_stats;
 
 typedef struct acdc_solve_result {

@@ -200,6 +200,36 @@ def test_shrinking_keeps_the_solution(ctx):
     assert set(np.nonzero(p.get_x())[0]) == set(np.nonzero(x_o)[0])
 
 
+@pytest.mark.parametrize("precision", [acdc.PREC_AUTO, acdc.PREC_FP64])
+def test_screened_evaluations_certify_the_gap(ctx, precision):
+    """Evaluations that read only the active columns report a duality gap no
+    smaller than the full pass's on the same iterate, and the solve they stop
+    reaches the oracle's optimum and support."""
+    inst = acdc.gen_lasso(4000, 40000, nnz_mode=acdc.NNZ_ZIPF, zipf_s=1.5, nnz_min=3,
+                          nnz_max=400, nnz_mean=12.0, n_star=60, lambda_frac=0.1, seed=83)
+    x_o, ev_o = oracle_optimum(inst, target=1e-10)
+    kw = dict(tau=256, warps_per_block=8, gap_target=1e-7, refresh_every=2, max_epochs=5000,
+              use_shrinking=1, shrinking_probability=0.9, shrinking_starting_iter=2, seed=5,
+              tau_active=64, active_passes=10, precision=precision)
+    p = acdc.Problem(ctx, inst, screened_eval=1, **kw)
+    r = p.solve()
+    assert r.converged, (r.eval.rel_gap, r.epochs)
+    assert r.stats.screened_evals > 0
+    full = p.evaluate()
+    assert full["primal"] == pytest.approx(r.eval.primal, rel=1e-12)
+    assert full["rel_gap"] <= r.eval.rel_gap * (1 + 1e-9) + 1e-15
+    assert abs(r.eval.primal - ev_o["primal"]) <= 1e-6 * abs(ev_o["primal"])
+    x = p.get_x()
+    assert set(np.nonzero(x)[0]) == set(np.nonzero(x_o)[0])
+    # the same solve with full evaluations only
+    q = acdc.Problem(ctx, inst, screened_eval=0, **kw)
+    rq = q.solve()
+    assert rq.converged and rq.stats.screened_evals == 0
+    assert abs(rq.eval.primal - ev_o["primal"]) <= 1e-6 * abs(ev_o["primal"])
+    q.close()
+    p.close()
+
+
 def test_invalid_inputs_are_rejected(ctx):
     inst = acdc.gen_lasso(50, 80, nnz_per_col=3, n_star=5, seed=1)
     bad = acdc.Instance(inst.loss, inst.m, inst.n, inst.col_ptr, inst.row_idx.copy(), inst.vals,
