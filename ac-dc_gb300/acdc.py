@@ -147,6 +147,7 @@ def gpu_lib():
         L.acdc_reset_stats.argtypes = [VP]
         L.acdc_synchronize.argtypes = [VP]
         L.acdc_debug_sample.argtypes = [VP, U64, U64, U64, I64, VP]
+        L.acdc_debug_sample_noalloc.argtypes = [VP, U64, U64, U64, I64, VP]
         L.acdc_batch_solve_path.argtypes = [VP, I32, VP, VP, C.POINTER(BatchOptions), VP, VP]
         L.acdc_server_create.argtypes = [VP, C.POINTER(ServerOptions), C.POINTER(VP)]
         L.acdc_server_submit.argtypes = [VP, C.POINTER(Request), C.POINTER(I64)]
@@ -350,6 +351,16 @@ def sample_coordinate(seed, k, n):
 def debug_sample(ctx, seed, k0, count, n):
     out = np.zeros(count, np.int64)
     ctx.check(ctx.L.acdc_debug_sample(ctx.h, seed, k0, count, n, _ptr(out)))
+    return out
+
+
+NOALLOC_MAX_SAMPLES = 65536  # ACDC_NOALLOC_MAX_SAMPLES
+
+
+def debug_sample_noalloc(ctx, seed, k0, count, n):
+    """acdc_debug_sample_noalloc: the same draws through a fixed device array."""
+    out = np.zeros(max(count, 1), np.int64)[:count]
+    ctx.check(ctx.L.acdc_debug_sample_noalloc(ctx.h, seed, k0, count, n, _ptr(out)))
     return out
 
 

@@ -214,6 +214,17 @@ int acdc_synchronize(acdc_problem* p);
 int acdc_debug_sample(acdc_ctx* ctx, uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
                       int64_t* out);
 
+/* acdc_debug_sample without any allocation (no counterpart in the reference,
+ * whose sampler is a host GSL call).  The draws go to a fixed device array of
+ * ACDC_NOALLOC_MAX_SAMPLES entries (512 KiB) instead of a per-call cudaMalloc;
+ * count beyond that returns ACDC_EINVAL.  The first call on a device looks up
+ * the array's address (cudaGetSymbolAddress, may load the module): make it
+ * before any stream capture.  One array per device: calls that overlap on a
+ * device race and must be serialised by the caller. */
+#define ACDC_NOALLOC_MAX_SAMPLES 65536
+int acdc_debug_sample_noalloc(acdc_ctx* ctx, uint64_t seed, uint64_t k0, uint64_t count,
+                              int64_t n, int64_t* out);
+
 /* ---- batched lambda paths (many instances, one launch sequence) --------- */
 typedef struct acdc_batch_options {
   int32_t path_len;         /* lambdas per instance                               */

@@ -1,0 +1,26 @@
+"""acdc_debug_sample_noalloc against acdc_debug_sample: the fixed-scratch
+variant (no allocation) returns the same draws on two calls in a row, and
+refuses counts beyond its scratch.  Collected last, so it also runs after every
+other GPU test has used the device."""
+import numpy as np
+import pytest
+
+import acdc
+
+pytestmark = pytest.mark.gpu
+
+
+def test_two_calls_in_a_row_match_the_allocating_entry_point(ctx):
+    cases = [(0xACDC0001, 1000, 4096, 10**7), (12345, 7, acdc.NOALLOC_MAX_SAMPLES, 2**33 + 7)]
+    for seed, k0, count, n in cases:
+        got = acdc.debug_sample_noalloc(ctx, seed, k0, count, n)
+        want = acdc.debug_sample(ctx, seed, k0, count, n)
+        np.testing.assert_array_equal(got, want)
+        assert got.min() >= 0 and got.max() < n
+
+
+def test_sizes_beyond_the_scratch_are_refused(ctx):
+    with pytest.raises(acdc.AcdcError) as e:
+        acdc.debug_sample_noalloc(ctx, 1, 0, acdc.NOALLOC_MAX_SAMPLES + 1, 100)
+    assert e.value.code == acdc.EINVAL
+    assert len(acdc.debug_sample_noalloc(ctx, 1, 0, 0, 100)) == 0
