@@ -43,6 +43,8 @@ enum {
   CNT_OMEGA_ACTIVE = 9,// max entries per residual row over the active columns
   CNT_NLONG = 10,      // number of columns with more than 32 entries
   CNT_COLSQ_BITS = 11, // max ||a_j||^2 as FP64 bits
+  CNT_HOT = 12,        // hot-set length
+  CNT_OMEGA_HOT = 13,  // max entries per residual row over the hot columns
   CNT_SLOTS = 16
 };
 
@@ -55,8 +57,8 @@ enum { DEV_ERR_BAD_INDEX = 1, DEV_ERR_BAD_LAYOUT = 2, DEV_ERR_BAD_STATE = 4 };
 // Partial slots: 0 sum r^2, 1 sum b r, 2 sum |x|, 3 max |a_j^T r| (short columns;
 // screened: active columns), 4 support, 5 max |a_j^T r| (long columns), 6 sum
 // (r - r_ref)^2 (screened), 7 and 8 max |a_j^T r| over the columns left out of
-// the active set (short, long).  SVM: 2 sum alpha, 3 sum hinge, 4 support,
-// 5 correct signs.
+// the active set (short, long), 9 max KKT violation over the active set.  SVM:
+// 2 sum alpha, 3 sum hinge, 4 support, 5 correct signs.
 
 // Parameters of one launch of the update kernel.
 struct UpdateParams {
@@ -75,6 +77,9 @@ struct UpdateParams {
   double inv_lambda_n_d;// SVM scatter factor 1/(lambda n)
   double li_scale;      // multiplies the stored Li (1 unless beta changes)
   uint32_t shrink_q32;  // probability of an active-set draw, scaled by 2^32 (0 = off)
+  uint32_t hot_q32 = 0;         // probability of a hot-set draw (part of shrink_q32)
+  const int32_t* hot = nullptr;  // hot list (length in counters[CNT_HOT])
+  double li_scale_hot = 1.0;     // step scale of hot-set draws
   int32_t n_warps;      // tau
   int32_t loss;
   int32_t fp64;         // 1: x and r in FP64 (x64, r64)
@@ -107,6 +112,14 @@ struct EvalParams {
   double* r_ref = nullptr;
   double col_norm_max = 0;
   int32_t screened = 0;
+  // Active-set KKT violations (Lasso with an active set): the active pass writes
+  // viol[t] for active[t] and the block maxima (slot 9); the hot-set kernels
+  // list the columns above hot_frac times the maximum and their row neighbours.
+  float* viol = nullptr;
+  int32_t* hot = nullptr;
+  uint8_t* row_flag = nullptr;  // m bytes, zero between evaluations
+  int32_t* rowcnt = nullptr;
+  double hot_frac = 0;
 };
 
 // ---- batched solves: many problems ("slots") served by one launch per kernel ----
@@ -159,6 +172,9 @@ struct DevProblem {
   int64_t n_long = 0;
   double* xbuf = nullptr;   // n doubles: staging for x up/downloads
   double* r_ref = nullptr;  // m doubles: residual of the last full evaluation (Lasso)
+  float* viol = nullptr;    // n floats: KKT violation of active[t] (Lasso)
+  int32_t* hot = nullptr;   // n ints: hot list (Lasso)
+  uint8_t* row_flag = nullptr;  // m bytes: rows of the hot columns (Lasso)
   double* part = nullptr;
   double* eval_out = nullptr;
   unsigned long long* counters = nullptr;
@@ -195,6 +211,10 @@ struct acdc_problem {
   // set; stale once the bound of the inactive columns reaches (1 - eps/2) lambda.
   bool screen_valid = false;
   double col_norm_max = 0;  // max ||a_j|| (from col_sq)
+  // Hot set (built after each evaluation while shrinking, Lasso).
+  int64_t hot_count = 0;
+  double hot_q = 0;
+  double li_scale_hot = 1.0;
   acdc_stats stats;
   double* h_eval = nullptr;               // pinned, 16 doubles
   unsigned long long* h_counters = nullptr;  // pinned, CNT_SLOTS
@@ -238,6 +258,10 @@ cudaError_t launch_list_long(const DevProblem& d, int32_t* list, unsigned long l
 // omega over the active list (counters[CNT_OMEGA_ACTIVE]); rowcnt holds m ints.
 cudaError_t launch_active_omega(const EvalParams& p, int32_t* rowcnt, cudaStream_t st);
 cudaError_t launch_gap(const EvalParams& p, cudaStream_t st);
+// Active-set violations (Lasso, after a full gap pass that built the list).
+cudaError_t launch_active_viol(const EvalParams& p, cudaStream_t st);
+// Hot list from the violations of the last evaluation; zeroes CNT_HOT first.
+cudaError_t launch_hot_set(const EvalParams& p, cudaStream_t st);
 cudaError_t launch_debug_sample(uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
                                 int64_t* out, cudaStream_t st);
 // Batched round: update, refresh, gap and control kernels over every live slot.

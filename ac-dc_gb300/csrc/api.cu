@@ -60,6 +60,7 @@ extern "C" void acdc_settings_default(acdc_settings* s) {
   s->precision = ACDC_PREC_AUTO;
   s->polish_rel_gap = 1e-5;
   s->screened_eval = 1;
+  s->hot_threshold = 0.1;
 }
 
 // ---- context ----
@@ -122,6 +123,9 @@ void free_problem_buffers(DevProblem& d) {
   cudaFree(d.rowcnt);
   cudaFree(d.long_cols);
   cudaFree(d.r_ref);
+  cudaFree(d.viol);
+  cudaFree(d.hot);
+  cudaFree(d.row_flag);
   cudaFree(d.part);
   cudaFree(d.eval_out);
   cudaFree(d.counters);
@@ -143,6 +147,12 @@ int check_status_word(acdc_problem* p) {
     return acdc_set_error(ctx, ACDC_EDEVICE, buf);
   }
   return ACDC_OK;
+}
+
+// The hot-set tier: Lasso with q-shrinking and screened evaluations.
+bool hot_enabled(const acdc_problem* p) {
+  return p->loss == ACDC_LOSS_L1_SQUARE && p->s.use_shrinking && p->s.screened_eval &&
+         p->s.hot_threshold > 0;
 }
 
 EvalParams eval_params(acdc_problem* p, bool build_active) {
@@ -167,6 +177,13 @@ EvalParams eval_params(acdc_problem* p, bool build_active) {
   e.n_long = p->d.n_long;
   if (build_active && p->loss == ACDC_LOSS_L1_SQUARE) e.r_ref = p->d.r_ref;
   e.col_norm_max = p->col_norm_max;
+  if (build_active && hot_enabled(p)) {
+    e.viol = p->d.viol;
+    e.hot = p->d.hot;
+    e.row_flag = p->d.row_flag;
+    e.rowcnt = p->d.rowcnt;
+    e.hot_frac = p->s.hot_threshold;
+  }
   return e;
 }
 
@@ -201,6 +218,12 @@ UpdateParams update_params(acdc_problem* p, uint64_t count, bool shrink) {
     u.shrink_q32 = (uint32_t)(q * 4294967296.0);
   u.n_warps = (shrink && p->s.tau_active > 0) ? p->s.tau_active : p->s.tau;
   u.loss = p->loss;
+  if (shrink && u.shrink_q32 && p->hot_count > 0 && p->hot_q > 0) {
+    u.hot = p->d.hot;
+    u.hot_q32 = (uint32_t)std::min(4294967295.0, p->hot_q * 4294967296.0);
+    if (u.hot_q32 > u.shrink_q32) u.hot_q32 = u.shrink_q32;
+    u.li_scale_hot = p->li_scale_hot;
+  }
   return u;
 }
 
@@ -228,7 +251,8 @@ int apply_settings(acdc_problem* p, const acdc_settings* s) {
       s->refresh_every < 1 ||
       s->max_epochs < 0 || !(s->gap_target >= 0) || s->shrinking_probability < 0 ||
       s->shrinking_probability > 1 || s->shrink_eps < 0 || s->shrink_eps >= 1 ||
-      s->precision < ACDC_PREC_AUTO || s->precision > ACDC_PREC_FP64 || !(s->polish_rel_gap >= 0))
+      s->precision < ACDC_PREC_AUTO || s->precision > ACDC_PREC_FP64 || !(s->polish_rel_gap >= 0) ||
+      !(s->hot_threshold >= 0))
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid settings value");
   p->s = *s;
   p->screen_valid = false;
@@ -338,7 +362,13 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
   STEP(dalloc(&d.xbuf, n, &d.bytes));
   STEP(dalloc(&d.x64, n, &d.bytes));
   STEP(dalloc(&d.rowcnt, m, &d.bytes));
-  if (loss == ACDC_LOSS_L1_SQUARE) STEP(dalloc(&d.r_ref, m, &d.bytes));
+  if (loss == ACDC_LOSS_L1_SQUARE) {
+    STEP(dalloc(&d.r_ref, m, &d.bytes));
+    STEP(dalloc(&d.viol, n, &d.bytes));
+    STEP(dalloc(&d.hot, n, &d.bytes));
+    STEP(dalloc(&d.row_flag, m, &d.bytes));
+    STEP(cudaMemsetAsync(d.row_flag, 0, m, st));
+  }
   STEP(dalloc(&d.part, (int64_t)ACDC_RED_BLOCKS * ACDC_NPART, &d.bytes));
   STEP(dalloc(&d.eval_out, 16, &d.bytes));
   STEP(cudaMemsetAsync(d.part, 0, sizeof(double) * ACDC_RED_BLOCKS * ACDC_NPART, st));
@@ -455,6 +485,9 @@ extern "C" int acdc_problem_reset(acdc_problem* p) {
   p->screen_valid = false;
   p->li_scale_shrink = 1.0;
   p->omega_active = 1;
+  p->hot_count = 0;
+  p->hot_q = 0;
+  p->li_scale_hot = 1.0;
   EvalParams e = eval_params(p, false);
   ACDC_CK(ctx, launch_refresh(e, ctx->stream));
   return ACDC_OK;
@@ -530,6 +563,8 @@ int evaluate_impl(acdc_problem* p, acdc_eval* out, float* ms, bool screened = fa
   ACDC_CK(ctx, launch_refresh(e, ctx->stream));
   ACDC_CK(ctx, launch_gap(e, ctx->stream));
   if (build_active) ACDC_CK(ctx, launch_active_omega(e, p->d.rowcnt, ctx->stream));
+  const bool hot = e.viol != nullptr;
+  if (hot) ACDC_CK(ctx, launch_hot_set(e, ctx->stream));
   ACDC_CK(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
   ACDC_CK(ctx, cudaMemcpyAsync(p->h_eval, p->d.eval_out, sizeof(double) * 16,
                                cudaMemcpyDeviceToHost, ctx->stream));
@@ -553,6 +588,24 @@ int evaluate_impl(acdc_problem* p, acdc_eval* out, float* ms, bool screened = fa
     const double beta_a =
         a > 1 ? 1.0 + ((double)p->omega_active - 1.0) * (tau_a - 1.0) / (a - 1.0) : 1.0;
     p->li_scale_shrink = p->beta / std::max(p->beta, beta_a);
+  }
+  p->hot_count = 0;
+  p->hot_q = 0;
+  p->li_scale_hot = 1.0;
+  if (hot) {
+    // About one draw per hot column per tau_active updates; ESO over the hot
+    // columns, whose rows hold at most omega_H of them.
+    const int64_t h = std::min<int64_t>((int64_t)p->h_counters[CNT_HOT], p->d.n);
+    const double tau_shrink = p->s.tau_active > 0 ? p->s.tau_active : p->s.tau;
+    if (h > 0) {
+      p->hot_count = h;
+      p->hot_q = std::min(p->s.shrinking_probability, (double)h / tau_shrink);
+      const double w_h = std::max<double>(1.0, (double)p->h_counters[CNT_OMEGA_HOT]);
+      const double draws = p->hot_q * tau_shrink;
+      const double beta_h = h > 1 && draws > 1 ? 1.0 + (w_h - 1.0) * (draws - 1.0) / ((double)h - 1.0)
+                                               : 1.0;
+      p->li_scale_hot = p->beta / std::max(p->beta, beta_h);
+    }
   }
   if (out) fill_eval(p->h_eval, out);
   if (!std::isfinite(p->h_eval[0]))

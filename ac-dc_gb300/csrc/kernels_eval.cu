@@ -226,12 +226,15 @@ __global__ void k_refresh_init(EvalParams p) { k_refresh_init_body(p, blockIdx.x
 
 // Each warp reads 32 consecutive coordinates, then scatters the nonzero ones
 // cooperatively: r64 += coef_j a_j with coef = x_j (Lasso) or
-// alpha_j y_j / (lambda n) after clipping alpha_j into [0, 1] (SVM).
+// alpha_j y_j / (lambda n) after clipping alpha_j into [0, 1] (SVM).  The
+// Lasso pass also sums |x_j| and the support (slots 2 and 4).
 __device__ __forceinline__ void k_refresh_scatter_body(const EvalParams& p, const int64_t rank,
                                                 const int64_t nb) {
+  __shared__ double s_l1[ACDC_RED_THREADS / 32], s_sp[ACDC_RED_THREADS / 32];
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)nb * blockDim.x) >> 5;
   const double inv_ln = 1.0 / (p.lambda * (double)p.n);
+  double l1 = 0, sp = 0;
   for (int64_t base = (((int64_t)rank * blockDim.x + threadIdx.x) >> 5) * 32; base < p.n;
        base += warps * 32) {
     const int64_t j = base + lane;
@@ -251,6 +254,8 @@ __device__ __forceinline__ void k_refresh_scatter_body(const EvalParams& p, cons
         coef = c * p.rhs64[j] * inv_ln;
       } else {
         coef = xv;
+        l1 += fabs(xv);
+        sp += xv != 0.0 ? 1.0 : 0.0;
       }
     }
     unsigned live = __ballot_sync(ACDC_FULL_MASK, coef != 0.0 && mt.y > 0);
@@ -263,6 +268,26 @@ __device__ __forceinline__ void k_refresh_scatter_body(const EvalParams& p, cons
       for (int32_t e = lane; e < len; e += 32)
         atomicAdd(p.r64 + p.idx[start + e], cj * (double)p.vals[start + e]);
     }
+  }
+  if (p.loss != ACDC_LOSS_L1_SQUARE) return;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    l1 += __shfl_down_sync(ACDC_FULL_MASK, l1, o);
+    sp += __shfl_down_sync(ACDC_FULL_MASK, sp, o);
+  }
+  if (lane == 0) {
+    s_l1[threadIdx.x >> 5] = l1;
+    s_sp[threadIdx.x >> 5] = sp;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0, t1 = 0;
+    for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) {
+      t0 += s_l1[w];
+      t1 += s_sp[w];
+    }
+    p.part[rank * ACDC_NPART + 2] = t0;
+    p.part[rank * ACDC_NPART + 4] = t1;
   }
 }
 
@@ -355,13 +380,12 @@ __device__ __forceinline__ void append_active(const EvalParams& p, bool join, in
 
 __device__ __forceinline__ void k_gap_lasso_short_body(const EvalParams& p, const int64_t rank,
                                                 const int64_t nb) {
-  __shared__ double s_l1[ACDC_RED_THREADS / 32], s_gm[ACDC_RED_THREADS / 32],
-      s_sp[ACDC_RED_THREADS / 32], s_go[ACDC_RED_THREADS / 32];
+  __shared__ double s_gm[ACDC_RED_THREADS / 32], s_go[ACDC_RED_THREADS / 32];
   __shared__ ShortWarp sw_all[ACDC_RED_THREADS / 32];
   const int lane = threadIdx.x & 31;
   ShortWarp& sw = sw_all[threadIdx.x >> 5];
   const int64_t stride = (int64_t)nb * blockDim.x;  // a multiple of 32
-  double l1 = 0, gmax = 0, sp = 0, gout = 0;
+  double gmax = 0, gout = 0;
   for (int64_t base = (int64_t)rank * blockDim.x + (threadIdx.x & ~31); base < p.n;
        base += stride) {
     const int64_t j = base + lane;
@@ -369,8 +393,6 @@ __device__ __forceinline__ void k_gap_lasso_short_body(const EvalParams& p, cons
     int4 mt = make_int4(0, 0, 0, 0);
     if (valid) mt = p.meta[j];
     const double xv = valid ? coord(p, j, mt) : 0.0;
-    l1 += fabs(xv);
-    sp += xv != 0.0 ? 1.0 : 0.0;
     const bool is_short = valid && mt.y <= kShortLen;
     const int units = is_short ? (mt.y + 3) >> 2 : 0;
     // Exclusive scan of the unit counts over the 32 columns.
@@ -425,29 +447,21 @@ __device__ __forceinline__ void k_gap_lasso_short_body(const EvalParams& p, cons
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    l1 += __shfl_down_sync(ACDC_FULL_MASK, l1, o);
     gmax = fmax(gmax, __shfl_down_sync(ACDC_FULL_MASK, gmax, o));
-    sp += __shfl_down_sync(ACDC_FULL_MASK, sp, o);
     gout = fmax(gout, __shfl_down_sync(ACDC_FULL_MASK, gout, o));
   }
   if (lane == 0) {
-    s_l1[threadIdx.x >> 5] = l1;
     s_gm[threadIdx.x >> 5] = gmax;
-    s_sp[threadIdx.x >> 5] = sp;
     s_go[threadIdx.x >> 5] = gout;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t0 = 0, t1 = 0, t2 = 0, t3 = 0;
+    double t1 = 0, t3 = 0;
     for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) {
-      t0 += s_l1[w];
       t1 = fmax(t1, s_gm[w]);
-      t2 += s_sp[w];
       t3 = fmax(t3, s_go[w]);
     }
-    p.part[rank * ACDC_NPART + 2] = t0;
     p.part[rank * ACDC_NPART + 3] = t1;
-    p.part[rank * ACDC_NPART + 4] = t2;
     p.part[rank * ACDC_NPART + 7] = t3;
   }
 }
@@ -551,67 +565,140 @@ __device__ __forceinline__ void k_gap_lasso_long_body(const EvalParams& p, const
 
 __global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_long(EvalParams p) { k_gap_lasso_long_body(p, blockIdx.x, gridDim.x); }
 
-// Screened Lasso gap: |x|_1 and the support over every coordinate (4 bytes of
-// each column record, or the FP64 coordinate), and |a_j^T r| over the active
-// list only, one warp per active column in 128-entry chunks (slots 2-4; the
-// inactive columns are bounded in the finalize step).
+// a_j^T r64 for one column, one warp, 128-entry chunks; every lane gets the sum.
+__device__ __forceinline__ double active_dot(const EvalParams& p, const int4 mt, int lane) {
+  const int64_t start = (int64_t)(uint32_t)mt.x << 2;
+  double g = 0;
+  for (int32_t off = 4 * lane; off < mt.y; off += 128) {
+    const float4 v = __ldcs(reinterpret_cast<const float4*>(p.vals + start + off));
+    const int4 id = __ldcs(reinterpret_cast<const int4*>(p.idx + start + off));
+    g += (double)v.x * p.r64[id.x];
+    g += (double)v.y * p.r64[id.y];
+    g += (double)v.z * p.r64[id.z];
+    g += (double)v.w * p.r64[id.w];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(ACDC_FULL_MASK, g, o);
+  return g;
+}
+
+// KKT violation of coordinate j with gradient g: |g + lambda sign(x_j)| when
+// x_j != 0, else max(|g| - lambda, 0); stored as viol[t] by lane 0.
+__device__ __forceinline__ double record_violation(const EvalParams& p, int64_t t, int32_t j,
+                                                   const int4 mt, double g, int lane) {
+  const double xv = coord(p, j, mt);
+  const double v = xv != 0.0 ? fabs(g + (xv > 0.0 ? p.lambda : -p.lambda))
+                             : fmax(fabs(g) - p.lambda, 0.0);
+  if (lane == 0) p.viol[t] = (float)v;
+  return v;
+}
+
+// Screened Lasso gap: |a_j^T r| over the active list only, one warp per
+// active column in 128-entry chunks (slot 3; the inactive columns are bounded
+// in the finalize step, |x|_1 and the support come from the refresh pass).
 __device__ __forceinline__ void k_gap_lasso_screened_body(const EvalParams& p, const int64_t rank,
                                                          const int64_t nb) {
-  __shared__ double s_l1[ACDC_RED_THREADS / 32], s_gm[ACDC_RED_THREADS / 32],
-      s_sp[ACDC_RED_THREADS / 32];
+  __shared__ double s_gm[ACDC_RED_THREADS / 32], s_vm[ACDC_RED_THREADS / 32];
   const int lane = threadIdx.x & 31;
-  const int64_t stride = (int64_t)nb * blockDim.x;
-  const int32_t* xbits = reinterpret_cast<const int32_t*>(p.meta) + 3;
-  double l1 = 0, sp = 0, gmax = 0;
-  for (int64_t j = (int64_t)rank * blockDim.x + threadIdx.x; j < p.n; j += stride) {
-    const double xv = p.x64 ? p.x64[j] : (double)__int_as_float(xbits[4 * j]);
-    l1 += fabs(xv);
-    sp += xv != 0.0 ? 1.0 : 0.0;
-  }
+  double gmax = 0, vmax = 0;
   const int64_t cnt = (int64_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n);
-  const int64_t warps = stride >> 5;
+  const int64_t warps = ((int64_t)nb * blockDim.x) >> 5;
   for (int64_t t = ((int64_t)rank * blockDim.x + threadIdx.x) >> 5; t < cnt; t += warps) {
-    const int4 mt = p.meta[p.active[t]];
-    const int64_t start = (int64_t)(uint32_t)mt.x << 2;
-    double g = 0;
-    for (int32_t off = 4 * lane; off < mt.y; off += 128) {
-      const float4 v = __ldcs(reinterpret_cast<const float4*>(p.vals + start + off));
-      const int4 id = __ldcs(reinterpret_cast<const int4*>(p.idx + start + off));
-      g += (double)v.x * p.r64[id.x];
-      g += (double)v.y * p.r64[id.y];
-      g += (double)v.z * p.r64[id.z];
-      g += (double)v.w * p.r64[id.w];
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(ACDC_FULL_MASK, g, o);
+    const int32_t j = p.active[t];
+    const int4 mt = p.meta[j];
+    const double g = active_dot(p, mt, lane);
     gmax = fmax(gmax, fabs(g));
+    if (p.viol) vmax = fmax(vmax, record_violation(p, t, j, mt, g, lane));
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    l1 += __shfl_down_sync(ACDC_FULL_MASK, l1, o);
-    sp += __shfl_down_sync(ACDC_FULL_MASK, sp, o);
-    gmax = fmax(gmax, __shfl_down_sync(ACDC_FULL_MASK, gmax, o));
-  }
+  for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(ACDC_FULL_MASK, vmax, o));
   if (lane == 0) {
-    s_l1[threadIdx.x >> 5] = l1;
     s_gm[threadIdx.x >> 5] = gmax;
-    s_sp[threadIdx.x >> 5] = sp;
+    s_vm[threadIdx.x >> 5] = vmax;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t0 = 0, t1 = 0, t2 = 0;
+    double t1 = 0, t2 = 0;
     for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) {
-      t0 += s_l1[w];
       t1 = fmax(t1, s_gm[w]);
-      t2 += s_sp[w];
+      t2 = fmax(t2, s_vm[w]);
     }
     double* q = p.part + rank * ACDC_NPART;
-    q[2] = t0;
     q[3] = t1;
-    q[4] = t2;
     q[5] = 0;
     q[7] = 0;
     q[8] = 0;
+    q[9] = t2;
+  }
+}
+
+// KKT violations of the active columns after a full pass (slot 9, viol[]).
+__device__ __forceinline__ void k_active_viol_body(const EvalParams& p, const int64_t rank,
+                                                  const int64_t nb) {
+  __shared__ double s_vm[ACDC_RED_THREADS / 32];
+  const int lane = threadIdx.x & 31;
+  double vmax = 0;
+  const int64_t cnt = (int64_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n);
+  const int64_t warps = ((int64_t)nb * blockDim.x) >> 5;
+  for (int64_t t = ((int64_t)rank * blockDim.x + threadIdx.x) >> 5; t < cnt; t += warps) {
+    const int32_t j = p.active[t];
+    const int4 mt = p.meta[j];
+    vmax = fmax(vmax, record_violation(p, t, j, mt, active_dot(p, mt, lane), lane));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(ACDC_FULL_MASK, vmax, o));
+  if (lane == 0) s_vm[threadIdx.x >> 5] = vmax;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t2 = 0;
+    for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) t2 = fmax(t2, s_vm[w]);
+    p.part[rank * ACDC_NPART + 9] = t2;
+  }
+}
+
+__global__ void __launch_bounds__(ACDC_RED_THREADS) k_active_viol(EvalParams p) {
+  k_active_viol_body(p, blockIdx.x, gridDim.x);
+}
+
+// Hot set, pass 1: rows of the active columns whose violation exceeds
+// hot_frac times the largest one (eval_out[12]) are flagged.
+__global__ void k_hot_mark(EvalParams p) {
+  const int lane = threadIdx.x & 31;
+  const int64_t cnt = (int64_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n);
+  const double vmax = p.eval_out[12];
+  if (!(vmax > 0)) return;
+  const float thresh = (float)(p.hot_frac * vmax);
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < cnt; t += warps) {
+    if (!(p.viol[t] > thresh)) continue;
+    const int4 mt = p.meta[p.active[t]];
+    const int64_t start = (int64_t)(uint32_t)mt.x << 2;
+    for (int32_t e = lane; e < mt.y; e += 32) p.row_flag[p.idx[start + e]] = 1;
+  }
+}
+
+// Hot set, pass 2: every active column with an entry in a flagged row joins the
+// hot list; its rows are counted for the hot set's ESO parameter.
+__global__ void k_hot_collect(EvalParams p) {
+  const int lane = threadIdx.x & 31;
+  const int64_t cnt = (int64_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n);
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < cnt; t += warps) {
+    const int32_t j = p.active[t];
+    const int4 mt = p.meta[j];
+    const int64_t start = (int64_t)(uint32_t)mt.x << 2;
+    bool touch = false;
+    for (int32_t e = lane; e < mt.y && !touch; e += 32) touch = p.row_flag[p.idx[start + e]] != 0;
+    if (!__any_sync(ACDC_FULL_MASK, touch)) continue;
+    if (lane == 0) {
+      const unsigned long long pos = atomicAdd(p.counters + CNT_HOT, 1ull);
+      if (pos < (unsigned long long)p.n) p.hot[pos] = j;
+    }
+    int32_t top = 0;
+    for (int32_t e = lane; e < mt.y; e += 32) top = max(top, atomicAdd(p.rowcnt + p.idx[start + e], 1) + 1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) top = max(top, __shfl_xor_sync(ACDC_FULL_MASK, top, o));
+    if (lane == 0) atomicMax(p.counters + CNT_OMEGA_HOT, (unsigned long long)top);
   }
 }
 
@@ -704,48 +791,35 @@ __global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_svm(EvalParams p) { k_
 // Adds the per-block partials in block order and forms P, D and the gap.
 // eval_out: [0] P [1] D [2] gap [3] rel_gap [4] 0-1 accuracy [5] reg_norm
 //           [6] sq_norm [7] max_abs_grad [8] support [9] active
-constexpr int kFinThreads = 256;
+constexpr int kFinThreads = 32 * ACDC_NPART;
 
-// Thread t adds blocks [t*S, (t+1)*S) in order; thread 0 then adds the stripes
-// in order, so the association is fixed and the result reproducible.
+// Warp w reduces partial slot w over the blocks: lane l takes blocks l, l+32,
+// ... in order, then a fixed butterfly combines the lanes, so the association
+// is fixed and the result reproducible.  Maxima (Lasso slots 3, 5, 7, 8) and
+// sums otherwise.
 __device__ __forceinline__ void k_finalize_body(const EvalParams& p, const int64_t nparts) {
-  __shared__ double st[kFinThreads][8];
-  const int S = (int)((nparts + kFinThreads - 1) / kFinThreads);
+  __shared__ double red[ACDC_NPART];
   const bool lasso = p.loss == ACDC_LOSS_L1_SQUARE;
-  double a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  for (int b = threadIdx.x * S; b < (int)(threadIdx.x + 1) * S && b < nparts; ++b) {
-    const double* q = p.part + b * ACDC_NPART;
-    a[0] += q[0];
-    a[1] += q[1];
-    a[2] += q[2];
-    a[4] += q[4];
-    if (lasso) {
-      a[3] = fmax(a[3], fmax(q[3], q[5]));  // short and long columns
-      a[6] += q[6];
-      a[7] = fmax(a[7], fmax(q[7], q[8]));
-    } else {
-      a[3] += q[3];
-      a[5] += q[5];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (w < ACDC_NPART) {
+    const bool is_max = lasso && (w == 3 || w == 5 || w == 7 || w == 8 || w == 9);
+    double a = 0;
+    for (int64_t b = lane; b < nparts; b += 32) {
+      const double v = p.part[b * ACDC_NPART + w];
+      a = is_max ? fmax(a, v) : a + v;
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double t = __shfl_xor_sync(ACDC_FULL_MASK, a, o);
+      a = is_max ? fmax(a, t) : a + t;
+    }
+    if (lane == 0) red[w] = a;
   }
-  for (int k = 0; k < 8; ++k) st[threadIdx.x][k] = a[k];
   __syncthreads();
   if (threadIdx.x != 0) return;
-  double rr = 0, br = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0, s6 = 0, s7 = 0;
-  for (int t = 0; t < kFinThreads; ++t) {
-    rr += st[t][0];
-    br += st[t][1];
-    s2 += st[t][2];
-    s4 += st[t][4];
-    if (lasso) {
-      s3 = fmax(s3, st[t][3]);
-      s6 += st[t][6];
-      s7 = fmax(s7, st[t][7]);
-    } else {
-      s3 += st[t][3];
-      s5 += st[t][5];
-    }
-  }
+  const double rr = red[0], br = red[1], s2 = red[2], s4 = red[4];
+  const double s3 = lasso ? fmax(red[3], red[5]) : red[3];
+  const double s5 = red[5], s6 = red[6], s7 = fmax(red[7], red[8]);
   double P, D, acc = 0, gmax = 0;
   const double nn = (double)p.n;
   double* o = p.eval_out;
@@ -760,6 +834,7 @@ __device__ __forceinline__ void k_finalize_body(const EvalParams& p, const int64
       o[10] = s7;
       o[11] = 0;
     }
+    if (p.viol) o[12] = red[9];
     P = 0.5 * rr + p.lambda * s2;
     const double s = gmax > p.lambda ? p.lambda / gmax : 1.0;
     D = -s * br - 0.5 * s * s * rr;
@@ -907,7 +982,7 @@ cudaError_t launch_x64_to_x32(const DevProblem& d, cudaStream_t st) {
 
 cudaError_t launch_refresh(const EvalParams& p, cudaStream_t st) {
   k_refresh_init<<<grid_for(p.m, 256, 152 * 8), 256, 0, st>>>(p);
-  k_refresh_scatter<<<grid_for((p.n + 31) / 32 * 32, 256, 152 * 16), 256, 0, st>>>(p);
+  k_refresh_scatter<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
   k_refresh_finish<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
   return cudaGetLastError();
 }
@@ -924,11 +999,23 @@ cudaError_t launch_gap(const EvalParams& p, cudaStream_t st) {
   {
     k_gap_lasso_short<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
     k_gap_lasso_long<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
+    if (p.viol && p.active) k_active_viol<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
   }
   else
     k_gap_svm<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
   k_finalize<<<1, kFinThreads, 0, st>>>(p);
   return cudaGetLastError();
+}
+
+cudaError_t launch_hot_set(const EvalParams& p, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(p.counters + CNT_HOT, 0, 2 * sizeof(unsigned long long), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(p.rowcnt, 0, sizeof(int32_t) * p.m, st);
+  if (e != cudaSuccess) return e;
+  k_hot_mark<<<152 * 4, 256, 0, st>>>(p);
+  k_hot_collect<<<152 * 4, 256, 0, st>>>(p);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemsetAsync(p.row_flag, 0, p.m, st);
+  return e;
 }
 
 // ---- batched rounds ----

@@ -75,11 +75,19 @@ __device__ __forceinline__ T column_sum(T v, uint32_t len) {
   return __shfl_sync(ACDC_FULL_MASK, v, 0);
 }
 
+// Coordinate of update k.  With shrinking, word 2 picks the tier (hot set below
+// hot_q32, active set below shrink_q32, else all coordinates) and word 3 the
+// entry of the list; a hot-set draw is returned with bit 31 set.
+constexpr int32_t kHotBit = (int32_t)0x80000000u;
+constexpr int32_t kCoordMask = 0x7fffffff;
+
 __device__ __forceinline__ int32_t draw_coord(const UpdateParams& p, uint64_t k,
-                                              int32_t active_cnt) {
+                                              int32_t active_cnt, int32_t hot_cnt) {
   acdc_u32x4 o = acdc_philox4x32_10((uint32_t)k, (uint32_t)(k >> 32), ACDC_STREAM_SAMPLER, 0u,
                                     (uint32_t)p.seed, (uint32_t)(p.seed >> 32));
   if (active_cnt > 0 && o.v[2] < p.shrink_q32) {
+    if (hot_cnt > 0 && o.v[2] < p.hot_q32)
+      return __ldg(p.hot + __umulhi(o.v[3], (uint32_t)hot_cnt)) | kHotBit;
     uint32_t t = __umulhi(o.v[3], (uint32_t)active_cnt);
     return __ldg(p.active + t);
   }
@@ -171,9 +179,12 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
   unsigned long long* work = p.counters + CNT_WORK;
   const int32_t active_cnt =
       p.shrink_q32 ? (int32_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n) : 0;
+  const int32_t hot_cnt =
+      p.hot_q32 ? (int32_t)min(p.counters[CNT_HOT], (unsigned long long)p.n) : 0;
   const T lam = (T)p.lambda_d;
   const T inv_ln = (T)p.inv_lambda_n_d;
   const T li_scale = (T)p.li_scale;
+  const T li_scale_hot = (T)p.li_scale_hot;
   unsigned long long n_upd = 0, n_nz = 0, n_read = 0, n_scat = 0;
 
   for (;;) {
@@ -185,14 +196,14 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
 #pragma unroll
     for (int q = 0; q < kChunk / 32; ++q) {
       const int s = 32 * q + lane;
-      w.coords[s] = s < cnt ? draw_coord(p, k_base + base + (uint64_t)s, active_cnt) : 0;
+      w.coords[s] = s < cnt ? draw_coord(p, k_base + base + (uint64_t)s, active_cnt, hot_cnt) : 0;
     }
     __syncwarp();
 
     // Prologue: metadata of updates 0..2D-1, then entries of updates 0..D-1,
     // one commit group per update so that wait_group(D-1) below always means
     // "the copies of update s have landed".
-    for (int t = 0; t < kDM && t < cnt; ++t) issue_meta(w, p, w.coords[t], t, lane);
+    for (int t = 0; t < kDM && t < cnt; ++t) issue_meta(w, p, w.coords[t] & kCoordMask, t, lane);
     cp_async_commit();
     cp_async_wait<0>();
     __syncwarp();
@@ -210,7 +221,8 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
     for (int s = 0; s < cnt; ++s) {
       cp_async_wait<kD - 1>();
       __syncwarp();  // copies of update s visible; every lane is done with update s-1
-      const int32_t j = w.coords[s];
+      const int32_t cj = w.coords[s];
+      const int32_t j = cj & kCoordMask;
       const int4 mt = w.meta[ms];
       T xj;
       if constexpr (sizeof(T) == 8)
@@ -226,7 +238,7 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
       c0.i = live0 ? w.idx[ds][lane] : make_int4(0, 0, 0, 0);
       // Refill: entries of update s + D, metadata of update s + 2D.
       if (s + kD < cnt) issue_entries(w, p, ms_d, ds_d, lane);
-      if (s + kDM < cnt) issue_meta(w, p, w.coords[s + kDM], ms_2d, lane);
+      if (s + kDM < cnt) issue_meta(w, p, w.coords[s + kDM] & kCoordMask, ms_2d, lane);
       cp_async_commit();
       ms = ring_next(ms, kMS);
       ds = ring_next(ds, kDS);
@@ -246,7 +258,7 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
       }
       const T g = column_sum<T>(acc, len);
 
-      const T li = (T)__int_as_float(mt.z) * li_scale;
+      const T li = (T)__int_as_float(mt.z) * (cj < 0 ? li_scale_hot : li_scale);
       T delta, coef;
       if (LOSS == ACDC_LOSS_L1_SQUARE) {
         const T z = xj - li * g;

@@ -86,6 +86,14 @@ typedef struct acdc_settings {
                                      that bound reaches (1 - eps/2) lambda.  The
                                      certificate stays a valid duality gap.       */
   int32_t reserved[2];
+  double hot_threshold;           /* Lasso with shrinking and screened_eval: after
+                                     each evaluation the active columns whose KKT
+                                     violation exceeds hot_threshold times the
+                                     largest one, plus the active columns sharing
+                                     a row with them, form a hot set that gets
+                                     about one draw each per tau_active updates
+                                     (ESO-scaled for the hot set); 0 = off,
+                                     default 0.1                                  */
 } acdc_settings;
 
 /* precision: FP32 x and residual with FP64 refresh and gap (FP32), the same
