@@ -593,13 +593,14 @@ int evaluate_impl(acdc_problem* p, acdc_eval* out, float* ms, bool screened = fa
   p->hot_q = 0;
   p->li_scale_hot = 1.0;
   if (hot) {
-    // About one draw per hot column per tau_active updates; ESO over the hot
-    // columns, whose rows hold at most omega_H of them.
+    // About one draw per hot column per tau_active updates, at most half of the
+    // active-set draws; ESO over the hot columns, whose rows hold at most
+    // omega_H of them.
     const int64_t h = std::min<int64_t>((int64_t)p->h_counters[CNT_HOT], p->d.n);
     const double tau_shrink = p->s.tau_active > 0 ? p->s.tau_active : p->s.tau;
     if (h > 0) {
       p->hot_count = h;
-      p->hot_q = std::min(p->s.shrinking_probability, (double)h / tau_shrink);
+      p->hot_q = std::min(0.5 * p->s.shrinking_probability, (double)h / tau_shrink);
       const double w_h = std::max<double>(1.0, (double)p->h_counters[CNT_OMEGA_HOT]);
       const double draws = p->hot_q * tau_shrink;
       const double beta_h = h > 1 && draws > 1 ? 1.0 + (w_h - 1.0) * (draws - 1.0) / ((double)h - 1.0)

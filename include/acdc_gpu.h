@@ -92,7 +92,8 @@ typedef struct acdc_settings {
                                      largest one, plus the active columns sharing
                                      a row with them, form a hot set that gets
                                      about one draw each per tau_active updates
-                                     (ESO-scaled for the hot set); 0 = off,
+                                     (at most half of the active-set draws,
+                                     ESO-scaled for the hot set); 0 = off,
                                      default 0.1                                  */
 } acdc_settings;
 
