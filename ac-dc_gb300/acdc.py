@@ -64,7 +64,8 @@ class ProblemInfo(C.Structure):
 
 class BatchOptions(C.Structure):
     _fields_ = [("path_len", I32), ("max_epochs", I32), ("gap_target", D), ("refresh_every", I32),
-                ("autotune", I32), ("tau_override", I32), ("plain", I32), ("reserved", I32 * 8)]
+                ("autotune", I32), ("tau_override", I32), ("plain", I32), ("use_shrinking", I32),
+                ("active_passes", I32), ("reserved", I32 * 6)]
 
 
 class BatchResult(C.Structure):
@@ -74,7 +75,7 @@ class BatchResult(C.Structure):
 
 class ServerOptions(C.Structure):
     _fields_ = [("memory_budget_bytes", I64), ("max_slots", I32), ("quantum_epochs", I32),
-                ("max_epochs", I32), ("reserved", I32 * 7)]
+                ("max_epochs", I32), ("use_shrinking", I32), ("reserved", I32 * 6)]
 
 
 class Request(C.Structure):
@@ -474,9 +475,10 @@ class Server:
     STATES = ("queued", "running", "done", "failed")
 
     def __init__(self, ctx, memory_budget_bytes=120 << 30, max_slots=256, quantum_rounds=4,
-                 max_epochs=2000):
+                 max_epochs=2000, use_shrinking=0):
         self.ctx, self.L = ctx, ctx.L
-        opt = ServerOptions(int(memory_budget_bytes), max_slots, quantum_rounds, max_epochs)
+        opt = ServerOptions(int(memory_budget_bytes), max_slots, quantum_rounds, max_epochs,
+                            use_shrinking)
         h = VP()
         ctx.check(self.L.acdc_server_create(ctx.h, C.byref(opt), C.byref(h)))
         self.h = h
@@ -522,12 +524,14 @@ class Server:
 
 
 def batch_solve_path(ctx, problems, lambdas, gap_target=1e-6, max_epochs=1000, refresh_every=5,
-                     autotune=1, tau_override=0, plain=0, want_x=False):
+                     autotune=1, tau_override=0, plain=0, want_x=False, use_shrinking=0,
+                     active_passes=0):
     """Solve every problem along its lambda row; returns (results[count][path], xs)."""
     count = len(problems)
     lam = np.ascontiguousarray(lambdas, np.float64).reshape(count, -1)
     path = lam.shape[1]
-    opt = BatchOptions(path, max_epochs, gap_target, refresh_every, autotune, tau_override, plain)
+    opt = BatchOptions(path, max_epochs, gap_target, refresh_every, autotune, tau_override, plain,
+                       use_shrinking, active_passes)
     res = (BatchResult * (count * path))()
     handles = (VP * count)(*[p.h for p in problems])
     xs = [np.zeros(p.n) for p in problems] if want_x else None

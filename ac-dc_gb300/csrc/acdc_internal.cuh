@@ -2,10 +2,11 @@
 //
 // Device layout of one problem (the column operand: A for the Lasso, X^T for
 // the SVM dual; "column" = coordinate, "row" = residual entry):
-//   meta[n]   int4 {start4, len, Li, x}: start4 = column start / 4 in the
+//   meta[n]   int4 {start4, len, Li, 0}: start4 = column start / 4 in the
 //             padded arrays, len = nonzeros, Li = 1/(beta ||a_j||^2) (FP32
-//             bits; for the SVM the sign carries y_j), x = coordinate value
-//             (FP32 bits, updated in place with red.global.add.f32).
+//             bits; for the SVM the sign carries y_j).
+//   x32[n]    FP32 coordinates, updated in place with red.global.add.f32
+//             (contiguous, so passes over every coordinate read 4 bytes each).
 //   vals[]    FP32 values, each column starting on a 16-byte boundary and
 //             zero-padded to a multiple of 4 entries (so one 128-bit load
 //             covers 4 entries and never crosses into the next column).
@@ -70,6 +71,7 @@ struct UpdateParams {
   unsigned long long* counters;
   double* x64;          // FP64 coordinates (polish mode)
   double* r64;          // FP64 residual (polish mode)
+  float* x32;           // FP32 coordinates
   int64_t n;
   uint64_t count;       // updates in this launch
   uint64_t seed;
@@ -98,7 +100,8 @@ struct EvalParams {
   unsigned long long* counters;
   double* part;         // ACDC_RED_BLOCKS * ACDC_NPART
   double* eval_out;     // 16 doubles
-  double* x64;          // FP64 coordinates when in polish mode, else nullptr (x in meta.w)
+  double* x64;          // FP64 coordinates when in polish mode, else nullptr (x in x32)
+  float* x32;           // FP32 coordinates
   const int32_t* long_cols;  // columns with more than 32 entries
   int64_t n_long;
   int64_t m, n;
@@ -137,6 +140,17 @@ struct SlotCtl {
   double polish_rel_gap;
   const double* lambdas; // path_len values
   double* results;       // path_len rows of kBatchResultLen doubles
+  // q-shrinking (Lasso): from the second round of each lambda, q of the draws
+  // come from the active set the round's gap pass built, with the step scale of
+  // beta_A = 1 + (omega_A-1)(q tau-1)/(|A|-1) (omega_A counted over the active
+  // columns each round), and a round is active_passes |A|/q updates.
+  int32_t shrink;
+  int32_t active_passes;
+  int32_t shrink_next;   // 1 when the next round may draw from the active set
+  uint32_t q32;
+  double q;
+  double omega;
+  double beta;
 };
 
 // Row of a per-lambda result: eval_out[0..9], lambda, converged, epochs, tau.
@@ -159,6 +173,7 @@ struct BatchDev {
 struct DevProblem {
   int64_t m = 0, n = 0, nnz = 0, nnz_pad = 0;
   int4* meta = nullptr;
+  float* x32 = nullptr;     // n FP32 coordinates
   float* vals = nullptr;
   int32_t* idx = nullptr;
   float* r32 = nullptr;

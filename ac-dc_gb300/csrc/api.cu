@@ -111,6 +111,7 @@ cudaError_t dalloc(T** p, int64_t count, int64_t* bytes) {
 
 void free_problem_buffers(DevProblem& d) {
   cudaFree(d.meta);
+  cudaFree(d.x32);
   cudaFree(d.vals);
   cudaFree(d.idx);
   cudaFree(d.r32);
@@ -173,6 +174,7 @@ EvalParams eval_params(acdc_problem* p, bool build_active) {
   e.shrink_thresh = (1.0 - p->s.shrink_eps) * p->lambda;
   e.loss = p->loss;
   e.x64 = p->fp64_mode ? p->d.x64 : nullptr;
+  e.x32 = p->d.x32;
   e.long_cols = p->d.long_cols;
   e.n_long = p->d.n_long;
   if (build_active && p->loss == ACDC_LOSS_L1_SQUARE) e.r_ref = p->d.r_ref;
@@ -208,6 +210,7 @@ UpdateParams update_params(acdc_problem* p, uint64_t count, bool shrink) {
   u.li_scale = shrink ? p->li_scale_shrink : 1.0;
   u.x64 = p->d.x64;
   u.r64 = p->d.r64;
+  u.x32 = p->d.x32;
   u.fp64 = p->fp64_mode ? 1 : 0;
   double q = p->s.shrinking_probability;
   if (!shrink || q <= 0)
@@ -352,6 +355,8 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
   d.nnz_pad = units * 4;
   const int64_t rhs_len = loss == ACDC_LOSS_L1_SQUARE ? m : n;
   STEP(dalloc(&d.meta, n, &d.bytes));
+  STEP(dalloc(&d.x32, n, &d.bytes));
+  STEP(cudaMemsetAsync(d.x32, 0, sizeof(float) * n, st));
   STEP(dalloc(&d.vals, d.nnz_pad, &d.bytes));
   STEP(dalloc(&d.idx, d.nnz_pad, &d.bytes));
   STEP(dalloc(&d.r32, m, &d.bytes));

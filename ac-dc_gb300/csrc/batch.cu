@@ -59,17 +59,32 @@ struct SolveOpts {
   int32_t refresh_every;
   int32_t autotune;
   int32_t tau_override;
+  int32_t use_shrinking = 0;
+  int32_t active_passes = 20;
 };
 
+SolveOpts solve_opts(const acdc_batch_options* opt) {
+  SolveOpts o{opt->gap_target, opt->max_epochs, opt->refresh_every, opt->autotune,
+              opt->tau_override};
+  o.use_shrinking = opt->use_shrinking;
+  o.active_passes = opt->active_passes > 0 ? opt->active_passes : 20;
+  return o;
+}
+
 // Settings of one problem for batched or plain solving: tau from the
-// autotuner (or the override), no shrinking, relative gap.
+// autotuner (or the override), relative gap, q-shrinking for the Lasso when
+// asked (from the first epoch on; the batched rounds start each lambda with
+// one uniform round).
 int prepare(acdc_problem* p, const SolveOpts& o, int wpb_cap) {
   acdc_settings s = p->s;
   s.gap_target = o.gap_target;
   s.gap_relative = 1;
   s.max_epochs = o.max_epochs;
   s.refresh_every = o.refresh_every;
-  s.use_shrinking = 0;
+  s.use_shrinking = o.use_shrinking && p->loss == ACDC_LOSS_L1_SQUARE ? 1 : 0;
+  s.shrinking_starting_iter = 1;
+  s.active_passes = o.active_passes;
+  s.tau_active = 0;
   if (o.tau_override > 0)
     s.tau = o.tau_override;
   else if (o.autotune)
@@ -117,6 +132,7 @@ class BatchEngine {
       u.counters = p->d.counters;
       u.x64 = p->d.x64;
       u.r64 = p->d.r64;
+      u.x32 = p->d.x32;
       u.n = p->d.n;
       u.count = (uint64_t)o.refresh_every * (uint64_t)p->d.n;
       u.seed = p->s.seed;
@@ -144,16 +160,28 @@ class BatchEngine {
       e.part = p->d.part;
       e.eval_out = p->d.eval_out;
       e.x64 = p->fp64_mode ? p->d.x64 : nullptr;
+      e.x32 = p->d.x32;
       e.long_cols = p->d.long_cols;
       e.n_long = p->d.n_long;
       e.m = p->d.m;
       e.n = p->d.n;
       e.lambda = p->lambda;
-      e.shrink_thresh = 0.9 * p->lambda;
+      e.shrink_thresh = (1.0 - p->s.shrink_eps) * p->lambda;
       e.loss = p->loss;
+      const bool shrink = p->s.use_shrinking != 0;
+      if (shrink) {
+        e.active = p->d.active;
+        e.rowcnt = p->d.rowcnt;
+      }
       SlotCtl& c = ctl[(size_t)i];
       std::memset(&c, 0, sizeof(c));
       c.live = 1;
+      c.shrink = shrink ? 1 : 0;
+      c.active_passes = o.active_passes;
+      c.q = p->s.shrinking_probability;
+      c.q32 = c.q >= 1 ? 0xffffffffu : (uint32_t)(c.q * 4294967296.0);
+      c.omega = (double)p->omega;
+      c.beta = p->beta;
       c.path_len = path;
       c.max_updates = (uint64_t)o.max_epochs * (uint64_t)p->d.n;
       c.round_updates = u.count;
@@ -322,8 +350,7 @@ void row_to_result(const double* row, acdc_batch_result* out) {
 int plain_path(acdc_ctx* ctx, int32_t count, acdc_problem* const* problems, const double* lambdas,
                const acdc_batch_options* opt, acdc_batch_result* results, double* const* x_out) {
   (void)ctx;
-  const SolveOpts o{opt->gap_target, opt->max_epochs, opt->refresh_every, opt->autotune,
-                    opt->tau_override};
+  const SolveOpts o = solve_opts(opt);
   for (int32_t i = 0; i < count; ++i) {
     acdc_problem* p = problems[i];
     int rc = prepare(p, o, 8);
@@ -355,16 +382,18 @@ int batched_path(acdc_ctx* ctx, int32_t count, acdc_problem* const* problems,
                  const double* lambdas, const acdc_batch_options* opt,
                  acdc_batch_result* results, double* const* x_out) {
   const int path = opt->path_len;
-  const SolveOpts o{opt->gap_target, opt->max_epochs, opt->refresh_every, opt->autotune,
-                    opt->tau_override};
+  const SolveOpts o = solve_opts(opt);
   std::vector<acdc_problem*> probs(problems, problems + count);
   BatchEngine eng(ctx);
   int rc = eng.build(probs, std::vector<double>(lambdas, lambdas + (size_t)count * path), path, o);
   if (rc) return rc;
   // Each slot advances refresh_every epochs per round and spends at most
   // max_epochs per lambda.
-  const int64_t max_rounds =
-      (int64_t)path * ((opt->max_epochs + opt->refresh_every - 1) / opt->refresh_every) + path + 1;
+  // (a shrinking round is at least a quarter epoch).
+  const int64_t rounds_per_lambda =
+      o.use_shrinking ? 4 * (int64_t)opt->max_epochs
+                      : (opt->max_epochs + opt->refresh_every - 1) / opt->refresh_every;
+  const int64_t max_rounds = (int64_t)path * rounds_per_lambda + path + 1;
   rc = eng.run_graph(max_rounds);
   if (rc) return rc;
   std::vector<double> rows;
@@ -567,7 +596,8 @@ extern "C" int acdc_server_step(acdc_server* s, int32_t* pending) {
       // x, residual and sampler state; new ones start from x = 0.
       std::vector<acdc_problem*> probs;
       std::vector<double> lams, targets;
-      const SolveOpts o{1e-6, s->opt.max_epochs, 1, 1, 0};
+      SolveOpts o{1e-6, s->opt.max_epochs, 1, 1, 0};
+      o.use_shrinking = s->opt.use_shrinking;
       for (Request* r : s->resident) {
         probs.push_back(r->prob);
         lams.push_back(r->lambda);

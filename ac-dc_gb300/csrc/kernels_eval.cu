@@ -179,12 +179,12 @@ __global__ void k_widen_i32(const int32_t* src, int64_t* dst, int64_t len) {
     dst[i] = (int64_t)src[i];
 }
 
-// xbuf (FP64, caller order) -> meta.w (FP32) and, in polish mode, x64.
+// xbuf (FP64, caller order) -> x32 and, in polish mode, x64.
 __global__ void k_set_x(DevProblem d, int fp64) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < d.n; j += stride) {
     const double v = d.xbuf[j];
-    d.meta[j].w = __float_as_int((float)v);
+    d.x32[j] = (float)v;
     if (fp64) d.x64[j] = v;
   }
 }
@@ -192,24 +192,24 @@ __global__ void k_set_x(DevProblem d, int fp64) {
 __global__ void k_get_x(DevProblem d, int fp64) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < d.n; j += stride)
-    d.xbuf[j] = fp64 ? __ldcg(d.x64 + j) : (double)__int_as_float(__ldcg(&d.meta[j].w));
+    d.xbuf[j] = fp64 ? __ldcg(d.x64 + j) : (double)__ldcg(d.x32 + j);
 }
 
 __global__ void k_x32_to_x64(DevProblem d) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < d.n; j += stride)
-    d.x64[j] = (double)__int_as_float(d.meta[j].w);
+    d.x64[j] = (double)d.x32[j];
 }
 
 __global__ void k_x64_to_x32(DevProblem d) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < d.n; j += stride)
-    d.meta[j].w = __float_as_int((float)d.x64[j]);
+    d.x32[j] = (float)d.x64[j];
 }
 
-// Coordinate j as the evaluation sees it: FP64 in polish mode, else FP32 bits.
-__device__ __forceinline__ double coord(const EvalParams& p, int64_t j, int4 mt) {
-  return p.x64 ? p.x64[j] : (double)__int_as_float(mt.w);
+// Coordinate j as the evaluation sees it: FP64 in polish mode, else FP32.
+__device__ __forceinline__ double coord(const EvalParams& p, int64_t j) {
+  return p.x64 ? p.x64[j] : (double)p.x32[j];
 }
 
 // ---- refresh ----
@@ -239,34 +239,49 @@ __device__ __forceinline__ void k_refresh_scatter_body(const EvalParams& p, cons
        base += warps * 32) {
     const int64_t j = base + lane;
     double coef = 0;
-    int4 mt = make_int4(0, 0, 0, 0);
     if (j < p.n) {
-      mt = p.meta[j];
-      const double xv = coord(p, j, mt);
+      const double xv = coord(p, j);
       if (p.loss == ACDC_LOSS_SVM_DUAL) {
         const double c = xv > 1.0 ? 1.0 : (xv < 0.0 ? 0.0 : xv);
         if (c != xv) {
           if (p.x64)
             p.x64[j] = c;
           else
-            p.meta[j].w = __float_as_int((float)c);
+            p.x32[j] = (float)c;
         }
-        coef = c * p.rhs64[j] * inv_ln;
+        if (c != 0.0) coef = c * p.rhs64[j] * inv_ln;
       } else {
         coef = xv;
         l1 += fabs(xv);
         sp += xv != 0.0 ? 1.0 : 0.0;
       }
     }
-    unsigned live = __ballot_sync(ACDC_FULL_MASK, coef != 0.0 && mt.y > 0);
+    // Columns of the nonzero coordinates, one at a time by the whole warp.  The
+    // records of the live lanes are loaded together first; each column's
+    // entries are loaded four 32-entry groups at a time before their atomics.
+    unsigned live = __ballot_sync(ACDC_FULL_MASK, coef != 0.0);
+    if (!live) continue;
+    int2 sl = make_int2(0, 0);
+    if (coef != 0.0) sl = *reinterpret_cast<const int2*>(p.meta + j);
     while (live) {
       const int src = __ffs(live) - 1;
       live &= live - 1;
       const double cj = __shfl_sync(ACDC_FULL_MASK, coef, src);
-      const int64_t start = (int64_t)(uint32_t)__shfl_sync(ACDC_FULL_MASK, mt.x, src) << 2;
-      const int32_t len = __shfl_sync(ACDC_FULL_MASK, mt.y, src);
-      for (int32_t e = lane; e < len; e += 32)
-        atomicAdd(p.r64 + p.idx[start + e], cj * (double)p.vals[start + e]);
+      const int64_t start = (int64_t)(uint32_t)__shfl_sync(ACDC_FULL_MASK, sl.x, src) << 2;
+      const int32_t len = __shfl_sync(ACDC_FULL_MASK, sl.y, src);
+      for (int32_t e0 = lane; e0 < len; e0 += 128) {
+        int32_t row[4];
+        float val[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int32_t e = e0 + 32 * k;
+          row[k] = e < len ? p.idx[start + e] : -1;
+          val[k] = e < len ? p.vals[start + e] : 0.f;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (row[k] >= 0) atomicAdd(p.r64 + row[k], cj * (double)val[k]);
+      }
     }
   }
   if (p.loss != ACDC_LOSS_L1_SQUARE) return;
@@ -392,7 +407,7 @@ __device__ __forceinline__ void k_gap_lasso_short_body(const EvalParams& p, cons
     const bool valid = j < p.n;
     int4 mt = make_int4(0, 0, 0, 0);
     if (valid) mt = p.meta[j];
-    const double xv = valid ? coord(p, j, mt) : 0.0;
+    const double xv = valid ? coord(p, j) : 0.0;
     const bool is_short = valid && mt.y <= kShortLen;
     const int units = is_short ? (mt.y + 3) >> 2 : 0;
     // Exclusive scan of the unit counts over the 32 columns.
@@ -529,7 +544,7 @@ __device__ __forceinline__ void k_gap_lasso_long_body(const EvalParams& p, const
     for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(ACDC_FULL_MASK, g, o);
     const double ag = fabs(g);
     gmax = fmax(gmax, ag);
-    const double xv = coord(p, j, mt);
+    const double xv = coord(p, j);
     if (p.active) {
       if (xv != 0.0 || ag > p.shrink_thresh) {
         if (lane == 0) {
@@ -565,53 +580,138 @@ __device__ __forceinline__ void k_gap_lasso_long_body(const EvalParams& p, const
 
 __global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_long(EvalParams p) { k_gap_lasso_long_body(p, blockIdx.x, gridDim.x); }
 
-// a_j^T r64 for one column, one warp, 128-entry chunks; every lane gets the sum.
+// a_j^T r64 for one column, one warp; every lane gets the sum.  The loads of
+// four 128-entry chunks are issued before their gathers, so a long column costs
+// a few memory latencies rather than one per chunk.
 __device__ __forceinline__ double active_dot(const EvalParams& p, const int4 mt, int lane) {
   const int64_t start = (int64_t)(uint32_t)mt.x << 2;
   double g = 0;
-  for (int32_t off = 4 * lane; off < mt.y; off += 128) {
-    const float4 v = __ldcs(reinterpret_cast<const float4*>(p.vals + start + off));
-    const int4 id = __ldcs(reinterpret_cast<const int4*>(p.idx + start + off));
-    g += (double)v.x * p.r64[id.x];
-    g += (double)v.y * p.r64[id.y];
-    g += (double)v.z * p.r64[id.z];
-    g += (double)v.w * p.r64[id.w];
+  for (int32_t off = 4 * lane; off < mt.y; off += 512) {
+    float4 v[4];
+    int4 id[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int32_t e = off + 128 * k;
+      if (e < mt.y) {
+        v[k] = __ldcs(reinterpret_cast<const float4*>(p.vals + start + e));
+        id[k] = __ldcs(reinterpret_cast<const int4*>(p.idx + start + e));
+      } else {
+        v[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        id[k] = make_int4(0, 0, 0, 0);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      g += (double)v[k].x * p.r64[id[k].x];
+      g += (double)v[k].y * p.r64[id[k].y];
+      g += (double)v[k].z * p.r64[id[k].z];
+      g += (double)v[k].w * p.r64[id[k].w];
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(ACDC_FULL_MASK, g, o);
   return g;
 }
 
-// KKT violation of coordinate j with gradient g: |g + lambda sign(x_j)| when
-// x_j != 0, else max(|g| - lambda, 0); stored as viol[t] by lane 0.
-__device__ __forceinline__ double record_violation(const EvalParams& p, int64_t t, int32_t j,
-                                                   const int4 mt, double g, int lane) {
-  const double xv = coord(p, j, mt);
-  const double v = xv != 0.0 ? fabs(g + (xv > 0.0 ? p.lambda : -p.lambda))
-                             : fmax(fabs(g) - p.lambda, 0.0);
-  if (lane == 0) p.viol[t] = (float)v;
-  return v;
+// KKT violation of coordinate j (value xv) with gradient g: |g + lambda sign(x_j)|
+// when x_j != 0, else max(|g| - lambda, 0).
+__device__ __forceinline__ double kkt_violation(const EvalParams& p, double xv, double g) {
+  return xv != 0.0 ? fabs(g + (xv > 0.0 ? p.lambda : -p.lambda)) : fmax(fabs(g) - p.lambda, 0.0);
 }
 
-// Screened Lasso gap: |a_j^T r| over the active list only, one warp per
-// active column in 128-entry chunks (slot 3; the inactive columns are bounded
-// in the finalize step, |x|_1 and the support come from the refresh pass).
-__device__ __forceinline__ void k_gap_lasso_screened_body(const EvalParams& p, const int64_t rank,
-                                                         const int64_t nb) {
+// Active columns of at most this many entries are summed by one lane alone.
+constexpr int kLaneLen = 16;
+
+// a_j^T r64 by one lane over a short column (len <= kLaneLen, padded to 4): all
+// entry loads first, then all gathers.
+__device__ __forceinline__ double lane_dot(const EvalParams& p, const int4 mt) {
+  const int64_t start = (int64_t)(uint32_t)mt.x << 2;
+  float4 v[kLaneLen / 4];
+  int4 id[kLaneLen / 4];
+#pragma unroll
+  for (int k = 0; k < kLaneLen / 4; ++k) {
+    if (4 * k < mt.y) {
+      v[k] = __ldcs(reinterpret_cast<const float4*>(p.vals + start + 4 * k));
+      id[k] = __ldcs(reinterpret_cast<const int4*>(p.idx + start + 4 * k));
+    } else {
+      v[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      id[k] = make_int4(0, 0, 0, 0);
+    }
+  }
+  double g = 0;
+#pragma unroll
+  for (int k = 0; k < kLaneLen / 4; ++k) {
+    if (4 * k < mt.y) {
+      g += (double)v[k].x * p.r64[id[k].x];
+      g += (double)v[k].y * p.r64[id[k].y];
+      g += (double)v[k].z * p.r64[id[k].z];
+      g += (double)v[k].w * p.r64[id[k].w];
+    }
+  }
+  return g;
+}
+
+// Pass over the active list, 32 columns per warp step: lane l takes column
+// base + l and sums it alone when short; the warp then sums the long ones
+// together.  Every lane ends with g and x of its own column (valid = false
+// past the end of the list).
+struct ActiveCol {
+  bool valid;
+  int32_t j;
+  int4 mt;
+  double g;
+  double xv;
+};
+
+__device__ __forceinline__ ActiveCol active_col(const EvalParams& p, int64_t t, int64_t cnt,
+                                                int lane) {
+  ActiveCol c;
+  c.valid = t < cnt;
+  c.j = c.valid ? p.active[t] : 0;
+  c.mt = c.valid ? p.meta[c.j] : make_int4(0, 0, 0, 0);
+  c.g = c.valid && c.mt.y <= kLaneLen ? lane_dot(p, c.mt) : 0.0;
+  unsigned longs = __ballot_sync(ACDC_FULL_MASK, c.valid && c.mt.y > kLaneLen);
+  while (longs) {
+    const int src = __ffs(longs) - 1;
+    longs &= longs - 1;
+    int4 m;
+    m.x = __shfl_sync(ACDC_FULL_MASK, c.mt.x, src);
+    m.y = __shfl_sync(ACDC_FULL_MASK, c.mt.y, src);
+    m.z = m.w = 0;
+    const double g = active_dot(p, m, lane);
+    if (lane == src) c.g = g;
+  }
+  c.xv = c.valid ? coord(p, c.j) : 0.0;
+  return c;
+}
+
+// Screened Lasso gap: |a_j^T r| over the active list only (slot 3; the inactive
+// columns are bounded in the finalize step, |x|_1 and the support come from the
+// refresh pass), with the active columns' KKT violations (viol[], slot 9).
+__device__ __forceinline__ void active_pass_body(const EvalParams& p, const int64_t rank,
+                                                 const int64_t nb, bool gap_slots) {
   __shared__ double s_gm[ACDC_RED_THREADS / 32], s_vm[ACDC_RED_THREADS / 32];
   const int lane = threadIdx.x & 31;
   double gmax = 0, vmax = 0;
   const int64_t cnt = (int64_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n);
-  const int64_t warps = ((int64_t)nb * blockDim.x) >> 5;
-  for (int64_t t = ((int64_t)rank * blockDim.x + threadIdx.x) >> 5; t < cnt; t += warps) {
-    const int32_t j = p.active[t];
-    const int4 mt = p.meta[j];
-    const double g = active_dot(p, mt, lane);
-    gmax = fmax(gmax, fabs(g));
-    if (p.viol) vmax = fmax(vmax, record_violation(p, t, j, mt, g, lane));
+  const int64_t step = (int64_t)nb * blockDim.x;
+  for (int64_t base = (int64_t)rank * blockDim.x + (threadIdx.x & ~31); base < cnt; base += step) {
+    const int64_t t = base + lane;
+    const ActiveCol c = active_col(p, t, cnt, lane);
+    if (c.valid) {
+      gmax = fmax(gmax, fabs(c.g));
+      if (p.viol) {
+        const double v = kkt_violation(p, c.xv, c.g);
+        p.viol[t] = (float)v;
+        vmax = fmax(vmax, v);
+      }
+    }
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(ACDC_FULL_MASK, vmax, o));
+  for (int o = 16; o > 0; o >>= 1) {
+    gmax = fmax(gmax, __shfl_xor_sync(ACDC_FULL_MASK, gmax, o));
+    vmax = fmax(vmax, __shfl_xor_sync(ACDC_FULL_MASK, vmax, o));
+  }
   if (lane == 0) {
     s_gm[threadIdx.x >> 5] = gmax;
     s_vm[threadIdx.x >> 5] = vmax;
@@ -624,40 +724,24 @@ __device__ __forceinline__ void k_gap_lasso_screened_body(const EvalParams& p, c
       t2 = fmax(t2, s_vm[w]);
     }
     double* q = p.part + rank * ACDC_NPART;
-    q[3] = t1;
-    q[5] = 0;
-    q[7] = 0;
-    q[8] = 0;
+    if (gap_slots) {
+      q[3] = t1;
+      q[5] = 0;
+      q[7] = 0;
+      q[8] = 0;
+    }
     q[9] = t2;
   }
 }
 
-// KKT violations of the active columns after a full pass (slot 9, viol[]).
-__device__ __forceinline__ void k_active_viol_body(const EvalParams& p, const int64_t rank,
-                                                  const int64_t nb) {
-  __shared__ double s_vm[ACDC_RED_THREADS / 32];
-  const int lane = threadIdx.x & 31;
-  double vmax = 0;
-  const int64_t cnt = (int64_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n);
-  const int64_t warps = ((int64_t)nb * blockDim.x) >> 5;
-  for (int64_t t = ((int64_t)rank * blockDim.x + threadIdx.x) >> 5; t < cnt; t += warps) {
-    const int32_t j = p.active[t];
-    const int4 mt = p.meta[j];
-    vmax = fmax(vmax, record_violation(p, t, j, mt, active_dot(p, mt, lane), lane));
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(ACDC_FULL_MASK, vmax, o));
-  if (lane == 0) s_vm[threadIdx.x >> 5] = vmax;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t2 = 0;
-    for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) t2 = fmax(t2, s_vm[w]);
-    p.part[rank * ACDC_NPART + 9] = t2;
-  }
+__device__ __forceinline__ void k_gap_lasso_screened_body(const EvalParams& p, const int64_t rank,
+                                                         const int64_t nb) {
+  active_pass_body(p, rank, nb, true);
 }
 
+// KKT violations of the active columns after a full pass (slot 9, viol[]).
 __global__ void __launch_bounds__(ACDC_RED_THREADS) k_active_viol(EvalParams p) {
-  k_active_viol_body(p, blockIdx.x, gridDim.x);
+  active_pass_body(p, blockIdx.x, gridDim.x, false);
 }
 
 // Hot set, pass 1: rows of the active columns whose violation exceeds
@@ -668,37 +752,90 @@ __global__ void k_hot_mark(EvalParams p) {
   const double vmax = p.eval_out[12];
   if (!(vmax > 0)) return;
   const float thresh = (float)(p.hot_frac * vmax);
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < cnt; t += warps) {
-    if (!(p.viol[t] > thresh)) continue;
-    const int4 mt = p.meta[p.active[t]];
-    const int64_t start = (int64_t)(uint32_t)mt.x << 2;
-    for (int32_t e = lane; e < mt.y; e += 32) p.row_flag[p.idx[start + e]] = 1;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < cnt;
+       base += step) {
+    const int64_t t = base + lane;
+    unsigned hot = __ballot_sync(ACDC_FULL_MASK, t < cnt && p.viol[t] > thresh);
+    while (hot) {
+      const int src = __ffs(hot) - 1;
+      hot &= hot - 1;
+      const int4 mt = p.meta[p.active[base + src]];
+      const int64_t start = (int64_t)(uint32_t)mt.x << 2;
+      for (int32_t e = lane; e < mt.y; e += 32) p.row_flag[p.idx[start + e]] = 1;
+    }
   }
 }
 
 // Hot set, pass 2: every active column with an entry in a flagged row joins the
-// hot list; its rows are counted for the hot set's ESO parameter.
+// hot list; its rows are counted for the hot set's ESO parameter.  A lane checks
+// a short column alone; the warp checks the long ones together.
 __global__ void k_hot_collect(EvalParams p) {
   const int lane = threadIdx.x & 31;
   const int64_t cnt = (int64_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n);
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < cnt; t += warps) {
-    const int32_t j = p.active[t];
-    const int4 mt = p.meta[j];
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < cnt;
+       base += step) {
+    const int64_t t = base + lane;
+    const bool valid = t < cnt;
+    const int32_t j = valid ? p.active[t] : 0;
+    const int4 mt = valid ? p.meta[j] : make_int4(0, 0, 0, 0);
     const int64_t start = (int64_t)(uint32_t)mt.x << 2;
     bool touch = false;
-    for (int32_t e = lane; e < mt.y && !touch; e += 32) touch = p.row_flag[p.idx[start + e]] != 0;
-    if (!__any_sync(ACDC_FULL_MASK, touch)) continue;
-    if (lane == 0) {
-      const unsigned long long pos = atomicAdd(p.counters + CNT_HOT, 1ull);
+    if (valid && mt.y <= kLaneLen) {
+      int4 id[kLaneLen / 4];
+#pragma unroll
+      for (int k = 0; k < kLaneLen / 4; ++k)
+        id[k] = 4 * k < mt.y ? __ldcs(reinterpret_cast<const int4*>(p.idx + start + 4 * k))
+                             : make_int4(0, 0, 0, 0);
+      // pad entries (index 0) sit past len: only the first len rows count
+#pragma unroll
+      for (int k = 0; k < kLaneLen / 4; ++k) {
+        const int32_t e = 4 * k;
+        touch |= e < mt.y && p.row_flag[id[k].x] != 0;
+        touch |= e + 1 < mt.y && p.row_flag[id[k].y] != 0;
+        touch |= e + 2 < mt.y && p.row_flag[id[k].z] != 0;
+        touch |= e + 3 < mt.y && p.row_flag[id[k].w] != 0;
+      }
+    }
+    unsigned longs = __ballot_sync(ACDC_FULL_MASK, valid && mt.y > kLaneLen);
+    while (longs) {
+      const int src = __ffs(longs) - 1;
+      longs &= longs - 1;
+      const int64_t s0 = (int64_t)(uint32_t)__shfl_sync(ACDC_FULL_MASK, mt.x, src) << 2;
+      const int32_t len = __shfl_sync(ACDC_FULL_MASK, mt.y, src);
+      bool any = false;
+      for (int32_t e = lane; e < len && !any; e += 32) any = p.row_flag[p.idx[s0 + e]] != 0;
+      any = __any_sync(ACDC_FULL_MASK, any);
+      if (lane == src) touch = any;
+    }
+    // Join: the list entry, then the rows of the column (short: by the lane;
+    // long: by the warp).
+    const unsigned joiners = __ballot_sync(ACDC_FULL_MASK, touch);
+    if (!joiners) continue;
+    const int leader = __ffs(joiners) - 1;
+    unsigned long long first = 0;
+    if (lane == leader) first = atomicAdd(p.counters + CNT_HOT, (unsigned long long)__popc(joiners));
+    first = __shfl_sync(ACDC_FULL_MASK, first, leader);
+    if (touch) {
+      const unsigned long long pos = first + __popc(joiners & ((1u << lane) - 1u));
       if (pos < (unsigned long long)p.n) p.hot[pos] = j;
     }
     int32_t top = 0;
-    for (int32_t e = lane; e < mt.y; e += 32) top = max(top, atomicAdd(p.rowcnt + p.idx[start + e], 1) + 1);
+    if (touch && mt.y <= kLaneLen)
+      for (int32_t e = 0; e < mt.y; ++e) top = max(top, atomicAdd(p.rowcnt + p.idx[start + e], 1) + 1);
+    unsigned jl = joiners & __ballot_sync(ACDC_FULL_MASK, mt.y > kLaneLen);
+    while (jl) {
+      const int src = __ffs(jl) - 1;
+      jl &= jl - 1;
+      const int64_t s0 = (int64_t)(uint32_t)__shfl_sync(ACDC_FULL_MASK, mt.x, src) << 2;
+      const int32_t len = __shfl_sync(ACDC_FULL_MASK, mt.y, src);
+      for (int32_t e = lane; e < len; e += 32)
+        top = max(top, atomicAdd(p.rowcnt + p.idx[s0 + e], 1) + 1);
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) top = max(top, __shfl_xor_sync(ACDC_FULL_MASK, top, o));
-    if (lane == 0) atomicMax(p.counters + CNT_OMEGA_HOT, (unsigned long long)top);
+    if (lane == 0 && top > 0) atomicMax(p.counters + CNT_OMEGA_HOT, (unsigned long long)top);
   }
 }
 
@@ -751,7 +888,7 @@ __device__ __forceinline__ void k_gap_svm_body(const EvalParams& p, const int64_
     for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(ACDC_FULL_MASK, g, o);
     if (lane == 0) {
       const double y = p.rhs64[j];
-      const double a = coord(p, j, mt);
+      const double a = coord(p, j);
       if (y * g > 0) ok += 1.0;
       double h = 1.0 - y * g;
       if (h < 0) h = 0;
@@ -1021,7 +1158,34 @@ cudaError_t launch_hot_set(const EvalParams& p, cudaStream_t st) {
 // ---- batched rounds ----
 namespace {
 
-enum { EV_REFRESH_INIT, EV_REFRESH_SCATTER, EV_REFRESH_FINISH, EV_GAP_SHORT, EV_GAP_LONG, EV_GAP_SVM };
+enum {
+  EV_REFRESH_INIT,
+  EV_REFRESH_SCATTER,
+  EV_REFRESH_FINISH,
+  EV_GAP_SHORT,
+  EV_GAP_LONG,
+  EV_GAP_SVM,
+  EV_ACTIVE_OMEGA
+};
+
+// omega_A of a slot's active list: rowcnt (zeroed by the refresh pass) counts
+// the active columns per row; the largest count lands in CNT_OMEGA_ACTIVE.
+__device__ __forceinline__ void active_omega_body(const EvalParams& p, const int64_t rank,
+                                                  const int64_t nb) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)nb * blockDim.x) >> 5;
+  const int64_t cnt = (int64_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n);
+  int32_t top = 0;
+  for (int64_t t = ((int64_t)rank * blockDim.x + threadIdx.x) >> 5; t < cnt; t += warps) {
+    const int4 mt = p.meta[p.active[t]];
+    const int64_t start = (int64_t)(uint32_t)mt.x << 2;
+    for (int32_t e = lane; e < mt.y; e += 32)
+      top = max(top, atomicAdd(p.rowcnt + p.idx[start + e], 1) + 1);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) top = max(top, __shfl_xor_sync(ACDC_FULL_MASK, top, o));
+  if (lane == 0 && top > 0) atomicMax(p.counters + CNT_OMEGA_ACTIVE, (unsigned long long)top);
+}
 
 // One evaluation kernel over every live slot; a block serves its slot at rank
 // blockIdx.x - first block of the slot, out of that slot's block count.
@@ -1035,6 +1199,19 @@ __global__ void __launch_bounds__(ACDC_RED_THREADS) k_eval_batch(BatchDev b) {
   const int64_t rank = (int64_t)blockIdx.x - b.eblk_first[s];
   const int64_t nb = b.eblk_count[s];
   if (KIND == EV_REFRESH_INIT) k_refresh_init_body(p, rank, nb);
+  if (KIND == EV_REFRESH_INIT && p.active && p.rowcnt) {
+    // The gap pass of this round rebuilds the active list and its row counts.
+    if (rank == 0 && threadIdx.x == 0) {
+      p.counters[CNT_ACTIVE] = 0;
+      p.counters[CNT_OMEGA_ACTIVE] = 0;
+    }
+    const int64_t stride = nb * blockDim.x;
+    for (int64_t i = rank * blockDim.x + threadIdx.x; i < p.m; i += stride) p.rowcnt[i] = 0;
+  }
+  if (KIND == EV_ACTIVE_OMEGA) {
+    if (p.active && p.rowcnt) active_omega_body(p, rank, nb);
+    return;
+  }
   if (KIND == EV_REFRESH_SCATTER) k_refresh_scatter_body(p, rank, nb);
   if (KIND == EV_REFRESH_FINISH) k_refresh_finish_body(p, rank, nb);
   if (KIND == EV_GAP_SHORT) k_gap_lasso_short_body(p, rank, nb);
@@ -1091,6 +1268,26 @@ __global__ void __launch_bounds__(kFinThreads) k_batch_control(BatchDev b) {
     } else if (!up.fp64 && o[3] <= c.polish_rel_gap) {
       action = 1;
     }
+    // Next round: uniform right after a lambda change (the active list was built
+    // for the previous lambda), else active-set draws.
+    c.shrink_next = c.updates_here > 0 ? 1 : 0;
+    const int64_t a = (int64_t)min(up.counters[CNT_ACTIVE], (unsigned long long)epc.n);
+    if (c.shrink && c.shrink_next && a > 0) {
+      const double tau = (double)up.n_warps;
+      const double draws = c.q * tau;
+      const double w_a = fmax(1.0, (double)up.counters[CNT_OMEGA_ACTIVE]);
+      const double beta_a =
+          a > 1 && draws > 1 ? 1.0 + (w_a - 1.0) * (draws - 1.0) / ((double)a - 1.0) : 1.0;
+      up.li_scale = c.beta / fmax(c.beta, beta_a);
+      up.shrink_q32 = c.q32;
+      const double lo = fmax(32.0 * tau, 0.25 * (double)epc.n);
+      const double want = (double)c.active_passes * (double)a / c.q;
+      up.count = (uint64_t)fmin((double)c.round_updates, fmax(lo, want));
+    } else {
+      up.li_scale = 1.0;
+      up.shrink_q32 = 0;
+      up.count = c.round_updates;
+    }
     up.counters[CNT_WORK] = 0;
     s_action = action;
   }
@@ -1098,10 +1295,10 @@ __global__ void __launch_bounds__(kFinThreads) k_batch_control(BatchDev b) {
   const int action = s_action;
   if (action == 1) {
     for (int64_t j = threadIdx.x; j < epc.n; j += blockDim.x)
-      up.x64[j] = (double)__int_as_float(epc.meta[j].w);
+      up.x64[j] = (double)epc.x32[j];
   } else if (action == 2) {
     for (int64_t j = threadIdx.x; j < epc.n; j += blockDim.x)
-      epc.meta[j].w = __float_as_int((float)up.x64[j]);
+      epc.x32[j] = (float)up.x64[j];
   }
   __syncthreads();
   if (threadIdx.x == 0 && action == 1) {
@@ -1123,6 +1320,7 @@ cudaError_t launch_batch_eval(const BatchDev& b, int eval_blocks, cudaStream_t s
   k_eval_batch<EV_GAP_SHORT><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
   k_eval_batch<EV_GAP_LONG><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
   k_eval_batch<EV_GAP_SVM><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
+  k_eval_batch<EV_ACTIVE_OMEGA><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
   k_batch_control<<<b.n_slots, kFinThreads, 0, st>>>(b);
   return cudaGetLastError();
 }

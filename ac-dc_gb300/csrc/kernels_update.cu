@@ -22,13 +22,13 @@
 // 4l..4l+3 as one 16-byte transfer of values and one of indices (the device
 // layout starts every column on a 16-byte boundary).  The warp waits only for
 // the copies of update s (cp.async.wait_group D-1), so D updates' worth of DRAM
-// traffic is in flight per warp while it waits on its L2 gathers of r.  x_j and
-// r are read when the update runs (ld.global.cg, L2), so the sequence of
+// traffic is in flight per warp while it waits on its L2 gathers of r.  x_j (in
+// x32 or x64) and r are read when the update runs (ld.global.cg, L2), so the sequence of
 // updates a warp performs reads exactly the state its own previous updates left.
 // Entries beyond the first 128 of a long column are streamed with direct loads.
 //
-// Precision: T = float keeps x in the column metadata and r in FP32 (the bulk
-// mode); T = double keeps x and r in FP64 arrays (the polish mode).  Matrix
+// Precision: T = float keeps x and r in FP32 (the bulk mode); T = double keeps
+// x and r in FP64 arrays (the polish mode).  Matrix
 // values are FP32 in both.
 #include "acdc_internal.cuh"
 
@@ -228,7 +228,7 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
       if constexpr (sizeof(T) == 8)
         xj = __ldcg(p.x64 + j);
       else
-        xj = __int_as_float(__ldcg(&p.meta[j].w));
+        xj = __ldcg(p.x32 + j);
       const uint64_t start = (uint64_t)(uint32_t)mt.x << 2;
       const uint32_t len = (uint32_t)mt.y;
       const uint32_t e0 = 4u * (uint32_t)lane;
@@ -289,7 +289,7 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
           if constexpr (sizeof(T) == 8)
             atomicAdd(p.x64 + j, delta);
           else
-            atomicAdd(reinterpret_cast<float*>(&p.meta[j].w), delta);
+            atomicAdd(p.x32 + j, delta);
         }
       }
     }

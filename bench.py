@@ -50,12 +50,26 @@ WORKLOADS = {
     "lasso_m2e3_n1e4": dict(m=2000, n=10000, nnz_mode=0, nnz_per_col=20, n_star=100,
                             noise_sigma=0.01, lambda_frac=0.1, seed=0xACDC0000, tau=64,
                             refresh_every=2, gap=1e-6, max_epochs=3000, tau_active=64, active_passes=20),
+    # hinge-loss SVM dual: 20,000 samples x 1,355,191 features, log-normal sample
+    # lengths (median 450, sigma 0.8), Exp(1) values scaled to unit rows, labels of
+    # a sparse w* (5,000 entries) with 5% flips, lambda = 1e-4, mini-batch of 1024
+    # in flight, absolute duality gap 1e-5
+    "svm_n2e4_d1355191": dict(loss="svm", m=1_355_191, n=20_000, nnz_median=450.0,
+                              nnz_sigma=0.8, w_star_nnz=5000, flip_prob=0.05, lam=1e-4,
+                              seed=0xACDC0002, tau=1024, refresh_every=5, gap=1e-5,
+                              max_epochs=3000),
 }
-METRIC = "lasso_time_to_gap_1e-6"
-# Kernels launched per evaluation (refresh: init, scatter, finish; gap: short,
-# long, finalize; active-set omega: row count, max) and per reset (set_x + refresh).
+METRICS = {"lasso": "lasso_time_to_gap_1e-6", "svm": "svm_time_to_gap_1e-5"}
+# Kernels launched per evaluation (refresh: init, scatter, finish; Lasso gap:
+# short, long, finalize; SVM gap: one pass, finalize) and per reset (set_x +
+# refresh).
 KERNELS_PER_EVAL = 6
-KERNELS_PER_EVAL_SHRINK = 8
+KERNELS_PER_EVAL_SVM = 5
+# Lasso with shrinking: a full evaluation adds the active-set violations, the
+# active-set omega (row count, max) and the hot set (mark, collect); a screened
+# one is refresh (3), the active-column pass, finalize and the hot set (2).
+KERNELS_PER_EVAL_SHRINK = 11
+KERNELS_PER_EVAL_SCREENED = 7
 KERNELS_PER_RESET = 4
 # Columns of the update kernel's algorithmic bytes (FP32 values and state, int32
 # indices): every update reads 12 bytes per entry (value, row index, residual
@@ -83,7 +97,139 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--max-epochs", type=int, default=0,
                     help="cap each solve (profiling runs; the line then reports converged=false)")
+    ap.add_argument("--batch-instances", type=int, default=8,
+                    help="instances of the batched lambda-path sample (0 = skip)")
+    ap.add_argument("--batch-max-epochs", type=int, default=300)
+    ap.add_argument("--serve-requests", type=int, default=128,
+                    help="requests of the serving sample (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=1000.0)
     return ap.parse_args()
+
+
+def batch_sample(count, seed=0xACDC0003):
+    """Instances of the batched lambda-path workload: m log-uniform in [500, 50,000],
+    n log-uniform in [1,000, 200,000], 5..50 entries per column, each with the
+    16-point path lambda_max 0.5^k, k = 1..16."""
+    import acdc
+    import numpy as np
+    insts = []
+    for i in range(count):
+        m, n = acdc.mix_sizes(seed, i)
+        insts.append(acdc.gen_lasso(m, n, nnz_mode=acdc.NNZ_UNIFORM, nnz_min=5, nnz_max=50,
+                                    n_star=max(1, n // 100), lambda_frac=1.0, seed=seed + i))
+    lams = np.array([[x.lam * 0.5 ** k for k in range(1, 17)] for x in insts])
+    return insts, lams
+
+
+def run_batched(ctx, count, max_epochs):
+    """Batched solves/s of the lambda-path sample against the plain one-instance
+    path on the same instances (both with q-shrinking, gap 1e-6 per lambda)."""
+    import acdc
+    insts, lams = batch_sample(count)
+    out = {"workload": "lasso_paths_mix", "instances": count, "lambdas_per_instance": 16,
+           "solves": count * 16, "gap_target_relative": 1e-6, "max_epochs_per_lambda": max_epochs,
+           "sizes": "m logU[500,5e4], n logU[1e3,2e5], 5..50 per column (the 512-instance "
+                    "workload's distribution, first %d instances)" % count,
+           "nnz": int(sum(x.nnz for x in insts))}
+    for plain in (0, 1):
+        probs = [acdc.Problem(ctx, x) for x in insts]
+        for q in probs:
+            q.synchronize()
+        t = time.perf_counter()
+        res, _ = acdc.batch_solve_path(ctx, probs, lams, gap_target=1e-6, max_epochs=max_epochs,
+                                       refresh_every=2, autotune=1, plain=plain, use_shrinking=1)
+        dt = time.perf_counter() - t
+        for q in probs:
+            q.close()
+        key = "plain" if plain else "batched"
+        conv = sum(r.converged for row in res for r in row)
+        out[key] = {"seconds": dt, "solves_per_s": count * 16 / dt, "converged": int(conv),
+                    "converged_per_s": conv / dt}
+    out["speedup"] = out["batched"]["solves_per_s"] / out["plain"]["solves_per_s"]
+    return out
+
+
+def serve_sample(count, rate, seed=0xACDC0004, scale=0.25):
+    """Requests of the serving workload: 70% Lasso of the lambda-path mix's size
+    distribution (m, n scaled by `scale`, lambda = lambda_max / 2), 30% SVM duals
+    from the SVM generator scaled down (samples log-uniform in [1,000, 50,000 x
+    scale], 10 features per sample, median 100 entries, lambda = 1e-3); Poisson
+    arrivals at `rate` per second."""
+    import acdc
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(count):
+        if rng.random() < 0.7:
+            m, n = acdc.mix_sizes(seed, i, m_lo=500, m_hi=int(50000 * scale), n_lo=1000,
+                                  n_hi=int(200000 * scale))
+            reqs.append(acdc.gen_lasso(m, n, nnz_mode=acdc.NNZ_UNIFORM, nnz_min=5, nnz_max=50,
+                                       n_star=max(1, n // 100), lambda_frac=0.5, seed=seed + i))
+        else:
+            _, ns = acdc.mix_sizes(seed + 0x10, i, n_lo=1000, n_hi=int(50000 * scale))
+            reqs.append(acdc.gen_svm(ns, 10 * ns, nnz_median=100, nnz_sigma=0.8,
+                                     w_star_nnz=max(10, ns // 20), lam=1e-3, seed=seed + 0x10 + i))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
+    return reqs, arrivals
+
+
+def latency_summary(lat_s, span_s, conv, count):
+    import numpy as np
+    lat = np.array(lat_s) * 1e3
+    return {"solves_per_s": count / span_s, "p50_ms": float(np.percentile(lat, 50)),
+            "p90_ms": float(np.percentile(lat, 90)), "p99_ms": float(np.percentile(lat, 99)),
+            "converged": int(conv), "span_s": span_s}
+
+
+def run_serving(ctx, count, rate):
+    """Continuous batching (acdc_server_*) against the plain path (one request at
+    a time through acdc_batch_solve_path with plain = 1) on the same arrivals;
+    latency = finish - arrival, host monotonic clock."""
+    import acdc
+    import numpy as np
+    reqs, arr = serve_sample(count, rate)
+    out = {"workload": "serve_mix_70_30", "requests": count, "rate_per_s": rate,
+           "gap_target": 1e-6, "nnz": int(sum(x.nnz for x in reqs))}
+    srv = acdc.Server(ctx, memory_budget_bytes=120 << 30, max_slots=256, quantum_rounds=2,
+                      max_epochs=3000, use_shrinking=1)
+    start = time.monotonic()
+    tickets, nxt = {}, 0
+    while True:
+        now = time.monotonic() - start
+        while nxt < count and arr[nxt] <= now:
+            tickets[nxt] = srv.submit(reqs[nxt], gap_target=1e-6, seed=1)
+            nxt += 1
+        pend = srv.step()
+        if nxt >= count and pend == 0:
+            break
+        if pend == 0 and nxt < count:
+            time.sleep(max(0.0, min(0.002, arr[nxt] - (time.monotonic() - start))))
+    lat, fin, conv = [], [], 0
+    for i in range(count):
+        res, _ = srv.poll(tickets[i])
+        lat.append(res.finish_time - (start + arr[i]))
+        fin.append(res.finish_time - start)
+        conv += res.converged
+    srv.close()
+    out["server"] = latency_summary(lat, max(fin) - arr[0], conv, count)
+    start = time.monotonic()
+    lat, fin, conv = [], [], 0
+    for i in range(count):
+        now = time.monotonic() - start
+        if now < arr[i]:
+            time.sleep(arr[i] - now)
+        q = acdc.Problem(ctx, reqs[i])
+        res, _ = acdc.batch_solve_path(ctx, [q], np.array([[reqs[i].lam]]), gap_target=1e-6,
+                                       max_epochs=3000, refresh_every=1, autotune=1, plain=1,
+                                       want_x=True, use_shrinking=1)
+        q.close()
+        t = time.monotonic() - start
+        lat.append(t - arr[i])
+        fin.append(t)
+        conv += res[0][0].converged
+    out["plain"] = latency_summary(lat, max(fin) - arr[0], conv, count)
+    out["speedup"] = out["server"]["solves_per_s"] / out["plain"]["solves_per_s"]
+    return out
 
 
 def dist_env():
@@ -171,8 +317,16 @@ def load_json(path, default=None):
         return default
 
 
+def is_svm(w):
+    return w.get("loss") == "svm"
+
+
 def generate(w, pinned):
     import acdc
+    if is_svm(w):
+        return acdc.gen_svm(w["n"], w["m"], nnz_median=w["nnz_median"], nnz_sigma=w["nnz_sigma"],
+                            w_star_nnz=w["w_star_nnz"], flip_prob=w["flip_prob"], lam=w["lam"],
+                            seed=w["seed"], pinned=pinned)
     if w["nnz_mode"] == 1:
         return acdc.gen_lasso(w["m"], w["n"], nnz_mode=acdc.NNZ_ZIPF, zipf_s=w["zipf_s"],
                               nnz_min=w["nnz_min"], nnz_max=w["nnz_max"], nnz_mean=w["nnz_mean"],
@@ -185,6 +339,11 @@ def generate(w, pinned):
 
 def settings_for(w):
     import acdc
+    if is_svm(w):
+        return acdc.default_settings(acdc.LOSS_SVM_DUAL, tau=w["tau"], warps_per_block=8,
+                                     refresh_every=w["refresh_every"], gap_target=w["gap"],
+                                     gap_relative=0, max_epochs=w["max_epochs"], seed=1,
+                                     precision=acdc.PREC_FP32)
     return acdc.default_settings(acdc.LOSS_L1_SQUARE, tau=w["tau"], warps_per_block=8,
                                  refresh_every=w["refresh_every"], gap_target=w["gap"],
                                  gap_relative=1, max_epochs=w["max_epochs"], use_shrinking=1,
@@ -198,7 +357,11 @@ def cpu_time_per_epoch(inst, threads, updates):
     on the host cores for a bounded number of updates from x = 0."""
     sys.path.insert(0, ORACLE)
     import oracle
-    L = oracle.Lasso(inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals, inst.rhs, inst.lam)
+    import acdc
+    if inst.loss == acdc.LOSS_SVM_DUAL:
+        L = oracle.SVM(inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals, inst.rhs, inst.lam)
+    else:
+        L = oracle.Lasso(inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals, inst.rhs, inst.lam)
     secs = L.hogwild(updates, 1, threads)
     return secs * inst.n / updates, secs
 
@@ -229,10 +392,11 @@ def run_reference(args, w):
               "%d threads; time-to-gap = s/epoch x %d epochs (the epochs the GPU solver needs "
               "with q-shrinking; the reference samples uniformly, so this is a lower bound)"
               % (upd, upd / inst.n, threads, epochs))
-    line = {"metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
+    line = {"metric": METRICS[w.get("loss", "lasso")], "value": value, "unit": "s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded Zipf Lasso generator)", "impl": "reference",
+            "data": "synthetic (seeded %s generator)" % ("SVM" if is_svm(w) else "Zipf Lasso"),
+            "impl": "reference",
             "config": {"workload": args.workload, "m": w["m"], "n": w["n"], "nnz": inst.nnz,
                        "threads": threads, "seconds_per_epoch": per_epoch},
             "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
@@ -316,9 +480,15 @@ def run_ours(args, w):
                 "alg_bytes_per_launch": alg_bytes / launches if launches else 0,
                 "avg_launch_ms": upd_ms / launches if launches else 0}
 
-    kpe = KERNELS_PER_EVAL_SHRINK if s.use_shrinking else KERNELS_PER_EVAL
-    gpu_launches = sum(r.stats.update_launches + kpe * r.stats.eval_launches + KERNELS_PER_RESET +
-                       (1 if r.fp64_epochs else 0) for r in results)
+    if is_svm(w):
+        k_full, k_scr = KERNELS_PER_EVAL_SVM, 0
+    elif s.use_shrinking:
+        k_full, k_scr = KERNELS_PER_EVAL_SHRINK, KERNELS_PER_EVAL_SCREENED
+    else:
+        k_full, k_scr = KERNELS_PER_EVAL, 0
+    gpu_launches = sum(r.stats.update_launches + k_scr * r.stats.screened_evals +
+                       k_full * (r.stats.eval_launches - r.stats.screened_evals) +
+                       KERNELS_PER_RESET + (1 if r.fp64_epochs else 0) for r in results)
 
     # e2e: the same metric through the C-ABI from pinned host buffers.
     h2d = inst.col_ptr.nbytes + inst.row_idx.nbytes + inst.vals.nbytes + inst.rhs.nbytes
@@ -350,18 +520,30 @@ def run_ours(args, w):
                           % (upd, secs, threads, ep))}
 
     p.close()
+    batched = serving = None
+    if rank == 0 and not is_svm(w):
+        if args.batch_instances > 0:
+            batched = run_batched(ctx, args.batch_instances, args.batch_max_epochs)
+        if args.serve_requests > 0:
+            serving = run_serving(ctx, args.serve_requests, args.serve_rate)
+    if is_svm(w):
+        solver_keys = {"gap_target_absolute": w["gap"], "q_shrinking": 0, "lambda": w["lam"]}
+    else:
+        solver_keys = {"gap_target_relative": w["gap"], "q_shrinking": 0.9,
+                       "tau_active": w["tau_active"], "active_passes": w["active_passes"],
+                       "screened_eval": 1, "hot_threshold": 0.1}
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "metric": METRICS[w.get("loss", "lasso")], "value": value, "unit": "s", "n_gpus": world,
+            "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded Zipf Lasso generator; inputs larger than L2)",
-            "config": {"workload": args.workload, "m": w["m"], "n": w["n"], "nnz": inst.nnz,
+            "data": "synthetic (seeded %s generator; inputs larger than L2)"
+                    % ("SVM" if is_svm(w) else "Zipf Lasso"),
+            "config": dict(solver_keys, **{
+                       "workload": args.workload, "m": w["m"], "n": w["n"], "nnz": inst.nnz,
                        "tau": w["tau"], "refresh_every": w["refresh_every"],
-                       "gap_target_relative": w["gap"], "q_shrinking": 0.9,
                        "precision": "fp32 bulk, fp64 refresh and gap",
-                       "tau_active": w["tau_active"], "active_passes": w["active_passes"],
-                       "screened_eval": 1, "hot_threshold": 0.1,
                        "updates": int(updates), "update_launches": int(launches),
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (no flush)", "omega": info.omega,
@@ -369,13 +551,15 @@ def run_ours(args, w):
                        "fp64_epochs": [r.fp64_epochs for r in results],
                        "converged": converged, "final_rel_gap": [r.eval.rel_gap for r in results],
                        "objective": results[-1].eval.primal, "support": results[-1].eval.support,
-                       "host_wall_s": wall / args.steps, "generate_s": t_gen},
+                       "host_wall_s": wall / args.steps, "generate_s": t_gen}),
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(gpu_launches),
             "clocks": clk,
+            "batched": batched,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -243,7 +243,11 @@ typedef struct acdc_batch_options {
   int32_t autotune;         /* 1: choose tau / CTA packing per instance           */
   int32_t tau_override;     /* > 0: fixed tau for every instance                  */
   int32_t plain;            /* 1: solve one instance per launch sequence (baseline) */
-  int32_t reserved[8];
+  int32_t use_shrinking;    /* 1: q-shrinking (q = 0.9) for Lasso instances, from
+                               the second round of each lambda                    */
+  int32_t active_passes;    /* while shrinking, passes over the active set per
+                               round (default 20 when 0)                          */
+  int32_t reserved[6];
 } acdc_batch_options;
 
 typedef struct acdc_batch_result {
@@ -268,9 +272,11 @@ int acdc_batch_solve_path(acdc_ctx* ctx, int32_t count, acdc_problem* const* pro
 typedef struct acdc_server_options {
   int64_t memory_budget_bytes;  /* device bytes admitted at once                  */
   int32_t max_slots;            /* requests on the device at once                 */
-  int32_t quantum_epochs;       /* epochs per scheduling round                    */
+  int32_t quantum_epochs;       /* rounds per acdc_server_step (a round is one
+                                   epoch, or with shrinking at most one)          */
   int32_t max_epochs;           /* per request                                    */
-  int32_t reserved[7];
+  int32_t use_shrinking;        /* 1: q-shrinking for Lasso requests              */
+  int32_t reserved[6];
 } acdc_server_options;
 
 typedef struct acdc_request {

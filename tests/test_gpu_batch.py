@@ -29,11 +29,12 @@ def path_for(inst):
     return np.array([inst.lam * 0.5 ** k for k in range(1, PATH + 1)])
 
 
-def solve_batch(ctx, insts, plain):
+def solve_batch(ctx, insts, plain, use_shrinking=0):
     probs = [acdc.Problem(ctx, inst) for inst in insts]
     lams = np.stack([path_for(inst) for inst in insts])
     res, xs = acdc.batch_solve_path(ctx, probs, lams, gap_target=1e-6, max_epochs=3000,
-                                    refresh_every=2, autotune=1, plain=plain, want_x=True)
+                                    refresh_every=2, autotune=1, plain=plain, want_x=True,
+                                    use_shrinking=use_shrinking)
     for p in probs:
         p.close()
     return res, xs
@@ -53,17 +54,31 @@ def test_batched_equals_plain_per_lambda(ctx):
         assert set(np.nonzero(xb[i])[0]) == set(np.nonzero(xp[i])[0]), i
 
 
-def test_batched_path_matches_oracle_warm_started_path(ctx):
+@pytest.mark.parametrize("use_shrinking", [0, 1])
+def test_batched_path_matches_oracle_warm_started_path(ctx, use_shrinking):
     insts = make_instances(11, 4)
-    rb, xb = solve_batch(ctx, insts, plain=0)
+    rb, xb = solve_batch(ctx, insts, plain=0, use_shrinking=use_shrinking)
     for i, inst in enumerate(insts):
         x = None
         for k, lam in enumerate(path_for(inst)):
             x, r, ev, ep = oracle.lasso_solve(inst.m, inst.n, inst.col_ptr, inst.row_idx,
                                               inst.vals, inst.rhs, lam, seed=1, target=1e-10,
                                               x0=x)
+            assert rb[i][k].converged, (i, k, rb[i][k].eval.rel_gap)
             assert abs(rb[i][k].eval.primal - ev["primal"]) <= 1e-6 * abs(ev["primal"]), (i, k)
         assert set(np.nonzero(xb[i])[0]) == set(np.nonzero(x)[0]), i
+
+
+def test_shrinking_batched_equals_shrinking_plain(ctx):
+    insts = make_instances(17, 6)
+    rb, xb = solve_batch(ctx, insts, plain=0, use_shrinking=1)
+    rp, xp = solve_batch(ctx, insts, plain=1, use_shrinking=1)
+    for i in range(len(insts)):
+        for k in range(PATH):
+            b, p = rb[i][k], rp[i][k]
+            assert b.converged and p.converged, (i, k, b.eval.rel_gap, p.eval.rel_gap)
+            assert abs(b.eval.primal - p.eval.primal) <= 1e-6 * abs(p.eval.primal), (i, k)
+        assert set(np.nonzero(xb[i])[0]) == set(np.nonzero(xp[i])[0]), i
 
 
 def test_batch_mixes_losses_and_sizes(ctx):
