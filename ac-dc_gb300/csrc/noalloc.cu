@@ -3,6 +3,12 @@
 // from cudaMalloc on every call; this variant writes the draws into a fixed
 // device array of this file and copies them out of it.
 //
+// Who needs it: a caller that must not allocate device memory while it runs.
+// Two examples are a process whose device memory the server's admission budget
+// has already handed to resident problems, where a cudaMalloc may fail, and a
+// caller checking the sampler while solves run on other streams, where
+// cudaFree would synchronise the whole device and stall them.
+//
 // Scratch: ACDC_NOALLOC_MAX_SAMPLES int64 draws (512 KiB) and one status word,
 // both file-scope __device__ arrays of this module.  Their device addresses
 // are looked up once per device with cudaGetSymbolAddress, with that device

@@ -1,7 +1,11 @@
-"""acdc_debug_sample_noalloc against acdc_debug_sample: the fixed-scratch
-variant (no allocation) returns the same draws on two calls in a row, and
-refuses counts beyond its scratch.  Collected last, so it also runs after every
-other GPU test has used the device."""
+"""acdc_debug_sample_noalloc against acdc_debug_sample.  The no-allocation
+variant serves callers that must not allocate device memory while they run (a
+process whose memory is committed to resident problems, or one checking the
+sampler beside running solves, where cudaFree would synchronise the device).
+Through the C-ABI it must return the same draws as the allocating entry point
+on two calls in a row (the fixed scratch keeps the previous call's contents),
+and refuse counts beyond its scratch.  Collected last, so a run that stops at
+the first failure has run every other test before it."""
 import numpy as np
 import pytest
 
