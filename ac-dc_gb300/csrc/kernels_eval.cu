@@ -651,9 +651,11 @@ __device__ __forceinline__ double lane_dot(const EvalParams& p, const int4 mt) {
   return g;
 }
 
-// Pass over the active list, 32 columns per warp step: lane l takes column
-// base + l and sums it alone when short; the warp then sums the long ones
-// together.  Every lane ends with g and x of its own column (valid = false
+// Pass over the active list, 32 columns per warp step.  The list holds the
+// long columns together (the long gap pass appends them), so the entries are
+// dealt out with a stride: in step k, lane l of warp w (of W) takes entry
+// 32 W k + W l + w, and no warp is left with a run of long columns.  A lane
+// sums a short column alone; the warp then sums the long ones together.  Every lane ends with g and x of its own column (valid = false
 // past the end of the list).
 struct ActiveCol {
   bool valid;
@@ -695,8 +697,9 @@ __device__ __forceinline__ void active_pass_body(const EvalParams& p, const int6
   double gmax = 0, vmax = 0;
   const int64_t cnt = (int64_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n);
   const int64_t step = (int64_t)nb * blockDim.x;
-  for (int64_t base = (int64_t)rank * blockDim.x + (threadIdx.x & ~31); base < cnt; base += step) {
-    const int64_t t = base + lane;
+  const int64_t nw = step >> 5, gw = ((int64_t)rank * blockDim.x + threadIdx.x) >> 5;
+  for (int64_t base = 0; base < cnt; base += step) {
+    const int64_t t = base + lane * nw + gw;
     const ActiveCol c = active_col(p, t, cnt, lane);
     if (c.valid) {
       gmax = fmax(gmax, fabs(c.g));
@@ -753,14 +756,14 @@ __global__ void k_hot_mark(EvalParams p) {
   if (!(vmax > 0)) return;
   const float thresh = (float)(p.hot_frac * vmax);
   const int64_t step = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < cnt;
-       base += step) {
-    const int64_t t = base + lane;
+  const int64_t nw = step >> 5, gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  for (int64_t base = 0; base < cnt; base += step) {
+    const int64_t t = base + lane * nw + gw;
     unsigned hot = __ballot_sync(ACDC_FULL_MASK, t < cnt && p.viol[t] > thresh);
     while (hot) {
       const int src = __ffs(hot) - 1;
       hot &= hot - 1;
-      const int4 mt = p.meta[p.active[base + src]];
+      const int4 mt = p.meta[p.active[base + src * nw + gw]];
       const int64_t start = (int64_t)(uint32_t)mt.x << 2;
       for (int32_t e = lane; e < mt.y; e += 32) p.row_flag[p.idx[start + e]] = 1;
     }
@@ -774,9 +777,9 @@ __global__ void k_hot_collect(EvalParams p) {
   const int lane = threadIdx.x & 31;
   const int64_t cnt = (int64_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n);
   const int64_t step = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < cnt;
-       base += step) {
-    const int64_t t = base + lane;
+  const int64_t nw = step >> 5, gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  for (int64_t base = 0; base < cnt; base += step) {
+    const int64_t t = base + lane * nw + gw;
     const bool valid = t < cnt;
     const int32_t j = valid ? p.active[t] : 0;
     const int4 mt = valid ? p.meta[j] : make_int4(0, 0, 0, 0);
@@ -805,7 +808,13 @@ __global__ void k_hot_collect(EvalParams p) {
       const int64_t s0 = (int64_t)(uint32_t)__shfl_sync(ACDC_FULL_MASK, mt.x, src) << 2;
       const int32_t len = __shfl_sync(ACDC_FULL_MASK, mt.y, src);
       bool any = false;
-      for (int32_t e = lane; e < len && !any; e += 32) any = p.row_flag[p.idx[s0 + e]] != 0;
+      for (int32_t e0 = lane; e0 < len && !any; e0 += 128) {
+        int32_t row[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) row[k] = e0 + 32 * k < len ? p.idx[s0 + e0 + 32 * k] : -1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) any |= row[k] >= 0 && p.row_flag[row[k]] != 0;
+      }
       any = __any_sync(ACDC_FULL_MASK, any);
       if (lane == src) touch = any;
     }
@@ -830,8 +839,14 @@ __global__ void k_hot_collect(EvalParams p) {
       jl &= jl - 1;
       const int64_t s0 = (int64_t)(uint32_t)__shfl_sync(ACDC_FULL_MASK, mt.x, src) << 2;
       const int32_t len = __shfl_sync(ACDC_FULL_MASK, mt.y, src);
-      for (int32_t e = lane; e < len; e += 32)
-        top = max(top, atomicAdd(p.rowcnt + p.idx[s0 + e], 1) + 1);
+      for (int32_t e0 = lane; e0 < len; e0 += 128) {
+        int32_t row[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) row[k] = e0 + 32 * k < len ? p.idx[s0 + e0 + 32 * k] : -1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (row[k] >= 0) top = max(top, atomicAdd(p.rowcnt + row[k], 1) + 1);
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) top = max(top, __shfl_xor_sync(ACDC_FULL_MASK, top, o));

@@ -7,8 +7,8 @@ and rescaled to mean 20 (about 2.0e8 nonzeros), uniform distinct rows, N(0,1)
 values scaled to unit columns; x* has 10,000 entries +-1; b = A x* + N(0, 0.01^2);
 lambda = 0.05 ||A^T b||_inf.  Seeded synthetic data (no dataset is shipped).
 PCDM with tau = 4096, FP32 bulk with FP64 refresh and duality gap every 5 epochs,
-q-shrinking (q = 0.9) after 5 epochs with 2048 updates in flight on the active
-set, 50 active-set passes between refreshes, screened evaluations and the
+q-shrinking (q = 0.9) after 5 epochs with 1024 updates in flight on the active
+set, 100 active-set passes between refreshes, screened evaluations and the
 hot-set tier (threshold 0.1); target relative duality gap 1e-6.
 
 A step is one solve from x = 0 to the target gap with the matrix resident in
@@ -39,7 +39,7 @@ WORKLOADS = {
     "lasso_m1e6_n1e7_zipf": dict(m=1_000_000, n=10_000_000, nnz_mode=1, zipf_s=1.5, nnz_min=1,
                                  nnz_max=2000, nnz_mean=20.0, n_star=10_000, noise_sigma=0.01,
                                  lambda_frac=0.05, seed=0xACDC0001, tau=4096, refresh_every=5,
-                                 gap=1e-6, max_epochs=12000, tau_active=2048, active_passes=50),
+                                 gap=1e-6, max_epochs=12000, tau_active=1024, active_passes=100),
     # the same generator at 3e5 x 3e6 (about 6e7 nonzeros): small enough for full
     # profiler captures
     "lasso_m3e5_n3e6_zipf": dict(m=300_000, n=3_000_000, nnz_mode=1, zipf_s=1.5, nnz_min=1,
@@ -103,7 +103,37 @@ def parse_args():
     ap.add_argument("--serve-requests", type=int, default=128,
                     help="requests of the serving sample (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=1000.0)
+    ap.add_argument("--probe-launches", action="store_true",
+                    help="profiling aid: run one uniform-draw update launch (refresh_every "
+                         "epochs) and one active-set launch (active_passes |A|/q updates) on "
+                         "the workload and print their work counters")
     return ap.parse_args()
+
+
+def probe_launches(w):
+    """Two update launches of known size for a profiler capture: a uniform bulk
+    from x = 0, then (after a full evaluation built the active set) one bulk of
+    active-set draws, without the hot tier."""
+    import acdc
+    inst = generate(w, pinned=False)
+    ctx = acdc.Context(0)
+    s = settings_for(w)
+    s.hot_threshold = 0.0
+    p = acdc.Problem(ctx, inst, s)
+    p.run_updates(w["refresh_every"] * inst.n)
+    p.synchronize()
+    first = p.stats()
+    ev = p.evaluate()
+    count = int(w["active_passes"] * ev["active"] / 0.9)
+    p.reset_stats()
+    p.run_updates(count)
+    p.synchronize()
+    second = p.stats()
+    print(json.dumps({"workload": w.get("name"), "uniform_launch": first,
+                      "active_launch": dict(second, active_set=ev["active"])}), flush=True)
+    p.close()
+    ctx.close()
+    return 0
 
 
 def batch_sample(count, seed=0xACDC0003):
@@ -470,10 +500,15 @@ def run_ours(args, w):
     peak_src = "measured"
     if not peak:
         peak, peak_src = 6800.0, "fallback"
+    # DRAM traffic per launch from the committed per-update figures of the two
+    # launch kinds: each solve's first launch draws uniformly (refresh_every
+    # epochs), the others draw mostly from the active set.
     traffic_rec = load_json(TRAFFIC_FILE, {})
     traffic = None
-    if traffic_rec.get("dram_bytes_per_update") and launches:
-        traffic = traffic_rec["dram_bytes_per_update"] * updates / launches
+    if traffic_rec.get("uniform_dram_bytes_per_update") and launches and not is_svm(w):
+        uniform = min(updates, len(results) * w["refresh_every"] * inst.n)
+        traffic = (traffic_rec["uniform_dram_bytes_per_update"] * uniform +
+                   traffic_rec["active_dram_bytes_per_update"] * (updates - uniform)) / launches
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if peak else None, "traffic": traffic,
                 "peak_source": peak_src, "kernel": "k_pcdm_update",
@@ -573,7 +608,9 @@ def main():
     args = parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    w = dict(WORKLOADS[args.workload])
+    w = dict(WORKLOADS[args.workload], name=args.workload)
+    if args.probe_launches:
+        return probe_launches(w)
     if args.max_epochs > 0:
         w["max_epochs"] = args.max_epochs
     if args.impl == "reference":
