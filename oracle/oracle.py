@@ -70,6 +70,14 @@ def lib():
         L.orc_svm_hogwild.argtypes = [I64, i64p, i32p, f64p, f64p, D, f64p, f64p, f64p, U64, U64,
                                       U64, I]
         L.orc_svm_hogwild.restype = D
+        L.orc_smooth_lipschitz.argtypes = [I, I64, i64p, f64p, D, D, D, f64p]
+        L.orc_smooth_residuals.argtypes = [I, I64, I64, i64p, i32p, f64p, f64p, f64p, f64p]
+        L.orc_smooth_updates.argtypes = [I, I64, i64p, i32p, f64p, f64p, D, f64p, f64p, f64p, U64,
+                                         U64, U64]
+        L.orc_smooth_eval.argtypes = [I, I64, I64, i64p, i32p, f64p, f64p, D, f64p, f64p, f64p]
+        L.orc_smooth_solve.argtypes = [I, I64, I64, i64p, i32p, f64p, f64p, D, D, D, U64, D, I,
+                                       I64, f64p, f64p, f64p]
+        L.orc_smooth_solve.restype = I64
         L.orc_omega.argtypes = [I64, I64, i64p, i32p]
         L.orc_omega.restype = I64
         L.orc_eso_beta.argtypes = [D, D, D]
@@ -87,6 +95,8 @@ def ref_lib():
                                     f64p, f64p]
         R.ref_svm_run.argtypes = [I, I, i32p, i32p, f64p, f64p, D, D, I, U64, I, C.c_ulong, f64p,
                                   f64p, f64p]
+        R.ref_smooth_run.argtypes = [I, I, I, i32p, i32p, f64p, f64p, D, D, I, U64, I, C.c_ulong,
+                                     f64p, f64p, f64p]
         _ref = R
     return _ref
 
@@ -111,6 +121,73 @@ def omega(m, n, col_ptr, row_idx):
 
 def eso_beta(omega_, tau, n):
     return float(lib().orc_eso_beta(omega_, tau, n))
+
+
+RIDGE, LOGISTIC = 1, 3
+
+
+class Smooth:
+    """Serial FP64 restatement of MulticoreL2SquareRegSquareLoss (loss 1) or
+    MulticoreL2SquareRegLogisticLoss (loss 3) driven by the sampler; A is CSC
+    over the coordinates (loss 3: features; rows are samples, b the labels)."""
+
+    def __init__(self, loss, m, n, col_ptr, row_idx, vals, b, lam, beta=1.0, sigma=1.0, x0=None):
+        self.loss, self.m, self.n, self.lam = int(loss), int(m), int(n), float(lam)
+        self.col_ptr = np.ascontiguousarray(col_ptr, np.int64)
+        self.row_idx = np.ascontiguousarray(row_idx, np.int32)
+        self.vals = np.ascontiguousarray(vals, np.float64)
+        self.b = np.ascontiguousarray(b, np.float64)
+        self.x = np.zeros(self.n) if x0 is None else np.array(x0, np.float64)
+        self.r = np.zeros(self.m)
+        self.Li = np.zeros(self.n)
+        lib().orc_smooth_lipschitz(self.loss, self.n, self.col_ptr, self.vals, self.lam,
+                                   float(beta), float(sigma), self.Li)
+        self.refresh()
+        self.k = 0
+
+    def refresh(self):
+        lib().orc_smooth_residuals(self.loss, self.m, self.n, self.col_ptr, self.row_idx,
+                                   self.vals, self.b, self.x, self.r)
+
+    def updates(self, count, seed):
+        lib().orc_smooth_updates(self.loss, self.n, self.col_ptr, self.row_idx, self.vals, self.b,
+                                 self.lam, self.Li, self.x, self.r, seed, self.k, int(count))
+        self.k += int(count)
+
+    def evaluate(self):
+        out = np.zeros(9)
+        lib().orc_smooth_eval(self.loss, self.m, self.n, self.col_ptr, self.row_idx, self.vals,
+                              self.b, self.lam, self.x, self.r, out)
+        return _eval_dict(out)
+
+
+def smooth_solve(loss, m, n, col_ptr, row_idx, vals, b, lam, beta=1.0, sigma=1.0, seed=1,
+                 target=1e-9, rel=True, max_epochs=100000, x0=None):
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64)
+    r = np.zeros(m)
+    out = np.zeros(9)
+    ep = lib().orc_smooth_solve(int(loss), m, n, np.ascontiguousarray(col_ptr, np.int64),
+                                np.ascontiguousarray(row_idx, np.int32),
+                                np.ascontiguousarray(vals, np.float64),
+                                np.ascontiguousarray(b, np.float64), lam, beta, sigma, seed,
+                                target, int(rel), max_epochs, x, r, out)
+    return x, r, _eval_dict(out), int(ep)
+
+
+def ref_smooth(loss, m, n, col_ptr, row_idx, vals, b, lam, sigma, seed, bulks, inner, threads=1):
+    """The reference engine's x, residuals and objective after each bulk (loss 1 or 3)."""
+    R = ref_lib()
+    if R is None:
+        return None
+    x = np.zeros(n)
+    r = np.zeros(m)
+    obj = np.zeros(bulks + 1)
+    rc = R.ref_smooth_run(int(loss), m, n, np.ascontiguousarray(col_ptr, np.int32),
+                          np.ascontiguousarray(row_idx, np.int32),
+                          np.ascontiguousarray(vals, np.float64), np.ascontiguousarray(b, np.float64),
+                          lam, sigma, threads, seed, bulks, inner, x, r, obj)
+    assert rc == 0
+    return x, r, obj
 
 
 class Lasso:

@@ -235,6 +235,186 @@ int64_t orc_lasso_solve_shrink(int64_t m, int64_t n, const int64_t* col_ptr,
   return epochs;
 }
 
+/* ---- L2-regularised square loss (lossFunction 1) and L2-regularised
+ *      logistic loss (lossFunction 3): the "smooth" losses ---- */
+
+/* MulticoreL2SquareRegSquareLoss::computeReciprocalLipConstants
+ * (cpp/src/solver/lossFunctions/squareLoss/MulticoreL2SquareRegSquareLoss.h:30-43):
+ * Li = 1/(lambda + ||a_j||^2), summed from lambda in column order.
+ * MulticoreL2SquareRegLogisticLoss::computeReciprocalLipConstants
+ * (cpp/src/solver/lossFunctions/logisticLoss/MulticoreL2SquareRegLogisticLoss.h:30-44):
+ * Li = 1/(sigma (lambda + ||a_j||^2 / 4)).  beta scales the ||a_j||^2 term of the
+ * square loss (1 reproduces the reference, which applies none there). */
+void orc_smooth_lipschitz(int loss, int64_t n, const int64_t* col_ptr, const double* vals,
+                          double lambda, double beta, double sigma, double* Li) {
+  for (int64_t i = 0; i < n; ++i) {
+    double acc = lambda;
+    if (loss == ORC_LOSS_RIDGE) {
+      if (beta == 1) {
+        for (int64_t j = col_ptr[i]; j < col_ptr[i + 1]; ++j) acc += vals[j] * vals[j];
+      } else {
+        double s = 0;
+        for (int64_t j = col_ptr[i]; j < col_ptr[i + 1]; ++j) s += vals[j] * vals[j];
+        acc = lambda + beta * s;
+      }
+    } else {
+      for (int64_t j = col_ptr[i]; j < col_ptr[i + 1]; ++j) acc += 0.25 * vals[j] * vals[j];
+      acc = acc * sigma;
+    }
+    Li[i] = acc > 0 ? 1 / acc : acc;
+  }
+}
+
+/* Residuals: MulticoreSquareLoss::recomputeResiduals (MulticoreSquareLoss.h:42-53),
+ * r = -b + A x, for loss 1; MulticoreLogisticLoss::recomputeResiduals
+ * (cpp/src/solver/lossFunctions/logisticLoss/MulticoreLogisticLoss.h:42-55),
+ * r_i = -b_i (A x)_i, for loss 3. */
+void orc_smooth_residuals(int loss, int64_t m, int64_t n, const int64_t* col_ptr,
+                          const int32_t* row_idx, const double* vals, const double* b,
+                          const double* x, double* r) {
+  if (loss == ORC_LOSS_RIDGE) {
+    orc_lasso_residuals(m, n, col_ptr, row_idx, vals, b, x, r);
+    return;
+  }
+  for (int64_t i = 0; i < m; ++i) r[i] = 0;
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t j = col_ptr[i]; j < col_ptr[i + 1]; ++j)
+      r[row_idx[j]] += -b[row_idx[j]] * vals[j] * x[i];
+}
+
+/* One serial update: MulticoreL2SquareRegSquareLoss::compute_update and
+ * performOneCoordinateUpdate (MulticoreL2SquareRegSquareLoss.h:56-78), or
+ * MulticoreL2SquareRegLogisticLoss::compute_update and
+ * performOneCoordinateUpdate (MulticoreL2SquareRegLogisticLoss.h:88-115), whose
+ * step is halved. */
+static void smooth_update(int loss, int64_t idx, const int64_t* col_ptr, const int32_t* row_idx,
+                          const double* vals, const double* b, double lambda, const double* Li,
+                          double* x, double* r) {
+  double tmp = 0;
+  if (loss == ORC_LOSS_RIDGE) {
+    for (int64_t j = col_ptr[idx]; j < col_ptr[idx + 1]; ++j) tmp += vals[j] * r[row_idx[j]];
+    tmp += lambda * x[idx];
+    tmp = -Li[idx] * tmp;
+    x[idx] = x[idx] + tmp;
+    for (int64_t j = col_ptr[idx]; j < col_ptr[idx + 1]; ++j)
+      r[row_idx[j]] = r[row_idx[j]] + tmp * vals[j];
+  } else {
+    for (int64_t j = col_ptr[idx]; j < col_ptr[idx + 1]; ++j) {
+      double tt = exp(r[row_idx[j]]);
+      tmp += -b[row_idx[j]] * vals[j] * tt / (1 + tt);
+    }
+    tmp += lambda * x[idx];
+    tmp = -Li[idx] * tmp;
+    tmp = tmp / 2;
+    x[idx] = x[idx] + tmp;
+    for (int64_t j = col_ptr[idx]; j < col_ptr[idx + 1]; ++j)
+      r[row_idx[j]] = r[row_idx[j]] + -b[row_idx[j]] * tmp * vals[j];
+  }
+}
+
+void orc_smooth_updates(int loss, int64_t n, const int64_t* col_ptr, const int32_t* row_idx,
+                        const double* vals, const double* b, double lambda, const double* Li,
+                        double* x, double* r, uint64_t seed, uint64_t k0, uint64_t count) {
+  for (uint64_t k = 0; k < count; ++k) {
+    int64_t idx = (int64_t)orc_sample(seed, k0 + k, (uint64_t)n);
+    smooth_update(loss, idx, col_ptr, row_idx, vals, b, lambda, Li, x, r);
+  }
+}
+
+/* Primal as computeObjectiveValue (MulticoreL2SquareRegSquareLoss.h:45-54:
+ * ||r||^2/2 + lambda ||x||^2/2; MulticoreL2SquareRegLogisticLoss.h:46-86:
+ * sum log(1 + exp(r_i)) + lambda ||x||^2/2, training accuracy = fraction of
+ * r_i < 0).  The duality gaps are this build's (the reference reports none):
+ *   loss 1: P - D = (1/(2 lambda)) sum_j (a_j^T r + lambda x_j)^2 with the
+ *           dual point u = r of D(u) = -||u||^2/2 - b^T u - ||A^T u||^2/(2 lambda);
+ *   loss 3: D(a) = -sum_i [a_i log a_i + (1-a_i) log(1-a_i)]
+ *                  - ||sum_i a_i b_i A_i.||^2/(2 lambda) at a_i = 1/(1+exp(-r_i)).
+ * out: [0] P [1] D [2] gap [3] rel_gap [4] accuracy (loss 3) [5] ||x||^2
+ *      [6] ||r||^2 (loss 1) or sum log(1+exp(r)) (loss 3) [7] 0 [8] support. */
+static double sigmoid(double z) {
+  if (z >= 0) return 1 / (1 + exp(-z));
+  double e = exp(z);
+  return e / (1 + e);
+}
+
+static double neg_entropy(double a) {
+  double s = 0;
+  if (a > 0) s += a * log(a);
+  if (a < 1) s += (1 - a) * log1p(-a);
+  return s;
+}
+
+void orc_smooth_eval(int loss, int64_t m, int64_t n, const int64_t* col_ptr,
+                     const int32_t* row_idx, const double* vals, const double* b, double lambda,
+                     const double* x, const double* r, double* out) {
+  double xx = 0, rows = 0, ent = 0, good = 0, cols = 0;
+  int64_t support = 0;
+  double* alpha = NULL;
+  if (loss == ORC_LOSS_LOGISTIC) alpha = (double*)malloc(sizeof(double) * (size_t)(m > 0 ? m : 1));
+  for (int64_t i = 0; i < m; ++i) {
+    if (loss == ORC_LOSS_RIDGE) {
+      rows += r[i] * r[i];
+    } else {
+      rows += r[i] > 0 ? r[i] + log1p(exp(-r[i])) : log1p(exp(r[i]));
+      alpha[i] = sigmoid(r[i]);
+      ent += neg_entropy(alpha[i]);
+      good += r[i] < 0;
+    }
+  }
+  for (int64_t j = 0; j < n; ++j) {
+    double g = 0;
+    if (loss == ORC_LOSS_RIDGE) {
+      for (int64_t e = col_ptr[j]; e < col_ptr[j + 1]; ++e) g += vals[e] * r[row_idx[e]];
+      g += lambda * x[j];
+    } else {
+      for (int64_t e = col_ptr[j]; e < col_ptr[j + 1]; ++e)
+        g += b[row_idx[e]] * vals[e] * alpha[row_idx[e]];
+    }
+    cols += g * g;
+    xx += x[j] * x[j];
+    support += x[j] != 0;
+  }
+  double P, D;
+  if (loss == ORC_LOSS_RIDGE) {
+    P = 0.5 * rows + 0.5 * lambda * xx;
+    D = P - cols / (2 * lambda);
+  } else {
+    P = rows + 0.5 * lambda * xx;
+    D = -ent - cols / (2 * lambda);
+  }
+  free(alpha);
+  out[0] = P;
+  out[1] = D;
+  out[2] = P - D;
+  out[3] = (P - D) / (fabs(P) > 1 ? fabs(P) : 1);
+  out[4] = loss == ORC_LOSS_LOGISTIC && m > 0 ? good / (double)m : 0;
+  out[5] = xx;
+  out[6] = rows;
+  out[7] = 0;
+  out[8] = (double)support;
+}
+
+int64_t orc_smooth_solve(int loss, int64_t m, int64_t n, const int64_t* col_ptr,
+                         const int32_t* row_idx, const double* vals, const double* b,
+                         double lambda, double beta, double sigma, uint64_t seed, double target,
+                         int rel, int64_t max_epochs, double* x, double* r, double* out) {
+  double* Li = (double*)malloc(sizeof(double) * (size_t)n);
+  orc_smooth_lipschitz(loss, n, col_ptr, vals, lambda, beta, sigma, Li);
+  orc_smooth_residuals(loss, m, n, col_ptr, row_idx, vals, b, x, r);
+  orc_smooth_eval(loss, m, n, col_ptr, row_idx, vals, b, lambda, x, r, out);
+  int64_t epochs = 0;
+  uint64_t k = 0;
+  while ((rel ? out[3] : out[2]) > target && epochs < max_epochs) {
+    orc_smooth_updates(loss, n, col_ptr, row_idx, vals, b, lambda, Li, x, r, seed, k, (uint64_t)n);
+    k += (uint64_t)n;
+    epochs += 1;
+    orc_smooth_residuals(loss, m, n, col_ptr, row_idx, vals, b, x, r);
+    orc_smooth_eval(loss, m, n, col_ptr, row_idx, vals, b, lambda, x, r, out);
+  }
+  free(Li);
+  return epochs;
+}
+
 /* ---- SVM dual ---- */
 
 /* MulticoreSVMDualLoss::computeReciprocalLipConstants (MulticoreSVMDualLoss.h:48-61). */

@@ -66,6 +66,26 @@ int64_t orc_lasso_solve_shrink(int64_t m, int64_t n, const int64_t* col_ptr,
                                int64_t start_epoch, double step_scale, double* x, double* r,
                                double* out, double* gap_trace);
 
+/* ---- losses 1 (L2-regularised square) and 3 (L2-regularised logistic); the
+ *      matrix is CSC over coordinates, m = residual entries (samples for 3) ---- */
+#define ORC_LOSS_RIDGE 1
+#define ORC_LOSS_LOGISTIC 3
+void orc_smooth_lipschitz(int loss, int64_t n, const int64_t* col_ptr, const double* vals,
+                          double lambda, double beta, double sigma, double* Li);
+void orc_smooth_residuals(int loss, int64_t m, int64_t n, const int64_t* col_ptr,
+                          const int32_t* row_idx, const double* vals, const double* b,
+                          const double* x, double* r);
+void orc_smooth_updates(int loss, int64_t n, const int64_t* col_ptr, const int32_t* row_idx,
+                        const double* vals, const double* b, double lambda, const double* Li,
+                        double* x, double* r, uint64_t seed, uint64_t k0, uint64_t count);
+void orc_smooth_eval(int loss, int64_t m, int64_t n, const int64_t* col_ptr,
+                     const int32_t* row_idx, const double* vals, const double* b, double lambda,
+                     const double* x, const double* r, double* out);
+int64_t orc_smooth_solve(int loss, int64_t m, int64_t n, const int64_t* col_ptr,
+                         const int32_t* row_idx, const double* vals, const double* b,
+                         double lambda, double beta, double sigma, uint64_t seed, double target,
+                         int rel, int64_t max_epochs, double* x, double* r, double* out);
+
 /* ---- SVM dual (loss 2); the matrix is CSR by sample, m = features ---- */
 void orc_svm_lipschitz(int64_t n, const int64_t* row_ptr, const double* vals, double sigma,
                        double* Li);

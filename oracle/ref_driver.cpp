@@ -1,6 +1,6 @@
 /*
  * ref_driver.cpp - runs the reference's own multicore engine
- * (MulticoreEngineExecutor + MulticoreL1RegSquareLoss / MulticoreSVMDualLoss,
+ * (MulticoreEngineExecutor with the loss plugins of lossFunction 0-3,
  * compiled from the reference sources with the GSL shim) on arrays passed in,
  * so tests can pin the oracle against the reference itself.
  *
@@ -96,5 +96,44 @@ extern "C" int ref_svm_run(int d, int n, const int* row_ptr, const int* col_idx,
   }
   for (int i = 0; i < n; ++i) alpha_out[i] = loss->instance.x[i];
   for (int i = 0; i < d; ++i) w_out[i] = loss->residuals[i];
+  return 0;
+}
+
+/* Losses 1 (MulticoreL2SquareRegSquareLoss) and 3 (MulticoreL2SquareRegLogisticLoss)
+ * through the same engine (MulticoreEngineExecutor.h:32-58).  A is CSC over the
+ * coordinates (for loss 3 the features, rows = samples, b = labels); sigma is
+ * instance.sigma, which loss 3's Lipschitz constants use.  The logistic
+ * objective walks A_test_csr_row_ptr.size() - 1 test rows, so that vector gets
+ * one entry (no test set). */
+extern "C" int ref_smooth_run(int loss, int m, int n, const int* col_ptr, const int* row_idx,
+                              const double* vals, const double* b, double lambda, double sigma,
+                              int threads, uint64_t seed, int bulks, unsigned long inner,
+                              double* x_out, double* r_out, double* obj_out) {
+  if (loss != 1 && loss != 3) return -1;
+  OptimizationSettings settings;
+  settings.lossFunction = loss;
+  settings.totalThreads = threads;
+  settings.innerIterations = inner;
+  settings.verbose = false;
+  ProblemData<int, double> inst;
+  const int nnz = col_ptr[n];
+  inst.A_csc_col_ptr.assign(col_ptr, col_ptr + n + 1);
+  inst.A_csc_row_idx.assign(row_idx, row_idx + nnz);
+  inst.A_csc_values.assign(vals, vals + nnz);
+  inst.b.assign(b, b + m);
+  inst.A_test_csr_row_ptr.assign(1, 0);
+  inst.m = m;
+  inst.n = n;
+  inst.lambda = lambda;
+  inst.sigma = sigma;
+  MulticoreEngineExecutor<int, double> executor(inst, &settings);
+  reset_sampler(seed);
+  obj_out[0] = executor.getObjectiveValue();
+  for (int k = 0; k < bulks; ++k) {
+    executor.executeBulkOfIterations();
+    obj_out[k + 1] = executor.getObjectiveValue();
+  }
+  for (int i = 0; i < n; ++i) x_out[i] = inst.x[i];
+  for (int i = 0; i < m; ++i) r_out[i] = executor.residuals[i];
   return 0;
 }

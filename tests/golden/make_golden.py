@@ -9,6 +9,12 @@ Fixtures (all inputs are stored, so no generator has to reproduce them):
   lasso_traj.npz   small Lasso: inputs + the reference engine's x, residuals and
                    objective after each of 6 bulks (one thread, seeded sampler)
   svm_traj.npz     small SVM dual: inputs + alpha, w and (gap, P, D, 0-1) per bulk
+  ridge_traj.npz   small L2-regularised square loss (lossFunction 1): inputs + x,
+                   residuals and objective per bulk
+  logistic_traj.npz
+                   small L2-regularised logistic loss (lossFunction 3), samples as
+                   rows and features as coordinates: inputs + x, residuals and
+                   objective per bulk
   lasso_config0.json
                    the 2,000 x 10,000 config-0 instance, identified by the SHA-256
                    of its generated arrays, with the reference engine's solution
@@ -66,6 +72,33 @@ def main(ref_root=None):
     np.savez_compressed(os.path.join(HERE, "svm_traj.npz"), d=sv.m, n=sv.n, row_ptr=sv.col_ptr,
                         col_idx=sv.row_idx, vals=sv.vals, y=sv.rhs, lam=sv.lam, sigma=sigma,
                         seed=seed, bulks=bulks, inner=inner, alpha=a, w=w, evals=ev)
+
+    # small L2-regularised square loss (lossFunction 1) trajectory
+    rd = acdc.gen_lasso(250, 900, nnz_per_col=7, n_star=25, noise_sigma=0.01, lambda_frac=0.1,
+                        seed=15)
+    seed, bulks, inner, lam = 4242, 5, 600, 0.3
+    x, r, obj = oracle.ref_smooth(1, rd.m, rd.n, rd.col_ptr.astype(np.int32), rd.row_idx, rd.vals,
+                                  rd.rhs, lam, 1.0, seed, bulks, inner)
+    np.savez_compressed(os.path.join(HERE, "ridge_traj.npz"), m=rd.m, n=rd.n, col_ptr=rd.col_ptr,
+                        row_idx=rd.row_idx, vals=rd.vals, b=rd.rhs, lam=lam, seed=seed,
+                        bulks=bulks, inner=inner, x=x, r=r, obj=obj)
+
+    # small L2-regularised logistic loss (lossFunction 3) trajectory: samples of the
+    # SVM generator as rows, features as coordinates (CSC over features), the
+    # engine's sigma taken above 1
+    lg = acdc.gen_svm(350, 800, nnz_median=18, nnz_sigma=0.6, w_star_nnz=60, lam=1e-3, seed=17)
+    import scipy.sparse as sp
+    X = sp.csr_matrix((lg.vals, lg.row_idx, lg.col_ptr), shape=(lg.n, lg.m)).tocsc()
+    X.sort_indices()
+    cp = X.indptr.astype(np.int64)
+    ri = X.indices.astype(np.int32)
+    va = X.data.astype(np.float64)
+    seed, bulks, inner, lam, sigma = 9191, 5, 800, 1e-2, 1.5
+    x, r, obj = oracle.ref_smooth(3, X.shape[0], X.shape[1], cp.astype(np.int32), ri, va, lg.rhs,
+                                  lam, sigma, seed, bulks, inner)
+    np.savez_compressed(os.path.join(HERE, "logistic_traj.npz"), m=X.shape[0], n=X.shape[1],
+                        col_ptr=cp, row_idx=ri, vals=va, b=lg.rhs, lam=lam, sigma=sigma, seed=seed,
+                        bulks=bulks, inner=inner, x=x, r=r, obj=obj)
 
     # config 0: the reference engine run epoch by epoch until the FP64 gap <= 1e-9
     c0 = acdc.gen_lasso(CONFIG0["m"], CONFIG0["n"], nnz_per_col=CONFIG0["nnz_per_col"],

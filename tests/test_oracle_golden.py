@@ -160,3 +160,64 @@ def test_hogwild_single_thread_is_the_serial_trajectory():
     A.updates(5000, 4)
     B.hogwild(5000, 4, threads=1)
     assert np.array_equal(A.x, B.x) and np.array_equal(A.r, B.r)
+
+
+@pytest.mark.parametrize("name,loss", [("ridge_traj.npz", oracle.RIDGE),
+                                       ("logistic_traj.npz", oracle.LOGISTIC)])
+def test_smooth_loss_trajectories_match_reference_engine_bit_for_bit(name, loss):
+    """Losses 1 (MulticoreL2SquareRegSquareLoss) and 3 (MulticoreL2SquareRegLogisticLoss):
+    x and the residuals after each bulk equal the reference engine's exactly."""
+    g = load(name)
+    sigma = float(g["sigma"]) if "sigma" in g.files else 1.0
+    S = oracle.Smooth(loss, int(g["m"]), int(g["n"]), g["col_ptr"], g["row_idx"], g["vals"],
+                      g["b"], float(g["lam"]), sigma=sigma)
+    objs = [S.evaluate()["primal"]]
+    for _ in range(int(g["bulks"])):
+        S.updates(int(g["inner"]), int(g["seed"]))
+        objs.append(S.evaluate()["primal"])
+    assert np.array_equal(S.x, g["x"])
+    assert np.array_equal(S.r, g["r"])
+    # the reference squares a norm of x (and of r for loss 1); the oracle sums squares
+    np.testing.assert_allclose(objs, g["obj"], rtol=1e-12)
+
+
+@ref_needed
+@pytest.mark.parametrize("loss", [oracle.RIDGE, oracle.LOGISTIC])
+def test_smooth_oracle_equals_reference_engine_on_random_cases(loss):
+    inst = acdc.gen_lasso(120, 400, nnz_per_col=5, n_star=10, lambda_frac=0.1, seed=31 + loss)
+    b = inst.rhs if loss == oracle.RIDGE else np.where(np.arange(inst.m) % 3, 1.0, -1.0)
+    lam, sigma = (0.2, 1.0) if loss == oracle.RIDGE else (0.05, 2.5)
+    cp = inst.col_ptr.copy()
+    # an empty column and a dense one
+    rows = [list(inst.row_idx[cp[j]:cp[j + 1]]) for j in range(inst.n)]
+    vals = [list(inst.vals[cp[j]:cp[j + 1]]) for j in range(inst.n)]
+    rows[3], vals[3] = [], []
+    rows[4] = list(range(inst.m))
+    vals[4] = list(np.linspace(-1, 1, inst.m) / np.sqrt(inst.m))
+    cp = np.concatenate([[0], np.cumsum([len(r) for r in rows])]).astype(np.int64)
+    ri = np.array([i for r in rows for i in r], np.int32)
+    va = np.array([v for vv in vals for v in vv])
+    x, r, obj = oracle.ref_smooth(loss, inst.m, inst.n, cp.astype(np.int32), ri, va, b, lam, sigma,
+                                  17, 3, 2 * inst.n)
+    S = oracle.Smooth(loss, inst.m, inst.n, cp, ri, va, b, lam, sigma=sigma)
+    for _ in range(3):
+        S.updates(2 * inst.n, 17)
+    assert np.array_equal(x, S.x) and np.array_equal(r, S.r)
+
+
+@pytest.mark.parametrize("loss", [oracle.RIDGE, oracle.LOGISTIC])
+def test_smooth_duality_gaps_close_at_the_optimum(loss):
+    """The duality gaps this build defines for losses 1 and 3 are nonnegative
+    along the way and reach 1e-10 relative at the optimum."""
+    inst = acdc.gen_lasso(200, 500, nnz_per_col=6, n_star=15, lambda_frac=0.1, seed=41)
+    b = inst.rhs if loss == oracle.RIDGE else np.sign(inst.rhs + 1e-12)
+    lam = 0.3 if loss == oracle.RIDGE else 0.02
+    S = oracle.Smooth(loss, inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals, b, lam)
+    for _ in range(3):
+        S.updates(inst.n, 3)
+        S.refresh()
+        ev = S.evaluate()
+        assert ev["gap"] >= -1e-12 * abs(ev["primal"])
+    x, r, ev, ep = oracle.smooth_solve(loss, inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals,
+                                       b, lam, target=1e-10, max_epochs=20000)
+    assert ev["rel_gap"] <= 1e-10 and abs(ev["primal"] - ev["dual"]) <= 1e-9 * abs(ev["primal"])
