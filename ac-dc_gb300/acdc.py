@@ -267,6 +267,27 @@ def gen_nesterov(m, n, p, n_nonzero, lam=1.0, rho=1.0, seed=1):
                     f_star=f.value)
 
 
+def transpose_compressed(rows, cols, ptr, idx, vals):
+    """Compressed rows (rows x cols) -> compressed columns of the same matrix:
+    (col_ptr[cols + 1], row_idx, vals), entries of each column in row order."""
+    ptr = np.asarray(ptr, np.int64)
+    idx = np.asarray(idx, np.int64)
+    row_of = np.repeat(np.arange(rows, dtype=np.int64), np.diff(ptr))
+    order = np.lexsort((row_of, idx))
+    col_ptr = np.zeros(cols + 1, np.int64)
+    np.cumsum(np.bincount(idx, minlength=cols), out=col_ptr[1:])
+    return col_ptr, row_of[order].astype(np.int32), np.asarray(vals, np.float64)[order]
+
+
+def logistic_from_svm(sv, lam):
+    """An L2-regularised logistic instance (loss 3) from an SVM-generator one:
+    samples become the rows and features the coordinates (CSC over features),
+    labels the right-hand side, as the reference's MultiCoreSolver.cpp:80-105
+    arranges LIBSVM data for this loss."""
+    cp, ri, va = transpose_compressed(sv.n, sv.m, sv.col_ptr, sv.row_idx, sv.vals)
+    return Instance(LOSS_LOGISTIC, sv.n, sv.m, cp, ri, va, np.array(sv.rhs, np.float64), lam)
+
+
 def mix_sizes(seed, index, m_lo=500, m_hi=50000, n_lo=1000, n_hi=200000):
     m, n = I64(0), I64(0)
     _check_host(host_lib().acdc_gen_mix_sizes(seed, index, m_lo, m_hi, n_lo, n_hi, C.byref(m),

@@ -1,8 +1,8 @@
 // acdc_solver: the console solver of the reference's
 // cpp/src/frontends/solvers/MultiCoreSolver.cpp:18-115 on the GPU engine.
 //
-// Same flags and flow: -A matrix (CSC text prefix for -f 0, LIBSVM file for
-// -f 2), -b vector file (-f 0), -l lambda, -t threads (tau), -f loss, -I inner
+// Same flags and flow: -A matrix (CSC text prefix for -f 0 and 1, LIBSVM file
+// for -f 2 and 3), -b vector file (-f 0, 1), -l lambda, -t threads (tau), -f loss, -I inner
 // iterations per bulk, -i show objectives; omega is the largest number of
 // entries in one residual row and sigma = 1 + (omega-1)(tau-1)/(n-1); the
 // Solver driver runs the bulks.  Flags the reference lacks:
@@ -31,14 +31,14 @@
 namespace {
 
 void usage() {
-  std::cout << "usage: acdc_solver -A <matrix> [-b <vector>] -l <lambda> [-t tau] [-f 0|2]\n"
+  std::cout << "usage: acdc_solver -A <matrix> [-b <vector>] -l <lambda> [-t tau] [-f 0|1|2|3]\n"
                "                   [-I inner] [-B bulks] [-i 0|1] [-d device] [-s seed]\n"
                "                   [-G gap] [-S q]\n";
 }
 
 bool load(int loss, const std::string& a, const std::string& b, double lambda,
           ProblemData<int, double>& inst) {
-  if (loss == 0) {
+  if (loss == 0 || loss == 1) {
     int64_t m = 0, n = 0, nnz = 0;
     if (acdc_load_csc_text_sizes(a.c_str(), b.c_str(), &m, &n, &nnz) != ACDC_OK) return false;
     std::vector<int64_t> cp((size_t)n + 1);
@@ -66,6 +66,25 @@ bool load(int loss, const std::string& a, const std::string& b, double lambda,
     inst.A_csr_col_idx.assign(ci.begin(), ci.end());
     inst.m = (int)d;
     inst.n = (int)n;
+    if (loss == 3) {
+      // MultiCoreSolver.cpp:80-105: the samples become the rows of a CSC matrix
+      // over the features (m = samples, n = features).
+      std::vector<int> cnt((size_t)d + 1, 0);
+      for (int64_t e = 0; e < nnz; ++e) cnt[(size_t)ci[(size_t)e] + 1]++;
+      for (int64_t f = 0; f < d; ++f) cnt[(size_t)f + 1] += cnt[(size_t)f];
+      inst.A_csc_col_ptr.assign(cnt.begin(), cnt.end());
+      inst.A_csc_row_idx.assign((size_t)nnz, 0);
+      inst.A_csc_values.assign((size_t)nnz, 0.0);
+      std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+      for (int64_t i = 0; i < n; ++i)
+        for (int64_t e = rp[(size_t)i]; e < rp[(size_t)i + 1]; ++e) {
+          const int f = ci[(size_t)e];
+          inst.A_csc_row_idx[(size_t)fill[(size_t)f]] = (int)i;
+          inst.A_csc_values[(size_t)fill[(size_t)f]++] = inst.A_csr_values[(size_t)e];
+        }
+      inst.m = (int)n;
+      inst.n = (int)d;
+    }
   }
   inst.lambda = lambda;
   return true;
@@ -102,7 +121,9 @@ int main(int argc, char* argv[]) {
       default: break;  // -x -y -z -r -e -c -T: accepted for compatibility
     }
   }
-  if (matrix.empty() || (settings.lossFunction == 0 && vector_file.empty()) || !(lambda > 0)) {
+  const int loss = settings.lossFunction;
+  if (matrix.empty() || ((loss == 0 || loss == 1) && vector_file.empty()) || !(lambda > 0) ||
+      loss < 0 || loss > 3) {
     usage();
     return 2;
   }
@@ -112,9 +133,10 @@ int main(int argc, char* argv[]) {
     return 1;
   }
   std::cout << "Data loaded with size: " << instance.m << " x " << instance.n << std::endl;
-  // omega = largest number of entries in one residual row (MultiCoreSolver.cpp:32-38, 55-62)
+  // omega = largest number of entries in one residual row (MultiCoreSolver.cpp:32-38, 55-62;
+  // for -f 3 the longest sample, :98-103)
   const std::vector<int>& idx =
-      settings.lossFunction == 0 ? instance.A_csc_row_idx : instance.A_csr_col_idx;
+      settings.lossFunction == 2 ? instance.A_csr_col_idx : instance.A_csc_row_idx;
   std::vector<int> rows((size_t)instance.m, 0);
   double omega = 1;
   for (int r : idx)

@@ -59,16 +59,16 @@ class CudaEngineExecutor : public AbstractEngineExecutor<L, D> {
       : instance(inst), opt_(opt) {
     this->settings = s;
     loss_ = s->lossFunction;
-    if (loss_ == ACDC_LOSS_L2_SQUARE || loss_ == ACDC_LOSS_LOGISTIC)
-      throw std::runtime_error("lossFunction " + std::to_string(loss_) +
-                               " is not served by the GPU engine (0 and 2 are)");
-    if (loss_ != ACDC_LOSS_L1_SQUARE && loss_ != ACDC_LOSS_SVM_DUAL)
+    if (loss_ < ACDC_LOSS_L1_SQUARE || loss_ > ACDC_LOSS_LOGISTIC)
       throw std::runtime_error("unknown lossFunction " + std::to_string(loss_));
     check(acdc_ctx_create(opt.device, &ctx_), "acdc_ctx_create");
-    const bool lasso = loss_ == ACDC_LOSS_L1_SQUARE;
-    const std::vector<L>& ptr = lasso ? inst.A_csc_col_ptr : inst.A_csr_row_ptr;
-    const std::vector<L>& idx = lasso ? inst.A_csc_row_idx : inst.A_csr_col_idx;
-    const std::vector<D>& val = lasso ? inst.A_csc_values : inst.A_csr_values;
+    // Losses 0, 1 and 3 read the CSC arrays (for 3 after MultiCoreSolver.cpp:80-105
+    // turned the samples into rows), the SVM dual the CSR by sample
+    // (MulticoreEngineExecutor.h:32-58).
+    const bool csc = loss_ != ACDC_LOSS_SVM_DUAL;
+    const std::vector<L>& ptr = csc ? inst.A_csc_col_ptr : inst.A_csr_row_ptr;
+    const std::vector<L>& idx = csc ? inst.A_csc_row_idx : inst.A_csr_col_idx;
+    const std::vector<D>& val = csc ? inst.A_csc_values : inst.A_csr_values;
     const int64_t n = (int64_t)inst.n;
     if ((int64_t)ptr.size() != n + 1) throw std::runtime_error("column pointers do not match n");
     std::vector<int64_t> cp(ptr.begin(), ptr.end());
@@ -85,9 +85,14 @@ class CudaEngineExecutor : public AbstractEngineExecutor<L, D> {
     st.tau = s->totalThreads > 0 ? s->totalThreads : 1;
     st.warps_per_block = opt.warps_per_block;
     st.seed = opt.seed;
-    st.sigma = s->forcedSigma > 0 ? s->forcedSigma : (lasso ? 0.0 : (double)inst.sigma);
+    // The SVM dual and the logistic loss take the engine's sigma into their
+    // Lipschitz constants (MulticoreSVMDualLoss.h:48-61,
+    // MulticoreL2SquareRegLogisticLoss.h:30-44); losses 0 and 1 let the library
+    // choose the ESO beta for tau.
+    const bool uses_sigma = loss_ == ACDC_LOSS_SVM_DUAL || loss_ == ACDC_LOSS_LOGISTIC;
+    st.sigma = s->forcedSigma > 0 ? s->forcedSigma : (uses_sigma ? (double)inst.sigma : 0.0);
     st.gap_target = opt.gap_target;
-    st.gap_relative = lasso ? 1 : 0;
+    st.gap_relative = loss_ == ACDC_LOSS_SVM_DUAL ? 0 : 1;
     st.max_epochs = opt.max_epochs;
     st.refresh_every = opt.refresh_every;
     st.use_shrinking = s->use_shrinking ? 1 : 0;
@@ -132,6 +137,9 @@ class CudaEngineExecutor : public AbstractEngineExecutor<L, D> {
     if (loss_ == ACDC_LOSS_SVM_DUAL)
       return "Elapsed iterations, Current duality gap, Primal objective, Dual objective, 0-1 loss, "
              "Pure computation time, Total time, Test 0-1";
+    if (loss_ == ACDC_LOSS_LOGISTIC)  // LogisticLoss.h:30-40
+      return "Elapsed iterations, Current objective value, Pure computation time, Total time, "
+             "Train 0-1 loss, Test 0-1 loss";
     return "Elapsed iterations, Current objective value, Pure computation time, Total time";
   }
 
@@ -144,6 +152,7 @@ class CudaEngineExecutor : public AbstractEngineExecutor<L, D> {
     } else {
       ss << statistics.elapsedIterations << "," << std::setprecision(16) << last_.primal << ","
          << statistics.elapsedPureComputationTime << "," << statistics.elapsed_time;
+      if (loss_ == ACDC_LOSS_LOGISTIC) ss << "," << last_.zero_one_accuracy << "," << 0;
     }
     return ss.str();
   }

@@ -123,6 +123,9 @@ struct EvalParams {
   uint8_t* row_flag = nullptr;  // m bytes, zero between evaluations
   int32_t* rowcnt = nullptr;
   double hot_frac = 0;
+  // Logistic loss: sigma(r_i) per row, written by the refresh pass for the
+  // column pass of the duality gap.
+  double* roww = nullptr;
 };
 
 // ---- batched solves: many problems ("slots") served by one launch per kernel ----
@@ -251,14 +254,15 @@ cudaError_t launch_layout_scan(const int64_t* col_ptr, int64_t n, int64_t* scrat
                                unsigned long long* counters, cudaStream_t st);
 cudaError_t launch_layout_fill(const int64_t* col_ptr, const int32_t* row_idx,
                                const double* vals64, int64_t m, int64_t n, int64_t* scratch,
-                               DevProblem& d, cudaStream_t st);
+                               DevProblem& d, int32_t loss, cudaStream_t st);
 cudaError_t launch_row_counts(const int32_t* idx, int64_t nnz, int32_t* counts, int64_t m,
                               unsigned long long* counters, cudaStream_t st);
 cudaError_t launch_max_i32(const int32_t* v, int64_t len, unsigned long long* out_slot,
                            cudaStream_t st);
 cudaError_t launch_widen_i32(const int32_t* src, int64_t* dst, int64_t len, cudaStream_t st);
-cudaError_t launch_set_li(const DevProblem& d, int32_t loss, double beta, cudaStream_t st);
-// x: host-order doubles in d.xbuf <-> FP32 meta.w (and FP64 x64 when fp64).
+cudaError_t launch_set_li(const DevProblem& d, int32_t loss, double beta, double lambda,
+                          cudaStream_t st);
+// x: host-order doubles in d.xbuf <-> x32 (and FP64 x64 when fp64).
 cudaError_t launch_set_x(const DevProblem& d, bool fp64, cudaStream_t st);
 cudaError_t launch_get_x(const DevProblem& d, bool fp64, cudaStream_t st);
 // Polish-mode transitions: x64 = (double) meta.w, or meta.w = (float) x64.

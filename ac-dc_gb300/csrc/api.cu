@@ -178,6 +178,7 @@ EvalParams eval_params(acdc_problem* p, bool build_active) {
   e.long_cols = p->d.long_cols;
   e.n_long = p->d.n_long;
   if (build_active && p->loss == ACDC_LOSS_L1_SQUARE) e.r_ref = p->d.r_ref;
+  if (p->loss == ACDC_LOSS_LOGISTIC) e.roww = p->d.r_ref;
   e.col_norm_max = p->col_norm_max;
   if (build_active && hot_enabled(p)) {
     e.viol = p->d.viol;
@@ -258,13 +259,15 @@ int apply_settings(acdc_problem* p, const acdc_settings* s) {
       !(s->hot_threshold >= 0))
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid settings value");
   p->s = *s;
+  // q-shrinking and its screened evaluations cover losses 0 and 2 only.
+  if (p->loss == ACDC_LOSS_L2_SQUARE || p->loss == ACDC_LOSS_LOGISTIC) p->s.use_shrinking = 0;
   p->screen_valid = false;
   const double n = (double)p->d.n;
   if (s->sigma > 0)
     p->beta = s->sigma;
   else
     p->beta = n > 1 ? 1.0 + ((double)p->omega - 1.0) * ((double)s->tau - 1.0) / (n - 1.0) : 1.0;
-  ACDC_CK(ctx, launch_set_li(p->d, p->loss, p->beta, ctx->stream));
+  ACDC_CK(ctx, launch_set_li(p->d, p->loss, p->beta, p->lambda, ctx->stream));
   return ACDC_OK;
 }
 
@@ -273,9 +276,7 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
                 const double* rhs, double lambda, acdc_problem** out) {
   if (!ctx || !out) return ACDC_EINVAL;
   *out = nullptr;
-  if (loss == ACDC_LOSS_L2_SQUARE || loss == ACDC_LOSS_LOGISTIC)
-    return acdc_set_error(ctx, ACDC_EUNSUPPORTED, "loss 1 and 3 are not on this path");
-  if (loss != ACDC_LOSS_L1_SQUARE && loss != ACDC_LOSS_SVM_DUAL)
+  if (loss < ACDC_LOSS_L1_SQUARE || loss > ACDC_LOSS_LOGISTIC)
     return acdc_set_error(ctx, ACDC_EINVAL, "unknown loss code");
   if (m <= 0 || n <= 0 || m > INT32_MAX || n > INT32_MAX || !(lambda > 0) || !rhs ||
       (!col_ptr64 && !col_ptr32))
@@ -353,7 +354,7 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
   if (units < 0 || units >= ((int64_t)1 << 32))
     return fail(acdc_set_error(ctx, ACDC_EINVAL, "matrix too large for 32-bit column starts"));
   d.nnz_pad = units * 4;
-  const int64_t rhs_len = loss == ACDC_LOSS_L1_SQUARE ? m : n;
+  const int64_t rhs_len = loss == ACDC_LOSS_SVM_DUAL ? n : m;
   STEP(dalloc(&d.meta, n, &d.bytes));
   STEP(dalloc(&d.x32, n, &d.bytes));
   STEP(cudaMemsetAsync(d.x32, 0, sizeof(float) * n, st));
@@ -367,6 +368,7 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
   STEP(dalloc(&d.xbuf, n, &d.bytes));
   STEP(dalloc(&d.x64, n, &d.bytes));
   STEP(dalloc(&d.rowcnt, m, &d.bytes));
+  if (loss == ACDC_LOSS_LOGISTIC) STEP(dalloc(&d.r_ref, m, &d.bytes));  // row weights
   if (loss == ACDC_LOSS_L1_SQUARE) {
     STEP(dalloc(&d.r_ref, m, &d.bytes));
     STEP(dalloc(&d.viol, n, &d.bytes));
@@ -378,7 +380,7 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
   STEP(dalloc(&d.eval_out, 16, &d.bytes));
   STEP(cudaMemsetAsync(d.part, 0, sizeof(double) * ACDC_RED_BLOCKS * ACDC_NPART, st));
   STEP(cudaMemcpyAsync(d.rhs64, rhs, sizeof(double) * rhs_len, cudaMemcpyHostToDevice, st));
-  STEP(launch_layout_fill(s_colptr, s_rows, s_vals, m, n, s_scratch, d, st));
+  STEP(launch_layout_fill(s_colptr, s_rows, s_vals, m, n, s_scratch, d, loss, st));
   // omega: the largest number of entries in one residual row, counted on the
   // unpadded input (pad entries all point at row 0).
   int32_t* counts = reinterpret_cast<int32_t*>(s_scratch);
@@ -530,6 +532,9 @@ extern "C" int acdc_problem_set_lambda(acdc_problem* p, double lambda) {
   p->lambda = lambda;
   p->active_valid = false;
   p->screen_valid = false;
+  // Losses 1 and 3 carry lambda in their Lipschitz constants.
+  if (p->loss == ACDC_LOSS_L2_SQUARE || p->loss == ACDC_LOSS_LOGISTIC)
+    ACDC_CK(p->ctx, launch_set_li(p->d, p->loss, p->beta, p->lambda, p->ctx->stream));
   // A new lambda starts with the FP32 bulk again (AUTO precision).
   if (p->s.precision == ACDC_PREC_AUTO) return leave_fp64(p);
   return ACDC_OK;

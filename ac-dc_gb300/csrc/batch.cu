@@ -421,9 +421,12 @@ extern "C" int acdc_batch_solve_path(acdc_ctx* ctx, int32_t count, acdc_problem*
       opt->path_len < 1 || opt->refresh_every < 1 || opt->max_epochs < 1 ||
       !(opt->gap_target >= 0))
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid batch arguments");
-  for (int32_t i = 0; i < count; ++i)
+  for (int32_t i = 0; i < count; ++i) {
     if (!problems[i] || problems[i]->ctx != ctx)
       return acdc_set_error(ctx, ACDC_EINVAL, "problem missing or from another context");
+    if (problems[i]->loss != ACDC_LOSS_L1_SQUARE && problems[i]->loss != ACDC_LOSS_SVM_DUAL)
+      return acdc_set_error(ctx, ACDC_EUNSUPPORTED, "batched paths cover losses 0 and 2");
+  }
   for (int64_t i = 0; i < (int64_t)count * opt->path_len; ++i)
     if (!(lambdas[i] > 0)) return acdc_set_error(ctx, ACDC_EINVAL, "lambdas must be positive");
   if (count == 0) return ACDC_OK;

@@ -99,9 +99,11 @@ __global__ void k_scan_apply(const int64_t* col_ptr, int64_t n, const int64_t* t
 
 // One warp per column: copy FP64 values to FP32 and indices into the padded
 // segment, zero the pad, check indices, compute ||a_j||^2 in FP64 and write meta.
+// For the logistic loss the stored value is b_i A_ij (the label folded in, so
+// the update never loads b); ||a_j||^2 is taken from A itself.
 __global__ void k_build_columns(const int64_t* col_ptr, const int32_t* row_idx,
                                 const double* vals64, const int64_t* start4, int64_t m, int64_t n,
-                                DevProblem d) {
+                                DevProblem d, int32_t loss) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < n; j += warps) {
@@ -121,7 +123,7 @@ __global__ void k_build_columns(const int64_t* col_ptr, const int32_t* row_idx,
           r = 0;
           dv = 0;
         }
-        v = (float)dv;
+        v = (float)(loss == ACDC_LOSS_LOGISTIC ? d.rhs64[r] * dv : dv);
         sq += dv * dv;
       }
       d.vals[dst + e] = v;
@@ -156,14 +158,24 @@ __global__ void k_max_i32(const int32_t* v, int64_t len, unsigned long long* out
 
 // Li = 1/(beta ||a_j||^2) (0 for an empty column); the SVM stores y_j Li.
 // Li of every column, and the largest ||a_j||^2 (CNT_COLSQ_BITS; non-negative
-// doubles order like their bit patterns).
-__global__ void k_set_li(DevProblem d, int32_t loss, double beta) {
+// doubles order like their bit patterns):
+//   losses 0, 2: 1/(beta ||a_j||^2)              (0 for an empty column)
+//   loss 1:      1/(lambda + beta ||a_j||^2)     (MulticoreL2SquareRegSquareLoss.h:30-43)
+//   loss 3:      1/(beta (lambda + ||a_j||^2/4)) (MulticoreL2SquareRegLogisticLoss.h:30-44,
+//                with the engine's sigma = beta)
+__global__ void k_set_li(DevProblem d, int32_t loss, double beta, double lambda) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   double sq_max = 0;
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < d.n; j += stride) {
     double sq = d.col_sq[j];
     sq_max = fmax(sq_max, sq);
-    double li = sq > 0 ? 1.0 / (beta * sq) : 0.0;
+    double li;
+    if (loss == ACDC_LOSS_L2_SQUARE)
+      li = 1.0 / (lambda + beta * sq);
+    else if (loss == ACDC_LOSS_LOGISTIC)
+      li = 1.0 / (beta * (lambda + 0.25 * sq));
+    else
+      li = sq > 0 ? 1.0 / (beta * sq) : 0.0;
     if (loss == ACDC_LOSS_SVM_DUAL && d.rhs64[j] < 0) li = -li;
     d.meta[j].z = __float_as_int((float)li);
   }
@@ -214,12 +226,12 @@ __device__ __forceinline__ double coord(const EvalParams& p, int64_t j) {
 
 // ---- refresh ----
 
-// r64 = -b (Lasso) or 0 (SVM).
+// r64 = -b (losses 0 and 1) or 0 (losses 2 and 3).
 __device__ __forceinline__ void k_refresh_init_body(const EvalParams& p, const int64_t rank,
                                                 const int64_t nb) {
   const int64_t stride = (int64_t)nb * blockDim.x;
   for (int64_t i = (int64_t)rank * blockDim.x + threadIdx.x; i < p.m; i += stride)
-    p.r64[i] = p.loss == ACDC_LOSS_L1_SQUARE ? -p.rhs64[i] : 0.0;
+    p.r64[i] = p.loss == ACDC_LOSS_L1_SQUARE || p.loss == ACDC_LOSS_L2_SQUARE ? -p.rhs64[i] : 0.0;
 }
 
 __global__ void k_refresh_init(EvalParams p) { k_refresh_init_body(p, blockIdx.x, gridDim.x); }
@@ -251,8 +263,9 @@ __device__ __forceinline__ void k_refresh_scatter_body(const EvalParams& p, cons
         }
         if (c != 0.0) coef = c * p.rhs64[j] * inv_ln;
       } else {
-        coef = xv;
-        l1 += fabs(xv);
+        // the logistic residual is r = -(b A) x with b folded into the values
+        coef = p.loss == ACDC_LOSS_LOGISTIC ? -xv : xv;
+        l1 += p.loss == ACDC_LOSS_L1_SQUARE ? fabs(xv) : xv * xv;
         sp += xv != 0.0 ? 1.0 : 0.0;
       }
     }
@@ -284,7 +297,7 @@ __device__ __forceinline__ void k_refresh_scatter_body(const EvalParams& p, cons
       }
     }
   }
-  if (p.loss != ACDC_LOSS_L1_SQUARE) return;
+  if (p.loss == ACDC_LOSS_SVM_DUAL) return;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     l1 += __shfl_down_sync(ACDC_FULL_MASK, l1, o);
@@ -310,7 +323,8 @@ __global__ void k_refresh_scatter(EvalParams p) { k_refresh_scatter_body(p, bloc
 
 // r32 = (float) r64 and the partial sums sum r^2 (slot 0), sum b r (slot 1).
 // With r_ref: a screened evaluation adds sum (r - r_ref)^2 (slot 6); a full one
-// stores r64 into r_ref.
+// stores r64 into r_ref.  The logistic loss sums log(1 + exp(r)) (slot 0), the
+// dual entropy terms (slot 1) and the rows with r < 0 (slot 6) instead.
 __device__ __forceinline__ void k_refresh_finish_body(const EvalParams& p, const int64_t rank,
                                                 const int64_t nb) {
   __shared__ double s0[ACDC_RED_THREADS / 32], s1[ACDC_RED_THREADS / 32],
@@ -320,6 +334,16 @@ __device__ __forceinline__ void k_refresh_finish_body(const EvalParams& p, const
   for (int64_t i = (int64_t)rank * blockDim.x + threadIdx.x; i < p.m; i += stride) {
     double v = p.r64[i];
     p.r32[i] = (float)v;
+    if (p.loss == ACDC_LOSS_LOGISTIC) {
+      // sum log(1 + exp(r)), sum of a log a + (1-a) log(1-a) at a = sigma(r),
+      // count of r < 0 (the training accuracy), and sigma(r) for the column pass
+      a0 += v > 0.0 ? v + log1p(exp(-v)) : log1p(exp(v));
+      const double a = v >= 0.0 ? 1.0 / (1.0 + exp(-v)) : exp(v) / (1.0 + exp(v));
+      a1 += (a > 0.0 ? a * log(a) : 0.0) + (a < 1.0 ? (1.0 - a) * log1p(-a) : 0.0);
+      a2 += v < 0.0 ? 1.0 : 0.0;
+      p.roww[i] = a;
+      continue;
+    }
     a0 += v * v;
     if (p.loss == ACDC_LOSS_L1_SQUARE) a1 += p.rhs64[i] * v;
     if (p.r_ref) {
@@ -580,10 +604,11 @@ __device__ __forceinline__ void k_gap_lasso_long_body(const EvalParams& p, const
 
 __global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_long(EvalParams p) { k_gap_lasso_long_body(p, blockIdx.x, gridDim.x); }
 
-// a_j^T r64 for one column, one warp; every lane gets the sum.  The loads of
+// a_j^T vec for one column, one warp; every lane gets the sum.  The loads of
 // four 128-entry chunks are issued before their gathers, so a long column costs
 // a few memory latencies rather than one per chunk.
-__device__ __forceinline__ double active_dot(const EvalParams& p, const int4 mt, int lane) {
+__device__ __forceinline__ double active_dot(const EvalParams& p, const int4 mt, int lane,
+                                             const double* vec) {
   const int64_t start = (int64_t)(uint32_t)mt.x << 2;
   double g = 0;
   for (int32_t off = 4 * lane; off < mt.y; off += 512) {
@@ -602,10 +627,10 @@ __device__ __forceinline__ double active_dot(const EvalParams& p, const int4 mt,
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      g += (double)v[k].x * p.r64[id[k].x];
-      g += (double)v[k].y * p.r64[id[k].y];
-      g += (double)v[k].z * p.r64[id[k].z];
-      g += (double)v[k].w * p.r64[id[k].w];
+      g += (double)v[k].x * vec[id[k].x];
+      g += (double)v[k].y * vec[id[k].y];
+      g += (double)v[k].z * vec[id[k].z];
+      g += (double)v[k].w * vec[id[k].w];
     }
   }
 #pragma unroll
@@ -622,9 +647,10 @@ __device__ __forceinline__ double kkt_violation(const EvalParams& p, double xv, 
 // Active columns of at most this many entries are summed by one lane alone.
 constexpr int kLaneLen = 16;
 
-// a_j^T r64 by one lane over a short column (len <= kLaneLen, padded to 4): all
+// a_j^T vec by one lane over a short column (len <= kLaneLen, padded to 4): all
 // entry loads first, then all gathers.
-__device__ __forceinline__ double lane_dot(const EvalParams& p, const int4 mt) {
+__device__ __forceinline__ double lane_dot(const EvalParams& p, const int4 mt,
+                                           const double* vec) {
   const int64_t start = (int64_t)(uint32_t)mt.x << 2;
   float4 v[kLaneLen / 4];
   int4 id[kLaneLen / 4];
@@ -642,10 +668,10 @@ __device__ __forceinline__ double lane_dot(const EvalParams& p, const int4 mt) {
 #pragma unroll
   for (int k = 0; k < kLaneLen / 4; ++k) {
     if (4 * k < mt.y) {
-      g += (double)v[k].x * p.r64[id[k].x];
-      g += (double)v[k].y * p.r64[id[k].y];
-      g += (double)v[k].z * p.r64[id[k].z];
-      g += (double)v[k].w * p.r64[id[k].w];
+      g += (double)v[k].x * vec[id[k].x];
+      g += (double)v[k].y * vec[id[k].y];
+      g += (double)v[k].z * vec[id[k].z];
+      g += (double)v[k].w * vec[id[k].w];
     }
   }
   return g;
@@ -671,7 +697,7 @@ __device__ __forceinline__ ActiveCol active_col(const EvalParams& p, int64_t t, 
   c.valid = t < cnt;
   c.j = c.valid ? p.active[t] : 0;
   c.mt = c.valid ? p.meta[c.j] : make_int4(0, 0, 0, 0);
-  c.g = c.valid && c.mt.y <= kLaneLen ? lane_dot(p, c.mt) : 0.0;
+  c.g = c.valid && c.mt.y <= kLaneLen ? lane_dot(p, c.mt, p.r64) : 0.0;
   unsigned longs = __ballot_sync(ACDC_FULL_MASK, c.valid && c.mt.y > kLaneLen);
   while (longs) {
     const int src = __ffs(longs) - 1;
@@ -680,7 +706,7 @@ __device__ __forceinline__ ActiveCol active_col(const EvalParams& p, int64_t t, 
     m.x = __shfl_sync(ACDC_FULL_MASK, c.mt.x, src);
     m.y = __shfl_sync(ACDC_FULL_MASK, c.mt.y, src);
     m.z = m.w = 0;
-    const double g = active_dot(p, m, lane);
+    const double g = active_dot(p, m, lane, p.r64);
     if (lane == src) c.g = g;
   }
   c.xv = c.valid ? coord(p, c.j) : 0.0;
@@ -854,6 +880,54 @@ __global__ void k_hot_collect(EvalParams p) {
   }
 }
 
+// Duality gap of losses 1 and 3, column pass (slot 3): sum_j q_j^2 with
+//   loss 1: q_j = a_j^T r + lambda x_j         (gap = sum q^2 / (2 lambda))
+//   loss 3: q_j = sum_i b_i A_ij sigma(r_i)    (dual term ||.||^2 / (2 lambda))
+// over every column: a lane sums a short column alone, the warp the long ones.
+__device__ __forceinline__ void k_gap_smooth_body(const EvalParams& p, const int64_t rank,
+                                                  const int64_t nb) {
+  __shared__ double s_q[ACDC_RED_THREADS / 32];
+  const int lane = threadIdx.x & 31;
+  const bool ridge = p.loss == ACDC_LOSS_L2_SQUARE;
+  const double* vec = ridge ? p.r64 : p.roww;
+  const int64_t step = (int64_t)nb * blockDim.x;
+  double qq = 0;
+  for (int64_t base = (int64_t)rank * blockDim.x + (threadIdx.x & ~31); base < p.n; base += step) {
+    const int64_t j = base + lane;
+    const bool valid = j < p.n;
+    const int4 mt = valid ? p.meta[j] : make_int4(0, 0, 0, 0);
+    double g = valid && mt.y <= kLaneLen ? lane_dot(p, mt, vec) : 0.0;
+    unsigned longs = __ballot_sync(ACDC_FULL_MASK, valid && mt.y > kLaneLen);
+    while (longs) {
+      const int src = __ffs(longs) - 1;
+      longs &= longs - 1;
+      int4 m;
+      m.x = __shfl_sync(ACDC_FULL_MASK, mt.x, src);
+      m.y = __shfl_sync(ACDC_FULL_MASK, mt.y, src);
+      m.z = m.w = 0;
+      const double gl = active_dot(p, m, lane, vec);
+      if (lane == src) g = gl;
+    }
+    if (valid) {
+      if (ridge) g += p.lambda * coord(p, j);
+      qq += g * g;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) qq += __shfl_down_sync(ACDC_FULL_MASK, qq, o);
+  if (lane == 0) s_q[threadIdx.x >> 5] = qq;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < ACDC_RED_THREADS / 32; ++w) t += s_q[w];
+    p.part[rank * ACDC_NPART + 3] = t;
+  }
+}
+
+__global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_smooth(EvalParams p) {
+  k_gap_smooth_body(p, blockIdx.x, gridDim.x);
+}
+
 __global__ void __launch_bounds__(ACDC_RED_THREADS) k_gap_lasso_screened(EvalParams p) {
   k_gap_lasso_screened_body(p, blockIdx.x, gridDim.x);
 }
@@ -990,6 +1064,13 @@ __device__ __forceinline__ void k_finalize_body(const EvalParams& p, const int64
     P = 0.5 * rr + p.lambda * s2;
     const double s = gmax > p.lambda ? p.lambda / gmax : 1.0;
     D = -s * br - 0.5 * s * s * rr;
+  } else if (p.loss == ACDC_LOSS_L2_SQUARE) {
+    P = 0.5 * rr + 0.5 * p.lambda * s2;
+    D = P - s3 / (2.0 * p.lambda);
+  } else if (p.loss == ACDC_LOSS_LOGISTIC) {
+    P = rr + 0.5 * p.lambda * s2;
+    D = -br - s3 / (2.0 * p.lambda);
+    acc = p.m > 0 ? s6 / (double)p.m : 0.0;
   } else {
     P = p.lambda * 0.5 * rr + s3 / nn;
     D = -p.lambda * 0.5 * rr + s2 / nn;
@@ -1036,14 +1117,15 @@ cudaError_t launch_layout_scan(const int64_t* col_ptr, int64_t n, int64_t* scrat
 // Pass 2: column starts and the padded FP32 / int32 arrays with ||a_j||^2.
 cudaError_t launch_layout_fill(const int64_t* col_ptr, const int32_t* row_idx,
                                const double* vals64, int64_t m, int64_t n, int64_t* scratch,
-                               DevProblem& d, cudaStream_t st) {
+                               DevProblem& d, int32_t loss, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   const int64_t tiles = layout_scan_tiles(n);
   int64_t* start4 = scratch;
   int64_t* tile_sums = scratch + n;
   k_scan_apply<<<(unsigned)tiles, kScanThreads, 0, st>>>(col_ptr, n, tile_sums, start4);
   const int64_t blocks = std::min<int64_t>((n + 7) / 8, 152 * 32);
-  k_build_columns<<<(unsigned)blocks, 256, 0, st>>>(col_ptr, row_idx, vals64, start4, m, n, d);
+  k_build_columns<<<(unsigned)blocks, 256, 0, st>>>(col_ptr, row_idx, vals64, start4, m, n, d,
+                                                      loss);
   return cudaGetLastError();
 }
 
@@ -1070,8 +1152,9 @@ static unsigned grid_for(int64_t n, int threads, int64_t cap) {
   return (unsigned)std::min<int64_t>(b, cap);
 }
 
-cudaError_t launch_set_li(const DevProblem& d, int32_t loss, double beta, cudaStream_t st) {
-  k_set_li<<<grid_for(d.n, 256, 152 * 8), 256, 0, st>>>(d, loss, beta);
+cudaError_t launch_set_li(const DevProblem& d, int32_t loss, double beta, double lambda,
+                          cudaStream_t st) {
+  k_set_li<<<grid_for(d.n, 256, 152 * 8), 256, 0, st>>>(d, loss, beta, lambda);
   return cudaGetLastError();
 }
 
@@ -1140,6 +1223,11 @@ cudaError_t launch_refresh(const EvalParams& p, cudaStream_t st) {
 }
 
 cudaError_t launch_gap(const EvalParams& p, cudaStream_t st) {
+  if (p.loss == ACDC_LOSS_L2_SQUARE || p.loss == ACDC_LOSS_LOGISTIC) {
+    k_gap_smooth<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
+    k_finalize<<<1, kFinThreads, 0, st>>>(p);
+    return cudaGetLastError();
+  }
   if (p.loss == ACDC_LOSS_L1_SQUARE && p.screened) {
     k_gap_lasso_screened<<<ACDC_RED_BLOCKS, ACDC_RED_THREADS, 0, st>>>(p);
     k_finalize<<<1, kFinThreads, 0, st>>>(p);

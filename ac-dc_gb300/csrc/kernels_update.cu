@@ -114,26 +114,45 @@ __device__ __forceinline__ Chunk load_chunk(const UpdateParams& p, uint64_t star
   return c;
 }
 
-template <typename T>
+// The residual entry as the gradient uses it: r itself, or for the logistic
+// loss sigma(r) = 1/(1 + exp(-r)), in a form that does not overflow.
+__device__ __forceinline__ float sigmoid_t(float z) {
+  if (z >= 0.f) return 1.f / (1.f + expf(-z));
+  const float e = expf(z);
+  return e / (1.f + e);
+}
+__device__ __forceinline__ double sigmoid_t(double z) {
+  if (z >= 0.0) return 1.0 / (1.0 + exp(-z));
+  const double e = exp(z);
+  return e / (1.0 + e);
+}
+template <int LOSS, typename T>
+__device__ __forceinline__ T rval(const T* r, int32_t i) {
+  const T v = __ldcg(r + i);
+  if constexpr (LOSS == ACDC_LOSS_LOGISTIC) return sigmoid_t(v);
+  return v;
+}
+
+template <int LOSS, typename T>
 __device__ __forceinline__ T gather_dot(const T* r, const Chunk& c, bool live) {
   if (!live) return T(0);
-  T a = (T)c.v.x * __ldcg(r + c.i.x);
-  a += (T)c.v.y * __ldcg(r + c.i.y);
-  a += (T)c.v.z * __ldcg(r + c.i.z);
-  a += (T)c.v.w * __ldcg(r + c.i.w);
+  T a = (T)c.v.x * rval<LOSS>(r, c.i.x);
+  a += (T)c.v.y * rval<LOSS>(r, c.i.y);
+  a += (T)c.v.z * rval<LOSS>(r, c.i.z);
+  a += (T)c.v.w * rval<LOSS>(r, c.i.w);
   return a;
 }
 
 // The same for the first chunk, skipping the pad entries of a column whose
 // length is not a multiple of 4 (most columns are short: one gather, not four).
-template <typename T>
+template <int LOSS, typename T>
 __device__ __forceinline__ T gather_dot_head(const T* r, const Chunk& c, uint32_t e0,
                                              uint32_t len) {
   T a = T(0);
-  if (e0 < len) a = (T)c.v.x * __ldcg(r + c.i.x);
-  if (e0 + 1u < len) a += (T)c.v.y * __ldcg(r + c.i.y);
-  if (e0 + 2u < len) a += (T)c.v.z * __ldcg(r + c.i.z);
-  if (e0 + 3u < len) a += (T)c.v.w * __ldcg(r + c.i.w);
+  if (e0 < len) a = (T)c.v.x * rval<LOSS>(r, c.i.x);
+  if (e0 + 1u < len) a += (T)c.v.y * rval<LOSS>(r, c.i.y);
+  if (e0 + 2u < len) a += (T)c.v.z * rval<LOSS>(r, c.i.z);
+  if (e0 + 3u < len) a += (T)c.v.w * rval<LOSS>(r, c.i.w);
   return a;
 }
 
@@ -247,12 +266,12 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
       ms_2d = ring_next(ms_2d, kMS);
 
       // g = a_j^T r.
-      T acc = gather_dot_head<T>(r, c0, e0, len);
+      T acc = gather_dot_head<LOSS, T>(r, c0, e0, len);
       if (len > 128u) {
         Chunk a = load_chunk(p, start, len, 128u, lane);
         for (uint32_t off = 128u; off < len; off += 128u) {
           Chunk b = load_chunk(p, start, len, off + 128u, lane);
-          acc += gather_dot<T>(r, a, off + e0 < len);
+          acc += gather_dot<LOSS, T>(r, a, off + e0 < len);
           a = b;
         }
       }
@@ -267,6 +286,16 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
         const T xn = z > T(0) ? a : (z < T(0) ? -a : T(0));
         delta = xn - xj;
         coef = delta;
+      } else if (LOSS == ACDC_LOSS_L2_SQUARE) {
+        // MulticoreL2SquareRegSquareLoss.h:56-78: delta = -Li (a_j^T r + lambda x_j)
+        delta = -li * (g + lam * xj);
+        coef = delta;
+      } else if (LOSS == ACDC_LOSS_LOGISTIC) {
+        // MulticoreL2SquareRegLogisticLoss.h:88-115 with the label folded into the
+        // values: gradient -sum_i v_i sigma(r_i) + lambda x_j, half step, and
+        // r_i += -delta v_i.
+        delta = -li * (lam * xj - g) / T(2);
+        coef = -delta;
       } else {
         const T y = li < T(0) ? T(-1) : T(1);
         delta = (T(1) - g * y) * lam * fabs(li);
@@ -362,18 +391,23 @@ cudaError_t launch_update(const UpdateParams& p, uint64_t k_base, int warps_per_
   if (e != cudaSuccess) return e;
   const int blocks = (p.n_warps + warps_per_block - 1) / warps_per_block;
   dim3 grid(blocks), block(warps_per_block * 32);
-  const bool svm = p.loss == ACDC_LOSS_SVM_DUAL;
+#define ACDC_LAUNCH(L, T) k_pcdm_update<L, T><<<grid, block, 0, st>>>(p, k_base)
   if (p.fp64) {
-    if (svm)
-      k_pcdm_update<ACDC_LOSS_SVM_DUAL, double><<<grid, block, 0, st>>>(p, k_base);
-    else
-      k_pcdm_update<ACDC_LOSS_L1_SQUARE, double><<<grid, block, 0, st>>>(p, k_base);
+    switch (p.loss) {
+      case ACDC_LOSS_L1_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L1_SQUARE, double); break;
+      case ACDC_LOSS_L2_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L2_SQUARE, double); break;
+      case ACDC_LOSS_SVM_DUAL: ACDC_LAUNCH(ACDC_LOSS_SVM_DUAL, double); break;
+      default: ACDC_LAUNCH(ACDC_LOSS_LOGISTIC, double); break;
+    }
   } else {
-    if (svm)
-      k_pcdm_update<ACDC_LOSS_SVM_DUAL, float><<<grid, block, 0, st>>>(p, k_base);
-    else
-      k_pcdm_update<ACDC_LOSS_L1_SQUARE, float><<<grid, block, 0, st>>>(p, k_base);
+    switch (p.loss) {
+      case ACDC_LOSS_L1_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L1_SQUARE, float); break;
+      case ACDC_LOSS_L2_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L2_SQUARE, float); break;
+      case ACDC_LOSS_SVM_DUAL: ACDC_LAUNCH(ACDC_LOSS_SVM_DUAL, float); break;
+      default: ACDC_LAUNCH(ACDC_LOSS_LOGISTIC, float); break;
+    }
   }
+#undef ACDC_LAUNCH
   return cudaGetLastError();
 }
 
@@ -395,6 +429,10 @@ cudaError_t update_kernels_init() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L1_SQUARE, double>, a, carve);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_SVM_DUAL, float>, a, carve);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_SVM_DUAL, double>, a, carve);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L2_SQUARE, float>, a, carve);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L2_SQUARE, double>, a, carve);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_LOGISTIC, float>, a, carve);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_LOGISTIC, double>, a, carve);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_L1_SQUARE, float>, a, carve);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_L1_SQUARE, double>, a, carve);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_SVM_DUAL, float>, a, carve);

@@ -4,8 +4,11 @@
  * The library replaces the hot path of optml/ac-dc's multicore engine:
  * randomized parallel coordinate descent (PCDM) for
  *   loss 0: L1-regularised least squares  min_x 0.5||Ax-b||^2 + lambda||x||_1
+ *   loss 1: L2-regularised least squares  min_x 0.5||Ax-b||^2 + (lambda/2)||x||^2
  *   loss 2: hinge-loss SVM dual (SDCA)    max_a (1/n)sum a_i - (lambda/2)||w(a)||^2,
  *                                          w(a) = (1/(lambda n)) sum_i a_i y_i x_i
+ *   loss 3: L2-regularised logistic       min_x sum_i log(1 + exp(-b_i A_i. x))
+ *                                                + (lambda/2)||x||^2
  * behind plain pointers and sizes.  A C++ engine (CudaEngineExecutor.h) plugs
  * these calls into the reference's AbstractEngineExecutor / Solver structure.
  *
@@ -13,9 +16,12 @@
  *  - Every function returns 0 (ACDC_OK) or a negative ACDC_E* status; no C++
  *    exception crosses this boundary.  acdc_last_error() gives the message.
  *  - Matrices arrive as compressed columns of the coordinate operand:
- *      loss 0: CSC of A (m rows x n columns), vector b of length m;
+ *      losses 0, 1: CSC of A (m rows x n columns), vector b of length m;
  *      loss 2: CSR of X by sample == CSC of X^T (m = features, n = samples),
- *              labels y of length n.
+ *              labels y of length n;
+ *      loss 3: CSC of A with samples as rows and features as columns, labels
+ *              b (+-1) of length m (MultiCoreSolver.cpp:80-105 arranges LIBSVM
+ *              data this way for this loss).
  *    This matches ProblemData<L,D> (cpp/src/solver/structures.h:31-97): the
  *    multicore Lasso reads A_csc_*, the SVM dual reads A_csr_*, and in both
  *    instance.m is the residual length and instance.n the coordinate count.
@@ -36,7 +42,7 @@ extern "C" {
 #define ACDC_OK 0
 #define ACDC_EINVAL (-1)      /* invalid argument (sizes, pointers, indices)        */
 #define ACDC_ENOMEM (-2)      /* device or host allocation failed                   */
-#define ACDC_EUNSUPPORTED (-3)/* loss code 1 or 3 (not on this path)                */
+#define ACDC_EUNSUPPORTED (-3)/* loss 1 or 3 in a batched path or the server        */
 #define ACDC_ECUDA (-4)       /* CUDA runtime error                                 */
 #define ACDC_ETIMEOUT (-5)    /* a bounded device wait ran out                      */
 #define ACDC_EDEVICE (-6)     /* a kernel reported a bad index or state             */
@@ -46,10 +52,13 @@ extern "C" {
 
 /* ---- loss codes (OptimizationSettings::lossFunction,
  *      cpp/src/solver/MulticoreEngineExecutor.h:32-58) ------------------- */
-#define ACDC_LOSS_L1_SQUARE 0
-#define ACDC_LOSS_L2_SQUARE 1 /* unsupported: returns ACDC_EUNSUPPORTED */
-#define ACDC_LOSS_SVM_DUAL 2
-#define ACDC_LOSS_LOGISTIC 3  /* unsupported: returns ACDC_EUNSUPPORTED */
+#define ACDC_LOSS_L1_SQUARE 0 /* MulticoreL1RegSquareLoss                          */
+#define ACDC_LOSS_L2_SQUARE 1 /* MulticoreL2SquareRegSquareLoss                    */
+#define ACDC_LOSS_SVM_DUAL 2  /* MulticoreSVMDualLoss                              */
+#define ACDC_LOSS_LOGISTIC 3  /* MulticoreL2SquareRegLogisticLoss                  */
+/* q-shrinking, screened evaluations, batched paths and the server cover losses
+ * 0 and 2; losses 1 and 3 solve one problem at a time (batched calls with them
+ * return ACDC_EUNSUPPORTED). */
 
 typedef struct acdc_ctx acdc_ctx;
 typedef struct acdc_problem acdc_problem;
@@ -58,7 +67,7 @@ typedef struct acdc_server acdc_server;
 /* Solver settings: the OptimizationSettings fields this path reads
  * (cpp/src/solver/settingsAndStatistics.h:11-93) plus the device knobs. */
 typedef struct acdc_settings {
-  int32_t loss;                   /* lossFunction: 0 or 2                          */
+  int32_t loss;                   /* lossFunction: 0, 1, 2 or 3                    */
   int32_t tau;                    /* updates in flight (= totalThreads); >= 1      */
   int32_t warps_per_block;        /* CTA size in warps for the update kernel       */
   int32_t refresh_every;          /* epochs between FP64 refresh + gap in solve    */
@@ -105,15 +114,24 @@ typedef struct acdc_settings {
 #define ACDC_PREC_FP32 1
 #define ACDC_PREC_FP64 2
 
-/* FP64 evaluation of the current iterate (after an FP64 refresh). */
+/* FP64 evaluation of the current iterate (after an FP64 refresh).  The duality
+ * gaps of losses 0, 1 and 3 are this library's (the reference reports a gap
+ * for the SVM dual only):
+ *   loss 0: dual point s r, s = min(1, lambda/||A^T r||_inf);
+ *   loss 1: P - D = sum_j (a_j^T r + lambda x_j)^2 / (2 lambda), dual point r;
+ *   loss 3: D(a) = -sum_i [a_i log a_i + (1-a_i) log(1-a_i)]
+ *                  - ||sum_i a_i b_i A_i.||^2 / (2 lambda) at a_i = sigmoid(r_i),
+ *           with r_i = -b_i A_i. x. */
 typedef struct acdc_eval {
   double primal;            /* P                                                  */
   double dual;              /* D                                                  */
   double gap;               /* P - D                                              */
   double rel_gap;           /* (P - D) / max(1, |P|)                              */
-  double zero_one_accuracy; /* SVM: fraction of y_i x_i^T w > 0; Lasso: 0         */
-  double reg_norm;          /* Lasso ||x||_1; SVM sum alpha_i                     */
-  double sq_norm;           /* Lasso ||Ax-b||^2; SVM ||w||^2                      */
+  double zero_one_accuracy; /* SVM: fraction of y_i x_i^T w > 0; logistic: fraction
+                               of correctly signed samples; 0 otherwise           */
+  double reg_norm;          /* loss 0: ||x||_1; 1, 3: ||x||^2; SVM: sum alpha_i    */
+  double sq_norm;           /* loss 0, 1: ||Ax-b||^2; SVM: ||w||^2; logistic:
+                               sum log(1 + exp(r_i))                              */
   double max_abs_grad;      /* Lasso ||A^T r||_inf (an upper bound of it after a
                                screened evaluation); SVM 0                        */
   int64_t support;          /* nonzeros of x (alpha)                              */
@@ -168,9 +186,10 @@ const char* acdc_status_string(int status);
 /* ---- problem upload (replaces InputOuputHelper::loadCSCData /
  *      loadDistributedSparseSVMRowData feeding MulticoreEngineExecutor's
  *      constructor, cpp/src/solver/MulticoreEngineExecutor.h:25-66) ------- */
-/* col_ptr: n+1 offsets; row_idx/vals: col_ptr[n] entries; rhs: b (loss 0, m
- * entries) or y (loss 2, n entries, +-1).  Values are stored on the device as
- * FP32 in 16-byte aligned column segments; x starts at 0. */
+/* col_ptr: n+1 offsets; row_idx/vals: col_ptr[n] entries; rhs: b (losses 0,
+ * 1: m entries), y (loss 2: n entries, +-1) or the labels (loss 3: m entries,
+ * +-1).  Values are stored on the device as FP32 in 16-byte aligned column
+ * segments (loss 3: b_i A_ij); x starts at 0. */
 int acdc_problem_create(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t* col_ptr,
                         const int32_t* row_idx, const double* vals, const double* rhs,
                         double lambda, acdc_problem** out);

@@ -89,3 +89,46 @@ def test_console_solver_bulk_mode_prints_reference_rows(tmp_path):
     objs = [float(r[1]) for r in rows]
     assert objs[-1] < objs[0] and all(b <= a * (1 + 1e-6) for a, b in zip(objs, objs[1:]))
     assert "Last objective value" in out.stdout
+
+
+def write_libsvm(path, sv):
+    """LIBSVM text of an SVM-generator instance (samples as lines, 1-based features)."""
+    with open(path, "w") as f:
+        for i in range(sv.n):
+            s, e = sv.col_ptr[i], sv.col_ptr[i + 1]
+            feats = " ".join("%d:%.17g" % (int(c) + 1, v)
+                             for c, v in zip(sv.row_idx[s:e], sv.vals[s:e]))
+            f.write("%d %s\n" % (int(sv.rhs[i]), feats))
+
+
+@pytest.mark.gpu
+def test_console_solver_ridge_and_logistic(tmp_path):
+    """-f 1 reads the CSC text format like -f 0; -f 3 reads LIBSVM samples and
+    turns them into rows over feature columns (MultiCoreSolver.cpp:80-105).
+    Both solve to the oracle's optimum."""
+    rd = acdc.gen_lasso(500, 1500, nnz_per_col=6, n_star=20, lambda_frac=0.1, seed=93)
+    pre, bfile = write_csc(tmp_path, rd)
+    lam = 0.2
+    x, r, ev, ep = oracle.smooth_solve(oracle.RIDGE, rd.m, rd.n, rd.col_ptr, rd.row_idx, rd.vals,
+                                       rd.rhs, lam, target=1e-11)
+    out = subprocess.run([SOLVER, "-A", pre, "-b", bfile, "-l", repr(lam), "-t", "32", "-f", "1",
+                          "-G", "1e-9"], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    line = [l for l in out.stdout.splitlines() if l.startswith("converged,")][-1].split(",")
+    fields = dict(zip(line[0::2], line[1::2]))
+    assert fields["converged"] == "1"
+    assert abs(float(fields["primal"]) - ev["primal"]) <= 1e-6 * ev["primal"]
+
+    sv = acdc.gen_svm(600, 1200, nnz_median=15, nnz_sigma=0.5, w_star_nnz=60, lam=1e-3, seed=94)
+    path = str(tmp_path / "train.libsvm")
+    write_libsvm(path, sv)
+    lg = acdc.logistic_from_svm(sv, 0.02)
+    x, r, ev, ep = oracle.smooth_solve(oracle.LOGISTIC, lg.m, lg.n, lg.col_ptr, lg.row_idx,
+                                       lg.vals, lg.rhs, 0.02, target=1e-11, max_epochs=50000)
+    out = subprocess.run([SOLVER, "-A", path, "-l", "0.02", "-t", "16", "-f", "3", "-G", "1e-9"],
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    line = [l for l in out.stdout.splitlines() if l.startswith("converged,")][-1].split(",")
+    fields = dict(zip(line[0::2], line[1::2]))
+    assert fields["converged"] == "1"
+    assert abs(float(fields["primal"]) - ev["primal"]) <= 1e-6 * ev["primal"]

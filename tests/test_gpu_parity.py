@@ -238,11 +238,17 @@ def test_invalid_inputs_are_rejected(ctx):
     with pytest.raises(acdc.AcdcError) as e:
         acdc.Problem(ctx, bad)
     assert e.value.code == acdc.EDEVICE
-    for loss in (acdc.LOSS_L2_SQUARE, acdc.LOSS_LOGISTIC):
-        with pytest.raises(acdc.AcdcError) as e:
-            acdc.Problem(ctx, acdc.Instance(loss, inst.m, inst.n, inst.col_ptr, inst.row_idx,
-                                            inst.vals, inst.rhs, inst.lam))
-        assert e.value.code == acdc.EUNSUPPORTED
+    # losses 1 and 3 solve one problem at a time; the batched paths take 0 and 2
+    ridge = acdc.Problem(ctx, acdc.Instance(acdc.LOSS_L2_SQUARE, inst.m, inst.n, inst.col_ptr,
+                                            inst.row_idx, inst.vals, inst.rhs, inst.lam))
+    with pytest.raises(acdc.AcdcError) as e:
+        acdc.batch_solve_path(ctx, [ridge], np.array([[inst.lam]]))
+    assert e.value.code == acdc.EUNSUPPORTED
+    ridge.close()
+    with pytest.raises(acdc.AcdcError) as e:
+        acdc.Problem(ctx, acdc.Instance(4, inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals,
+                                        inst.rhs, inst.lam))
+    assert e.value.code == acdc.EINVAL
     cp = inst.col_ptr.copy()
     cp[0] = 1
     with pytest.raises(acdc.AcdcError) as e:
