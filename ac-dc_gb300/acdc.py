@@ -182,6 +182,11 @@ def host_lib():
         H.acdc_load_csc_text_sizes.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(I64),
                                                C.POINTER(I64), C.POINTER(I64)]
         H.acdc_load_csc_text.argtypes = [C.c_char_p, C.c_char_p, VP, VP, VP, VP]
+        H.acdc_load_csc_binary_sizes.argtypes = [C.c_char_p, C.c_char_p, C.c_int32, C.c_char_p,
+                                                 I64, C.POINTER(I64), C.POINTER(I64),
+                                                 C.POINTER(I64)]
+        H.acdc_load_csc_binary.argtypes = [C.c_char_p, C.c_char_p, C.c_int32, C.c_char_p, I64,
+                                           VP, VP, VP, VP]
         H.acdc_load_libsvm_sizes.argtypes = [C.c_char_p, C.POINTER(I64), C.POINTER(I64),
                                              C.POINTER(I64)]
         H.acdc_load_libsvm.argtypes = [C.c_char_p, VP, VP, VP, VP]
@@ -314,6 +319,22 @@ def load_csc_text(prefix, vector_file, lam):
     _check_host(H.acdc_load_csc_text(prefix.encode(), vector_file.encode(), _ptr(col_ptr),
                                      _ptr(row_idx), _ptr(vals), _ptr(b)), "load_csc_text")
     return Instance(LOSS_L1_SQUARE, m.value, n.value, col_ptr, row_idx, vals, b, lam)
+
+
+def load_csc_binary(prefix, suffix, rank, vector_file, local_n, lam, loss=LOSS_L1_SQUARE):
+    """The binary per-rank CSC format (loadANSCIAndBinaryData)."""
+    H = host_lib()
+    m, n, nnz = I64(0), I64(0), I64(0)
+    args = (prefix.encode(), suffix.encode(), int(rank), vector_file.encode(), int(local_n))
+    _check_host(H.acdc_load_csc_binary_sizes(*args, C.byref(m), C.byref(n), C.byref(nnz)),
+                "load_csc_binary_sizes")
+    col_ptr = np.zeros(n.value + 1, np.int64)
+    row_idx = np.zeros(nnz.value, np.int32)
+    vals = np.zeros(nnz.value)
+    b = np.zeros(m.value)
+    _check_host(H.acdc_load_csc_binary(*args, _ptr(col_ptr), _ptr(row_idx), _ptr(vals), _ptr(b)),
+                "load_csc_binary")
+    return Instance(loss, m.value, n.value, col_ptr, row_idx, vals, b, lam)
 
 
 def load_libsvm(path, lam):

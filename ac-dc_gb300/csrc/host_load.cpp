@@ -6,6 +6,11 @@
 //    list read by loadVectorData (:32-48).  One deliberate difference: the
 //    reference drops a final value that has no trailing whitespace (its
 //    read-then-test-eof loop); this reader keeps it.
+//  * Binary per-rank CSC: loadANSCIAndBinaryData
+//    (cpp/src/utils/file_reader.h:50-106): <prefix>_colptr_<rank><suffix> holds
+//    local_n + 1 whitespace-separated column offsets, <prefix>_rowid_<rank><suffix>
+//    the row indices as raw int32 and <prefix>_values_<rank><suffix> the values
+//    as raw doubles (native byte order); b comes from a text vector file.
 //  * LIBSVM text: loadDistributedSparseSVMRowData
 //    (cpp/src/utils/distributed_instances_loader.h:68-193) with sizes from
 //    parse_LIB_SVM_data_get_size (cpp/src/svm/svm_parser.h:11-77): one sample
@@ -81,6 +86,52 @@ int read_csc_text(const char* prefix, const char* vector_file, CscText& t) {
   for (int64_t r : t.rows)
     if (r < 0 || r >= m) return ACDC_EINVAL;
   return ACDC_OK;
+}
+
+struct CscBinary {
+  std::vector<int64_t> col_ptr;
+  std::vector<double> b;
+  std::string rowid, values;
+};
+
+long file_size(const std::string& path) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return -1;
+  std::fseek(f, 0, SEEK_END);
+  long len = std::ftell(f);
+  std::fclose(f);
+  return len;
+}
+
+// Column offsets, b and the paths of the two binary files, with their sizes checked.
+int read_csc_binary_head(const char* prefix, const char* suffix, int32_t rank,
+                         const char* vector_file, int64_t local_n, CscBinary& t) {
+  if (!prefix || !vector_file || local_n < 0) return ACDC_EINVAL;
+  const std::string pre(prefix), suf(suffix ? suffix : ""), rk = std::to_string(rank);
+  std::string s;
+  if (!read_file(vector_file, s) || !parse_numbers(s, t.b)) return ACDC_EINVAL;
+  std::vector<int64_t> ptr;
+  if (!read_file(pre + "_colptr_" + rk + suf, s) || !parse_numbers(s, ptr)) return ACDC_EINVAL;
+  if ((int64_t)ptr.size() < local_n + 1 || ptr[0] != 0) return ACDC_EINVAL;
+  t.col_ptr.assign(ptr.begin(), ptr.begin() + local_n + 1);
+  for (int64_t j = 0; j < local_n; ++j)
+    if (t.col_ptr[(size_t)j + 1] < t.col_ptr[(size_t)j]) return ACDC_EINVAL;
+  const int64_t nnz = t.col_ptr[(size_t)local_n];
+  t.rowid = pre + "_rowid_" + rk + suf;
+  t.values = pre + "_values_" + rk + suf;
+  if (file_size(t.rowid) < (long)(nnz * (int64_t)sizeof(int32_t)) ||
+      file_size(t.values) < (long)(nnz * (int64_t)sizeof(double)))
+    return ACDC_EINVAL;
+  return ACDC_OK;
+}
+
+bool read_raw(const std::string& path, void* dst, size_t bytes) {
+  if (bytes == 0) return true;
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return false;
+  const size_t got = std::fread(dst, 1, bytes, f);
+  std::fclose(f);
+  return got == bytes;
 }
 
 struct LibsvmScan {
@@ -159,6 +210,39 @@ extern "C" int acdc_load_csc_text(const char* prefix, const char* vector_file, i
   std::memcpy(col_ptr, t.col_ptr.data(), sizeof(int64_t) * t.col_ptr.size());
   for (size_t e = 0; e < t.rows.size(); ++e) row_idx[e] = (int32_t)t.rows[e];
   if (!t.vals.empty()) std::memcpy(vals, t.vals.data(), sizeof(double) * t.vals.size());
+  std::memcpy(b, t.b.data(), sizeof(double) * t.b.size());
+  return ACDC_OK;
+}
+
+extern "C" int acdc_load_csc_binary_sizes(const char* prefix, const char* suffix, int32_t rank,
+                                          const char* vector_file, int64_t local_n, int64_t* m,
+                                          int64_t* n, int64_t* nnz) {
+  if (!m || !n || !nnz) return ACDC_EINVAL;
+  CscBinary t;
+  int rc = read_csc_binary_head(prefix, suffix, rank, vector_file, local_n, t);
+  if (rc) return rc;
+  *m = (int64_t)t.b.size();
+  *n = local_n;
+  *nnz = t.col_ptr[(size_t)local_n];
+  return ACDC_OK;
+}
+
+extern "C" int acdc_load_csc_binary(const char* prefix, const char* suffix, int32_t rank,
+                                    const char* vector_file, int64_t local_n, int64_t* col_ptr,
+                                    int32_t* row_idx, double* vals, double* b) {
+  if (!col_ptr || !b) return ACDC_EINVAL;
+  CscBinary t;
+  int rc = read_csc_binary_head(prefix, suffix, rank, vector_file, local_n, t);
+  if (rc) return rc;
+  const int64_t nnz = t.col_ptr[(size_t)local_n];
+  if (nnz > 0 && (!row_idx || !vals)) return ACDC_EINVAL;
+  if (!read_raw(t.rowid, row_idx, sizeof(int32_t) * (size_t)nnz) ||
+      !read_raw(t.values, vals, sizeof(double) * (size_t)nnz))
+    return ACDC_EINVAL;
+  const int64_t m = (int64_t)t.b.size();
+  for (int64_t e = 0; e < nnz; ++e)
+    if (row_idx[e] < 0 || row_idx[e] >= m) return ACDC_EINVAL;
+  std::memcpy(col_ptr, t.col_ptr.data(), sizeof(int64_t) * t.col_ptr.size());
   std::memcpy(b, t.b.data(), sizeof(double) * t.b.size());
   return ACDC_OK;
 }

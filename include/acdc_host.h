@@ -116,6 +116,19 @@ int acdc_load_csc_text_sizes(const char* prefix, const char* vector_file, int64_
 int acdc_load_csc_text(const char* prefix, const char* vector_file, int64_t* col_ptr,
                        int32_t* row_idx, double* vals, double* b);
 
+/* Binary per-rank CSC: <prefix>_colptr_<rank><suffix> (local_n + 1 text
+ * offsets), <prefix>_rowid_<rank><suffix> (raw int32 rows) and
+ * <prefix>_values_<rank><suffix> (raw doubles, native byte order) plus the text
+ * vector file: the format read by loadANSCIAndBinaryData
+ * (cpp/src/utils/file_reader.h:50-106), whose column count local_n the caller
+ * gives.  Phase 1 returns the sizes, phase 2 fills. */
+int acdc_load_csc_binary_sizes(const char* prefix, const char* suffix, int32_t rank,
+                               const char* vector_file, int64_t local_n, int64_t* m, int64_t* n,
+                               int64_t* nnz);
+int acdc_load_csc_binary(const char* prefix, const char* suffix, int32_t rank,
+                         const char* vector_file, int64_t local_n, int64_t* col_ptr,
+                         int32_t* row_idx, double* vals, double* b);
+
 /* LIBSVM text (label index:value ...), 1-based feature indices mapped to
  * 0-based, labels 0 mapped to -1 for two classes: the reader
  * loadDistributedSparseSVMRowData (cpp/src/utils/distributed_instances_loader.h:68-193,

@@ -141,6 +141,48 @@ def test_csc_text_loader_rejects_bad_input(tmp_path):
         acdc.load_csc_text(str(tmp_path / "missing"), str(tmp_path / "b.txt"), 1.0)
 
 
+def write_csc_binary(pre, suffix, rank, inst, b_path):
+    np.savetxt("%s_colptr_%d%s" % (pre, rank, suffix), inst.col_ptr, fmt="%d")
+    inst.row_idx.astype(np.int32).tofile("%s_rowid_%d%s" % (pre, rank, suffix))
+    inst.vals.astype(np.float64).tofile("%s_values_%d%s" % (pre, rank, suffix))
+    np.savetxt(b_path, inst.rhs, fmt="%.17g")
+
+
+def test_csc_binary_loader_roundtrip(tmp_path):
+    """loadANSCIAndBinaryData's per-rank format: text offsets, raw int32 rows,
+    raw doubles (file_reader.h:50-106)."""
+    inst = acdc.gen_lasso(50, 80, nnz_per_col=4, n_star=5, seed=2)
+    pre, b_path = str(tmp_path / "A"), str(tmp_path / "b.txt")
+    write_csc_binary(pre, ".dat", 3, inst, b_path)
+    got = acdc.load_csc_binary(pre, ".dat", 3, b_path, inst.n, 0.5)
+    assert (got.m, got.n) == (inst.m, inst.n)
+    assert np.array_equal(got.col_ptr, inst.col_ptr)
+    assert np.array_equal(got.row_idx, inst.row_idx)
+    assert np.array_equal(got.vals, inst.vals) and np.array_equal(got.rhs, inst.rhs)
+    # fewer columns than the offsets file holds: the first local_n are read
+    part = acdc.load_csc_binary(pre, ".dat", 3, b_path, 10, 0.5)
+    assert part.n == 10 and np.array_equal(part.col_ptr, inst.col_ptr[:11])
+    assert np.array_equal(part.vals, inst.vals[:inst.col_ptr[10]])
+
+
+def test_csc_binary_loader_rejects_bad_input(tmp_path):
+    inst = acdc.gen_lasso(30, 40, nnz_per_col=3, n_star=4, seed=3)
+    pre, b_path = str(tmp_path / "A"), str(tmp_path / "b.txt")
+    write_csc_binary(pre, "", 0, inst, b_path)
+    with pytest.raises(acdc.AcdcError):  # more columns than offsets
+        acdc.load_csc_binary(pre, "", 0, b_path, inst.n + 1, 1.0)
+    with pytest.raises(acdc.AcdcError):  # missing rank
+        acdc.load_csc_binary(pre, "", 1, b_path, inst.n, 1.0)
+    rows = inst.row_idx.astype(np.int32).copy()
+    rows[5] = inst.m  # out of range
+    rows.tofile(pre + "_rowid_0")
+    with pytest.raises(acdc.AcdcError):
+        acdc.load_csc_binary(pre, "", 0, b_path, inst.n, 1.0)
+    inst.row_idx.astype(np.int32)[:-2].tofile(pre + "_rowid_0")  # truncated
+    with pytest.raises(acdc.AcdcError):
+        acdc.load_csc_binary(pre, "", 0, b_path, inst.n, 1.0)
+
+
 def test_libsvm_loader(tmp_path):
     p = tmp_path / "d.svm"
     p.write_text("+1 1:0.5 3:1.5\n-1 2:2\n\n0 1:1 4:-1\n")
