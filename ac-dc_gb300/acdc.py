@@ -148,6 +148,7 @@ def gpu_lib():
         L.acdc_reset_stats.argtypes = [VP]
         L.acdc_synchronize.argtypes = [VP]
         L.acdc_debug_sample.argtypes = [VP, U64, U64, U64, I64, VP]
+        L.acdc_test_accuracy.argtypes = [VP, I64, VP, VP, VP, VP, C.POINTER(D)]
         L.acdc_debug_sample_noalloc.argtypes = [VP, U64, U64, U64, I64, VP]
         L.acdc_batch_solve_path.argtypes = [VP, I32, VP, VP, C.POINTER(BatchOptions), VP, VP]
         L.acdc_server_create.argtypes = [VP, C.POINTER(ServerOptions), C.POINTER(VP)]
@@ -487,6 +488,19 @@ class Problem:
         r = np.zeros(self.m)
         self.ctx.check(self.L.acdc_get_residuals(self.h, _ptr(r)))
         return r
+
+    def test_accuracy(self, row_ptr, col_idx, vals, labels):
+        """0-1 accuracy on held-out samples (CSR over the features)."""
+        rp = np.ascontiguousarray(row_ptr, np.int64)
+        ci = np.ascontiguousarray(col_idx, np.int32)
+        va = np.ascontiguousarray(vals, np.float64)
+        lb = np.ascontiguousarray(labels, np.float64)
+        acc = D(0)
+        self.ctx.check(self.L.acdc_test_accuracy(self.h, len(rp) - 1, _ptr(rp),
+                                                 _ptr(ci) if ci.size else None,
+                                                 _ptr(va) if va.size else None, _ptr(lb),
+                                                 C.byref(acc)))
+        return acc.value
 
     def stats(self):
         s = Stats()

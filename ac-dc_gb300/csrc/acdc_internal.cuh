@@ -279,6 +279,11 @@ cudaError_t launch_active_omega(const EvalParams& p, int32_t* rowcnt, cudaStream
 cudaError_t launch_gap(const EvalParams& p, cudaStream_t st);
 // Active-set violations (Lasso, after a full gap pass that built the list).
 cudaError_t launch_active_viol(const EvalParams& p, cudaStream_t st);
+// Test-set 0-1 accuracy (count of positive margins into *good).
+cudaError_t launch_test_accuracy(int64_t n_test, const int64_t* row_ptr, const int32_t* col_idx,
+                                 const double* vals, const double* labels, const double* w64,
+                                 const float* w32, int64_t w_len, unsigned long long* good,
+                                 cudaStream_t st);
 // Hot list from the violations of the last evaluation; zeroes CNT_HOT first.
 cudaError_t launch_hot_set(const EvalParams& p, cudaStream_t st);
 cudaError_t launch_debug_sample(uint64_t seed, uint64_t k0, uint64_t count, int64_t n,

@@ -791,3 +791,72 @@ extern "C" int acdc_debug_sample(acdc_ctx* ctx, uint64_t seed, uint64_t k0, uint
   if (e != cudaSuccess) return acdc_cuda_error(ctx, e, "acdc_debug_sample");
   return ACDC_OK;
 }
+
+// Test-set accuracy: the test loop of MulticoreSVMDualLoss::computeObjectiveValue
+// (cpp/src/solver/lossFunctions/SVMDualLoss/MulticoreSVMDualLoss.h:95-112) for the
+// SVM dual, with w refreshed from the current alpha in FP64, and of
+// MulticoreL2SquareRegLogisticLoss::computeObjectiveValue (MulticoreL2SquareRegLogisticLoss.h:65-81)
+// for the logistic loss, with the coordinates x as weights (that loop reads the
+// training matrix's feature indices; the test matrix's own are read here).
+extern "C" int acdc_test_accuracy(acdc_problem* p, int64_t n_test, const int64_t* row_ptr,
+                                  const int32_t* col_idx, const double* vals,
+                                  const double* labels, double* accuracy) {
+  if (!p || !accuracy || n_test < 0 || (n_test > 0 && (!row_ptr || !labels))) return ACDC_EINVAL;
+  acdc_ctx* ctx = p->ctx;
+  if (p->loss != ACDC_LOSS_SVM_DUAL && p->loss != ACDC_LOSS_LOGISTIC)
+    return acdc_set_error(ctx, ACDC_EUNSUPPORTED, "test accuracy is for losses 2 and 3");
+  *accuracy = 0;
+  if (n_test == 0) return ACDC_OK;
+  const int64_t nnz = row_ptr[n_test];
+  if (row_ptr[0] != 0 || nnz < 0 || (nnz > 0 && (!col_idx || !vals)))
+    return acdc_set_error(ctx, ACDC_EINVAL, "invalid test matrix");
+  for (int64_t i = 0; i < n_test; ++i)
+    if (row_ptr[i + 1] < row_ptr[i]) return acdc_set_error(ctx, ACDC_EINVAL, "invalid test matrix");
+  cudaStream_t st = ctx->stream;
+  const double* w64 = nullptr;
+  const float* w32 = nullptr;
+  int64_t w_len = 0;
+  if (p->loss == ACDC_LOSS_SVM_DUAL) {
+    int rc = acdc_recompute_residuals(p);
+    if (rc != ACDC_OK) return rc;
+    w64 = p->d.r64;
+    w_len = p->d.m;
+  } else {
+    if (p->fp64_mode)
+      w64 = p->d.x64;
+    else
+      w32 = p->d.x32;
+    w_len = p->d.n;
+  }
+  int64_t* d_ptr = nullptr;
+  int32_t* d_idx = nullptr;
+  double *d_vals = nullptr, *d_lab = nullptr;
+  unsigned long long* d_good = nullptr;
+  unsigned long long good = 0;
+  cudaError_t e = cudaMalloc((void**)&d_ptr, sizeof(int64_t) * (n_test + 1));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&d_idx, sizeof(int32_t) * (nnz > 0 ? nnz : 1));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&d_vals, sizeof(double) * (nnz > 0 ? nnz : 1));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&d_lab, sizeof(double) * n_test);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&d_good, sizeof(unsigned long long));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_ptr, row_ptr, sizeof(int64_t) * (n_test + 1), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && nnz > 0)
+    e = cudaMemcpyAsync(d_idx, col_idx, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && nnz > 0)
+    e = cudaMemcpyAsync(d_vals, vals, sizeof(double) * nnz, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_lab, labels, sizeof(double) * n_test, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = launch_test_accuracy(n_test, d_ptr, d_idx, d_vals, d_lab, w64, w32, w_len, d_good, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&good, d_good, sizeof(good), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_ptr);
+  cudaFree(d_idx);
+  cudaFree(d_vals);
+  cudaFree(d_lab);
+  cudaFree(d_good);
+  if (e != cudaSuccess) return acdc_cuda_error(ctx, e, "acdc_test_accuracy");
+  *accuracy = (double)good / (double)n_test;
+  return ACDC_OK;
+}

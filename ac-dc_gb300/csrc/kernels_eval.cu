@@ -1247,6 +1247,41 @@ cudaError_t launch_gap(const EvalParams& p, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// Test-set 0-1 accuracy: one warp per test sample i, margin y_i x_i^T w in FP64
+// with w the weight vector (the SVM's w = r64 after a refresh, the logistic
+// loss's x); features at or beyond the weights' length count as zero.  Adds the
+// number of positive margins to *good.
+__global__ void k_test_accuracy(int64_t n_test, const int64_t* row_ptr, const int32_t* col_idx,
+                                const double* vals, const double* labels, const double* w64,
+                                const float* w32, int64_t w_len, unsigned long long* good) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  unsigned long long mine = 0;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n_test; i += warps) {
+    double s = 0;
+    for (int64_t e = row_ptr[i] + lane; e < row_ptr[i + 1]; e += 32) {
+      const int32_t f = col_idx[e];
+      if (f >= 0 && f < w_len) s += vals[e] * (w64 ? w64[f] : (double)w32[f]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(ACDC_FULL_MASK, s, o);
+    if (lane == 0 && labels[i] * s > 0.0) ++mine;
+  }
+  if (lane == 0 && mine) atomicAdd(good, mine);
+}
+
+cudaError_t launch_test_accuracy(int64_t n_test, const int64_t* row_ptr, const int32_t* col_idx,
+                                 const double* vals, const double* labels, const double* w64,
+                                 const float* w32, int64_t w_len, unsigned long long* good,
+                                 cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(good, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess || n_test == 0) return e;
+  const int64_t blocks = std::min<int64_t>((n_test + 7) / 8, 152 * 16);
+  k_test_accuracy<<<(unsigned)blocks, 256, 0, st>>>(n_test, row_ptr, col_idx, vals, labels, w64,
+                                                    w32, w_len, good);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_hot_set(const EvalParams& p, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(p.counters + CNT_HOT, 0, 2 * sizeof(unsigned long long), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(p.rowcnt, 0, sizeof(int32_t) * p.m, st);

@@ -232,6 +232,15 @@ int acdc_get_x(acdc_problem* p, double* x);        /* n entries (alpha for loss 
 int acdc_set_x(acdc_problem* p, const double* x);  /* warm start; refreshes r      */
 int acdc_get_residuals(acdc_problem* p, double* r);/* m entries: Ax-b or w, FP32 working copy */
 int acdc_get_stats(acdc_problem* p, acdc_stats* s);
+/* 0-1 accuracy of the current model on n_test held-out samples given as CSR
+ * (row_ptr[n_test + 1], 0-based feature indices, labels +-1): the fraction with
+ * label * (sample . weights) > 0.  Weights: the SVM dual's w, refreshed from the
+ * current alpha in FP64 (the test loop of MulticoreSVMDualLoss.h:95-112), or the
+ * logistic loss's x (MulticoreL2SquareRegLogisticLoss.h:65-81).  Features beyond
+ * the weights' length count as zero.  Losses 0 and 1: ACDC_EUNSUPPORTED. */
+int acdc_test_accuracy(acdc_problem* p, int64_t n_test, const int64_t* row_ptr,
+                       const int32_t* col_idx, const double* vals, const double* labels,
+                       double* accuracy);
 int acdc_reset_stats(acdc_problem* p);
 int acdc_synchronize(acdc_problem* p);
 

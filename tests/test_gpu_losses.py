@@ -103,3 +103,54 @@ def test_lambda_change_recomputes_the_step_sizes(ctx):
                                              max_epochs=50000)
     assert abs(r.eval.primal - ev_o["primal"]) <= 1e-6 * abs(ev_o["primal"])
     p.close()
+
+
+def split_rows(sv, n_train):
+    """First n_train samples of an SVM-generator instance, and the rest as CSR."""
+    cp = sv.col_ptr
+    train = acdc.Instance(acdc.LOSS_SVM_DUAL, sv.m, n_train, cp[:n_train + 1].copy(),
+                          sv.row_idx[:cp[n_train]].copy(), sv.vals[:cp[n_train]].copy(),
+                          sv.rhs[:n_train].copy(), sv.lam)
+    s = cp[n_train]
+    test = (cp[n_train:] - s, sv.row_idx[s:], sv.vals[s:], sv.rhs[n_train:])
+    return train, test
+
+
+def margins_accuracy(test, w):
+    rp, ci, va, y = test
+    s = np.array([va[rp[i]:rp[i + 1]] @ w[ci[rp[i]:rp[i + 1]]] for i in range(len(rp) - 1)])
+    return np.mean(y * s > 0)
+
+
+def test_test_set_accuracy_svm_and_logistic(ctx):
+    """acdc_test_accuracy: the SVM's w (from the FP64 refresh of alpha) or the
+    logistic model's x applied to held-out samples, against numpy margins on the
+    same model (FP32-rounded training values, as the device stores them)."""
+    sv = acdc.gen_svm(3000, 4000, nnz_median=30, nnz_sigma=0.6, w_star_nnz=200, lam=1e-3, seed=105)
+    train, test = split_rows(sv, 2400)
+    p = acdc.Problem(ctx, train, tau=64, warps_per_block=8, gap_target=1e-6, gap_relative=0,
+                     max_epochs=2000, seed=4)
+    assert p.solve().converged
+    a = p.get_x()
+    v32 = train.vals.astype(np.float32).astype(np.float64)
+    w = np.zeros(train.m)
+    for i in range(train.n):
+        s, e = train.col_ptr[i], train.col_ptr[i + 1]
+        w[train.row_idx[s:e]] += a[i] * train.rhs[i] * v32[s:e] / (train.lam * train.n)
+    acc = p.test_accuracy(*test)
+    want = margins_accuracy(test, w)
+    assert abs(acc - want) <= 1.0 / (len(test[0]) - 1)
+    assert acc > 0.7  # labels of a sparse w* with 5% flips: well above chance
+    p.close()
+
+    lg = acdc.logistic_from_svm(train, 1e-2)
+    q = acdc.Problem(ctx, lg, tau=32, warps_per_block=8, gap_target=1e-7, gap_relative=1,
+                     max_epochs=20000, seed=4)
+    assert q.solve().converged
+    acc = q.test_accuracy(*test)
+    assert abs(acc - margins_accuracy(test, q.get_x())) <= 1.0 / (len(test[0]) - 1)
+    assert acc > 0.7
+    with pytest.raises(acdc.AcdcError) as e:
+        acdc.Problem(ctx, ridge_instance(106)).test_accuracy(*test)
+    assert e.value.code == acdc.EUNSUPPORTED
+    q.close()
