@@ -16,17 +16,64 @@
 //    parse_LIB_SVM_data_get_size (cpp/src/svm/svm_parser.h:11-77): one sample
 //    per line, "label index:value ...", 1-based indices made 0-based, label 0
 //    mapped to -1.
+//
+// The text formats are parsed by several host threads: the file is cut into
+// pieces just after a separator (whitespace for number lists, a newline for
+// LIBSVM), each piece is scanned on its own thread, and the pieces' counts are
+// prefix-summed so that every thread writes its own part of the output.  The
+// result does not depend on the number of threads.
+#include <algorithm>
+#include <atomic>
 #include <cerrno>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/acdc_gpu.h"
 #include "../../include/acdc_host.h"
 
 namespace {
+
+std::atomic<int> g_threads{0};
+
+// Pieces a text of len bytes is cut into: the fixed count if one was set,
+// else one per MiB of text up to the hardware threads.
+int pieces_for(size_t len) {
+  const int set = g_threads.load();
+  if (set > 0) return set;
+  const unsigned hw = std::thread::hardware_concurrency();
+  const size_t by_size = len / ((size_t)1 << 20) + 1;
+  return (int)std::max<size_t>(1, std::min<size_t>(hw ? hw : 1, by_size));
+}
+
+bool is_space(char c) { return c == ' ' || c == '\n' || c == '\r' || c == '\t'; }
+bool is_newline(char c) { return c == '\n'; }
+
+// Cuts [0, len) into k ranges whose inner boundaries sit just after a
+// separator, so that no token (or line) is split; ranges may be empty.
+std::vector<size_t> cut_after(const std::string& text, int k, bool (*sep)(char)) {
+  std::vector<size_t> b((size_t)k + 1, text.size());
+  b[0] = 0;
+  for (int i = 1; i < k; ++i) {
+    size_t p = std::max(b[(size_t)i - 1], text.size() / (size_t)k * (size_t)i);
+    while (p < text.size() && !sep(text[p])) ++p;
+    b[(size_t)i] = p < text.size() ? p + 1 : text.size();
+  }
+  return b;
+}
+
+// Runs fn(i) for i in [0, k) on k threads (the calling thread takes i = 0).
+template <typename F>
+void run_pieces(int k, F fn) {
+  std::vector<std::thread> th;
+  th.reserve((size_t)k);
+  for (int i = 1; i < k; ++i) th.emplace_back(fn, i);
+  fn(0);
+  for (auto& t : th) t.join();
+}
 
 bool read_file(const std::string& path, std::string& out) {
   FILE* f = std::fopen(path.c_str(), "rb");
@@ -44,22 +91,42 @@ bool read_file(const std::string& path, std::string& out) {
   return got == (size_t)len;
 }
 
-// Parses every number of a whitespace-separated file; false on a bad token.
+// Numbers of [p, end), a range that ends just after whitespace or at the end
+// of the text; false on a bad token.
 template <typename T>
-bool parse_numbers(const std::string& text, std::vector<T>& out) {
-  out.clear();
-  const char* p = text.c_str();
-  const char* end = p + text.size();
+bool parse_range(const char* p, const char* end, std::vector<T>& out) {
   while (p < end) {
-    while (p < end && (*p == ' ' || *p == '\n' || *p == '\r' || *p == '\t')) ++p;
+    while (p < end && is_space(*p)) ++p;
     if (p >= end) break;
     char* q = nullptr;
     errno = 0;
     double v = std::strtod(p, &q);
-    if (q == p || errno == ERANGE) return false;
+    if (q == p || q > end || errno == ERANGE) return false;
     out.push_back((T)v);
     p = q;
   }
+  return true;
+}
+
+// Parses every number of a whitespace-separated file; false on a bad token.
+template <typename T>
+bool parse_numbers(const std::string& text, std::vector<T>& out) {
+  out.clear();
+  const int k = pieces_for(text.size());
+  const std::vector<size_t> b = cut_after(text, k, is_space);
+  std::vector<std::vector<T>> part((size_t)k);
+  std::vector<char> ok((size_t)k, 0);
+  const char* base = text.c_str();
+  run_pieces(k, [&](int i) {
+    ok[(size_t)i] = parse_range(base + b[(size_t)i], base + b[(size_t)i + 1], part[(size_t)i]);
+  });
+  size_t total = 0;
+  for (int i = 0; i < k; ++i) {
+    if (!ok[(size_t)i]) return false;
+    total += part[(size_t)i].size();
+  }
+  out.reserve(total);
+  for (auto& v : part) out.insert(out.end(), v.begin(), v.end());
   return true;
 }
 
@@ -138,11 +205,11 @@ struct LibsvmScan {
   int64_t n = 0, d = 0, nnz = 0;
 };
 
-// Walks the file; when out pointers are given also fills them.
-int walk_libsvm(const std::string& text, LibsvmScan& sc, int64_t* row_ptr, int32_t* col_idx,
-                double* vals, double* y) {
-  const char* p = text.c_str();
-  const char* end = p + text.size();
+// Walks the lines of [p, end) (a range of whole lines); when out pointers are
+// given also fills them, sample n0 + i and entry nnz0 + e of the range at
+// index i and e.
+int walk_libsvm(const char* p, const char* end, LibsvmScan& sc, int64_t n0, int64_t nnz0,
+                int64_t* row_ptr, int32_t* col_idx, double* vals, double* y) {
   int64_t n = 0, nnz = 0, d = 0;
   while (p < end) {
     const char* eol = (const char*)std::memchr(p, '\n', (size_t)(end - p));
@@ -152,11 +219,11 @@ int walk_libsvm(const std::string& text, LibsvmScan& sc, int64_t* row_ptr, int32
     if (q < eol && *q != '#') {
       char* r = nullptr;
       double label = std::strtod(q, &r);
-      if (r == q) return ACDC_EINVAL;
+      if (r == q || r > eol) return ACDC_EINVAL;
       q = r;
       if (row_ptr) {
-        row_ptr[n] = nnz;
-        y[n] = label == 0 ? -1.0 : label;
+        row_ptr[n0 + n] = nnz0 + nnz;
+        y[n0 + n] = label == 0 ? -1.0 : label;
       }
       for (;;) {
         while (q < eol && (*q == ' ' || *q == '\t' || *q == '\r')) ++q;
@@ -164,14 +231,16 @@ int walk_libsvm(const std::string& text, LibsvmScan& sc, int64_t* row_ptr, int32
         long long idx = std::strtoll(q, &r, 10);
         if (r == q || r >= eol || *r != ':' || idx < 1) return ACDC_EINVAL;
         q = r + 1;
+        // the value follows the colon directly (strtod would skip a line end)
+        if (q >= eol || *q == ' ' || *q == '\t' || *q == '\r') return ACDC_EINVAL;
         double v = std::strtod(q, &r);
-        if (r == q) return ACDC_EINVAL;
+        if (r == q || r > eol) return ACDC_EINVAL;
         q = r;
         if (idx > d) d = idx;
+        if (idx - 1 > INT32_MAX) return ACDC_EINVAL;
         if (col_idx) {
-          if (idx - 1 > INT32_MAX) return ACDC_EINVAL;
-          col_idx[nnz] = (int32_t)(idx - 1);
-          vals[nnz] = v;
+          col_idx[nnz0 + nnz] = (int32_t)(idx - 1);
+          vals[nnz0 + nnz] = v;
         }
         ++nnz;
       }
@@ -179,7 +248,6 @@ int walk_libsvm(const std::string& text, LibsvmScan& sc, int64_t* row_ptr, int32
     }
     p = eol + 1;
   }
-  if (row_ptr) row_ptr[n] = nnz;
   sc.n = n;
   sc.d = d;
   sc.nnz = nnz;
@@ -247,13 +315,57 @@ extern "C" int acdc_load_csc_binary(const char* prefix, const char* suffix, int3
   return ACDC_OK;
 }
 
+namespace {
+
+// LIBSVM in pieces of whole lines: per-piece sizes, then (when row_ptr is
+// given) each piece fills its samples and entries at the prefix sums.
+int scan_libsvm(const std::string& text, LibsvmScan& total, int64_t* row_ptr, int32_t* col_idx,
+                double* vals, double* y) {
+  const int k = pieces_for(text.size());
+  const std::vector<size_t> b = cut_after(text, k, is_newline);
+  const char* base = text.c_str();
+  std::vector<LibsvmScan> sc((size_t)k);
+  std::vector<int> rc((size_t)k, ACDC_OK);
+  run_pieces(k, [&](int i) {
+    rc[(size_t)i] = walk_libsvm(base + b[(size_t)i], base + b[(size_t)i + 1], sc[(size_t)i], 0, 0,
+                                nullptr, nullptr, nullptr, nullptr);
+  });
+  std::vector<int64_t> n0((size_t)k + 1, 0), z0((size_t)k + 1, 0);
+  total = LibsvmScan();
+  for (int i = 0; i < k; ++i) {
+    if (rc[(size_t)i]) return rc[(size_t)i];
+    n0[(size_t)i + 1] = n0[(size_t)i] + sc[(size_t)i].n;
+    z0[(size_t)i + 1] = z0[(size_t)i] + sc[(size_t)i].nnz;
+    total.d = std::max(total.d, sc[(size_t)i].d);
+  }
+  total.n = n0[(size_t)k];
+  total.nnz = z0[(size_t)k];
+  if (!row_ptr) return ACDC_OK;
+  if (total.nnz > 0 && (!col_idx || !vals)) return ACDC_EINVAL;
+  run_pieces(k, [&](int i) {
+    LibsvmScan again;
+    rc[(size_t)i] = walk_libsvm(base + b[(size_t)i], base + b[(size_t)i + 1], again, n0[(size_t)i],
+                                z0[(size_t)i], row_ptr, col_idx, vals, y);
+  });
+  for (int i = 0; i < k; ++i)
+    if (rc[(size_t)i]) return rc[(size_t)i];
+  row_ptr[total.n] = total.nnz;
+  return ACDC_OK;
+}
+
+}  // namespace
+
+extern "C" int acdc_host_threads(int32_t threads) {
+  return g_threads.exchange(threads > 0 ? threads : 0);
+}
+
 extern "C" int acdc_load_libsvm_sizes(const char* path, int64_t* n_samples, int64_t* d,
                                       int64_t* nnz) {
   if (!path || !n_samples || !d || !nnz) return ACDC_EINVAL;
   std::string text;
   if (!read_file(path, text)) return ACDC_EINVAL;
   LibsvmScan sc;
-  int rc = walk_libsvm(text, sc, nullptr, nullptr, nullptr, nullptr);
+  int rc = scan_libsvm(text, sc, nullptr, nullptr, nullptr, nullptr);
   if (rc) return rc;
   *n_samples = sc.n;
   *d = sc.d;
@@ -267,8 +379,5 @@ extern "C" int acdc_load_libsvm(const char* path, int64_t* row_ptr, int32_t* col
   std::string text;
   if (!read_file(path, text)) return ACDC_EINVAL;
   LibsvmScan sc;
-  int rc = walk_libsvm(text, sc, nullptr, nullptr, nullptr, nullptr);
-  if (rc) return rc;
-  if (sc.nnz > 0 && (!col_idx || !vals)) return ACDC_EINVAL;
-  return walk_libsvm(text, sc, row_ptr, col_idx, vals, y);
+  return scan_libsvm(text, sc, row_ptr, col_idx, vals, y);
 }

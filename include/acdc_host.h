@@ -129,6 +129,14 @@ int acdc_load_csc_binary(const char* prefix, const char* suffix, int32_t rank,
                          const char* vector_file, int64_t local_n, int64_t* col_ptr,
                          int32_t* row_idx, double* vals, double* b);
 
+/* Host threads of the text loaders (acdc_load_csc_text*, the offsets file of
+ * acdc_load_csc_binary*, acdc_load_libsvm*): > 0 cuts every text into that
+ * many pieces, each parsed on its own thread; 0 (the default) uses one piece
+ * per MiB of text, up to the hardware threads.  The loaded arrays do not
+ * depend on it.  Returns the previous setting.  The reference's readers
+ * (file_reader.h, distributed_instances_loader.h) parse on one thread. */
+int acdc_host_threads(int32_t threads);
+
 /* LIBSVM text (label index:value ...), 1-based feature indices mapped to
  * 0-based, labels 0 mapped to -1 for two classes: the reader
  * loadDistributedSparseSVMRowData (cpp/src/utils/distributed_instances_loader.h:68-193,

@@ -197,6 +197,77 @@ def test_libsvm_loader(tmp_path):
         acdc.load_libsvm(str(p), 0.1)
 
 
+def libsvm_reference_parse(text):
+    """LIBSVM parsed line by line in Python: (row_ptr, col_idx, vals, y, d)."""
+    rp, ci, va, y, d = [0], [], [], [], 0
+    for line in text.split("\n"):
+        t = line.strip(" \t\r")
+        if not t or t.startswith("#"):
+            continue
+        toks = t.split()
+        y.append(-1.0 if float(toks[0]) == 0 else float(toks[0]))
+        for tok in toks[1:]:
+            i, v = tok.split(":")
+            ci.append(int(i) - 1)
+            va.append(float(v))
+            d = max(d, int(i))
+        rp.append(len(ci))
+    return np.array(rp), np.array(ci), np.array(va), np.array(y), d
+
+
+@pytest.mark.parametrize("threads", [1, 2, 3, 7, 64])
+def test_loaders_do_not_depend_on_threads(tmp_path, threads):
+    """Every text loader cuts its file into pieces at separators and parses them
+    on separate threads: the arrays match a line-by-line Python parse and the
+    one-thread result for any number of pieces, including more pieces than lines
+    and files without a final newline."""
+    rng = np.random.default_rng(threads)
+    lines = []
+    for i in range(300):
+        k = int(rng.integers(0, 12))
+        feats = np.sort(rng.choice(5000, size=k, replace=False)) + 1
+        lab = ["+1", "-1", "0"][i % 3]
+        body = " ".join("%d:%.17g" % (f, rng.normal()) for f in feats)
+        lines.append(("%s %s" % (lab, body)).rstrip() + (" \r" if i % 17 == 0 else ""))
+        if i % 41 == 0:
+            lines.append("")  # blank line
+        if i % 53 == 0:
+            lines.append("# comment 1:2")
+    text = "\n".join(lines)  # no final newline
+    p = tmp_path / "d.svm"
+    p.write_text(text)
+    want = libsvm_reference_parse(text)
+    old = acdc.host_threads(threads)
+    try:
+        got = acdc.load_libsvm(str(p), 0.1)
+        assert np.array_equal(got.col_ptr, want[0]) and np.array_equal(got.row_idx, want[1])
+        assert np.array_equal(got.vals, want[2]) and np.array_equal(got.rhs, want[3])
+        assert got.m == want[4]
+        inst = acdc.gen_lasso(70, 90, nnz_per_col=4, n_star=5, seed=threads)
+        pre = str(tmp_path / "A")
+        with open(pre + "_values.txt", "w") as f:  # mixed separators, no final newline
+            f.write("\t".join("%.17g" % v for v in inst.vals[:50]) + "\n\n  ")
+            f.write("  ".join("%.17g" % v for v in inst.vals[50:]))
+        np.savetxt(pre + "_colPtr.txt", inst.col_ptr, fmt="%d")
+        np.savetxt(pre + "_rowIdx.txt", inst.row_idx, fmt="%d")
+        np.savetxt(str(tmp_path / "b.txt"), inst.rhs, fmt="%.17g")
+        c = acdc.load_csc_text(pre, str(tmp_path / "b.txt"), 0.5)
+        assert np.array_equal(c.col_ptr, inst.col_ptr) and np.array_equal(c.row_idx, inst.row_idx)
+        assert np.array_equal(c.vals, inst.vals) and np.array_equal(c.rhs, inst.rhs)
+    finally:
+        acdc.host_threads(old)
+
+
+def test_libsvm_value_must_follow_the_colon(tmp_path):
+    p = tmp_path / "d.svm"
+    p.write_text("+1 1:0.5 3:\n-1 2:2\n")  # a value may not come from the next line
+    with pytest.raises(acdc.AcdcError):
+        acdc.load_libsvm(str(p), 0.1)
+    p.write_text("+1 1: 0.5\n")
+    with pytest.raises(acdc.AcdcError):
+        acdc.load_libsvm(str(p), 0.1)
+
+
 def test_host_omega_matches_oracle():
     import oracle
     inst = acdc.gen_lasso(300, 900, nnz_per_col=9, n_star=5, seed=12)
