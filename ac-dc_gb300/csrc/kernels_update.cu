@@ -46,6 +46,7 @@ struct WarpRing {
   int4 idx[kDS][32];
   int4 meta[kMS];
   int32_t coords[kChunk];  // coordinates of the current chunk of updates
+  float scale[kChunk];     // their list step scales (0: the tier's li_scale)
 };
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -77,18 +78,24 @@ __device__ __forceinline__ T column_sum(T v, uint32_t len) {
 
 // Coordinate of update k.  With shrinking, word 2 picks the tier (hot set below
 // hot_q32, active set below shrink_q32, else all coordinates) and word 3 the
-// entry of the list; a hot-set draw is returned with bit 31 set.
+// entry of the list; a hot-set draw is returned with bit 31 set.  sc receives
+// the list entry's step scale where the tier has per-entry scales, else 0.
 constexpr int32_t kHotBit = (int32_t)0x80000000u;
 constexpr int32_t kCoordMask = 0x7fffffff;
 
 __device__ __forceinline__ int32_t draw_coord(const UpdateParams& p, uint64_t k,
-                                              int32_t active_cnt, int32_t hot_cnt) {
+                                              int32_t active_cnt, int32_t hot_cnt, float& sc) {
   acdc_u32x4 o = acdc_philox4x32_10((uint32_t)k, (uint32_t)(k >> 32), ACDC_STREAM_SAMPLER, 0u,
                                     (uint32_t)p.seed, (uint32_t)(p.seed >> 32));
+  sc = 0.f;
   if (active_cnt > 0 && o.v[2] < p.shrink_q32) {
-    if (hot_cnt > 0 && o.v[2] < p.hot_q32)
-      return __ldg(p.hot + __umulhi(o.v[3], (uint32_t)hot_cnt)) | kHotBit;
-    uint32_t t = __umulhi(o.v[3], (uint32_t)active_cnt);
+    if (hot_cnt > 0 && o.v[2] < p.hot_q32) {
+      const uint32_t t = __umulhi(o.v[3], (uint32_t)hot_cnt);
+      if (p.hot_scale) sc = __ldg(p.hot_scale + t);
+      return __ldg(p.hot + t) | kHotBit;
+    }
+    const uint32_t t = __umulhi(o.v[3], (uint32_t)active_cnt);
+    if (p.active_scale) sc = __ldg(p.active_scale + t);
     return __ldg(p.active + t);
   }
   uint64_t u = ((uint64_t)o.v[0] << 32) | (uint64_t)o.v[1];
@@ -215,7 +222,9 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
 #pragma unroll
     for (int q = 0; q < kChunk / 32; ++q) {
       const int s = 32 * q + lane;
-      w.coords[s] = s < cnt ? draw_coord(p, k_base + base + (uint64_t)s, active_cnt, hot_cnt) : 0;
+      float sc = 0.f;
+      w.coords[s] = s < cnt ? draw_coord(p, k_base + base + (uint64_t)s, active_cnt, hot_cnt, sc) : 0;
+      w.scale[s] = sc;
     }
     __syncwarp();
 
@@ -277,7 +286,8 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
       }
       const T g = column_sum<T>(acc, len);
 
-      const T li = (T)__int_as_float(mt.z) * (cj < 0 ? li_scale_hot : li_scale);
+      const float sc = w.scale[s];
+      const T li = (T)__int_as_float(mt.z) * (sc != 0.f ? (T)sc : (cj < 0 ? li_scale_hot : li_scale));
       T delta, coef;
       if (LOSS == ACDC_LOSS_L1_SQUARE) {
         const T z = xj - li * g;

@@ -103,6 +103,9 @@ def parse_args():
     ap.add_argument("--serve-requests", type=int, default=128,
                     help="requests of the serving sample (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=1000.0)
+    ap.add_argument("--row-eso", type=int, default=1, choices=[0, 1],
+                    help="step sizes of the active and hot tiers: 1 per-column row-wise ESO "
+                         "weights, 0 one ESO parameter per tier")
     ap.add_argument("--probe-launches", action="store_true",
                     help="profiling aid: run one uniform-draw update launch (refresh_every "
                          "epochs) and one active-set launch (active_passes |A|/q updates) on "
@@ -451,6 +454,7 @@ def run_ours(args, w):
     inst = generate(w, pinned=True)
     t_gen = time.time() - t_gen
     s = settings_for(w)
+    s.row_eso = args.row_eso
     ctx = acdc.Context(local)
     p = acdc.Problem(ctx, inst, s)
     info = p.info()
@@ -566,7 +570,7 @@ def run_ours(args, w):
     else:
         solver_keys = {"gap_target_relative": w["gap"], "q_shrinking": 0.9,
                        "tau_active": w["tau_active"], "active_passes": w["active_passes"],
-                       "screened_eval": 1, "hot_threshold": 0.1}
+                       "screened_eval": 1, "hot_threshold": 0.1, "row_eso": args.row_eso}
     if rank == 0:
         line = {
             "metric": METRICS[w.get("loss", "lasso")], "value": value, "unit": "s", "n_gpus": world,

@@ -126,7 +126,9 @@ def test_test_set_accuracy_svm_and_logistic(ctx):
     """acdc_test_accuracy: the SVM's w (from the FP64 refresh of alpha) or the
     logistic model's x applied to held-out samples, against numpy margins on the
     same model (FP32-rounded training values, as the device stores them)."""
-    sv = acdc.gen_svm(3000, 4000, nnz_median=30, nnz_sigma=0.6, w_star_nnz=200, lam=1e-3, seed=105)
+    # 800 features, 2400 training samples: the oracle's exact solutions reach
+    # 0.78 held-out accuracy on both losses (4000 features only reach 0.6)
+    sv = acdc.gen_svm(3000, 800, nnz_median=60, nnz_sigma=0.6, w_star_nnz=80, lam=1e-3, seed=105)
     train, test = split_rows(sv, 2400)
     p = acdc.Problem(ctx, train, tau=64, warps_per_block=8, gap_target=1e-6, gap_relative=0,
                      max_epochs=2000, seed=4)
