@@ -30,8 +30,7 @@ class Settings(C.Structure):
                 ("max_epochs", I32), ("use_shrinking", I32), ("shrinking_starting_iter", I32),
                 ("shrinking_probability", D), ("shrink_eps", D), ("precision", I32),
                 ("tau_active", I32), ("polish_rel_gap", D), ("active_passes", I32),
-                ("screened_eval", I32), ("row_eso", I32), ("reserved", I32),
-                ("hot_threshold", D)]
+                ("screened_eval", I32), ("reserved", I32 * 2), ("hot_threshold", D)]
 
 
 class Eval(C.Structure):
@@ -151,7 +150,6 @@ def gpu_lib():
         L.acdc_debug_sample.argtypes = [VP, U64, U64, U64, I64, VP]
         L.acdc_test_accuracy.argtypes = [VP, I64, VP, VP, VP, VP, C.POINTER(D)]
         L.acdc_debug_sample_noalloc.argtypes = [VP, U64, U64, U64, I64, VP]
-        L.acdc_debug_tier.argtypes = [VP, I32, I64, VP, VP, VP]
         L.acdc_batch_solve_path.argtypes = [VP, I32, VP, VP, C.POINTER(BatchOptions), VP, VP]
         L.acdc_server_create.argtypes = [VP, C.POINTER(ServerOptions), C.POINTER(VP)]
         L.acdc_server_submit.argtypes = [VP, C.POINTER(Request), C.POINTER(I64)]
@@ -470,16 +468,6 @@ class Problem:
 
     def recompute_residuals(self):
         self.ctx.check(self.L.acdc_recompute_residuals(self.h))
-
-    def debug_tier(self, tier):
-        """acdc_debug_tier: (list, step scales) of the active (0) or hot (1) tier."""
-        cnt = I64()
-        self.ctx.check(self.L.acdc_debug_tier(self.h, tier, 0, None, None, C.byref(cnt)))
-        lst = np.zeros(max(cnt.value, 1), np.int32)
-        sc = np.zeros(max(cnt.value, 1), np.float32)
-        self.ctx.check(self.L.acdc_debug_tier(self.h, tier, cnt.value, _ptr(lst), _ptr(sc),
-                                              C.byref(cnt)))
-        return lst[:cnt.value], sc[:cnt.value]
 
     def evaluate(self):
         e = Eval()

@@ -82,10 +82,6 @@ struct UpdateParams {
   uint32_t hot_q32 = 0;         // probability of a hot-set draw (part of shrink_q32)
   const int32_t* hot = nullptr;  // hot list (length in counters[CNT_HOT])
   double li_scale_hot = 1.0;     // step scale of hot-set draws
-  // Per-entry step scales of the active and hot lists (row-wise ESO); null:
-  // li_scale and li_scale_hot apply to every draw of the tier.
-  const float* active_scale = nullptr;
-  const float* hot_scale = nullptr;
   int32_t n_warps;      // tau
   int32_t loss;
   int32_t fp64;         // 1: x and r in FP64 (x64, r64)
@@ -196,8 +192,6 @@ struct DevProblem {
   double* r_ref = nullptr;  // m doubles: residual of the last full evaluation (Lasso)
   float* viol = nullptr;    // n floats: KKT violation of active[t] (Lasso)
   int32_t* hot = nullptr;   // n ints: hot list (Lasso)
-  float* active_scale = nullptr;  // n floats: step scale of active[t] (row-wise ESO)
-  float* hot_scale = nullptr;     // n floats: step scale of hot[t] (Lasso)
   uint8_t* row_flag = nullptr;  // m bytes: rows of the hot columns (Lasso)
   double* part = nullptr;
   double* eval_out = nullptr;
@@ -292,20 +286,6 @@ cudaError_t launch_test_accuracy(int64_t n_test, const int64_t* row_ptr, const i
                                  cudaStream_t st);
 // Hot list from the violations of the last evaluation; zeroes CNT_HOT first.
 cudaError_t launch_hot_set(const EvalParams& p, cudaStream_t st);
-// Row-wise ESO step scales of a tier's list (the active or the hot list), from
-// rowcnt[i] = w_i, the number of the tier's columns with an entry in row i:
-//   scale[t] = min(1, beta ||a_j||^2 / sum_i beta_i A_ij^2),  j = list[t],
-//   beta_i = 1 + (w_i - 1)(t_draws - 1) / max(1, c - 1),
-// c = *count (capped at n), t_draws = draws, or min(draws, c) when
-// cap_by_count.  The stored Li = 1/(beta ||a_j||^2) times scale[t] is
-// 1/max(beta ||a_j||^2, v_j) with v_j the ESO weight of column j for t_draws
-// draws from the c columns (Fercoq & Richtarik, "Accelerated, parallel and
-// proximal coordinate descent", SIAM J. Optim. 25(4), 2015: the per-coordinate
-// ESO of the tau-nice sampling).
-cudaError_t launch_tier_scale(const int4* meta, const float* vals, const int32_t* idx,
-                              const int32_t* list, const unsigned long long* count, int64_t n,
-                              const int32_t* rowcnt, double draws, int cap_by_count, double beta,
-                              float* scale, cudaStream_t st);
 cudaError_t launch_debug_sample(uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
                                 int64_t* out, cudaStream_t st);
 // Batched round: update, refresh, gap and control kernels over every live slot.

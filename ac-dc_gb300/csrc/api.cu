@@ -61,7 +61,6 @@ extern "C" void acdc_settings_default(acdc_settings* s) {
   s->polish_rel_gap = 1e-5;
   s->screened_eval = 1;
   s->hot_threshold = 0.1;
-  s->row_eso = 1;
 }
 
 // ---- context ----
@@ -120,8 +119,6 @@ void free_problem_buffers(DevProblem& d) {
   cudaFree(d.rhs64);
   cudaFree(d.col_sq);
   cudaFree(d.active);
-  cudaFree(d.active_scale);
-  cudaFree(d.hot_scale);
   cudaFree(d.xbuf);
   cudaFree(d.x64);
   cudaFree(d.rowcnt);
@@ -230,9 +227,7 @@ UpdateParams update_params(acdc_problem* p, uint64_t count, bool shrink) {
     u.hot_q32 = (uint32_t)std::min(4294967295.0, p->hot_q * 4294967296.0);
     if (u.hot_q32 > u.shrink_q32) u.hot_q32 = u.shrink_q32;
     u.li_scale_hot = p->li_scale_hot;
-    if (p->s.row_eso) u.hot_scale = p->d.hot_scale;
   }
-  if (shrink && u.shrink_q32 && p->s.row_eso) u.active_scale = p->d.active_scale;
   return u;
 }
 
@@ -261,7 +256,7 @@ int apply_settings(acdc_problem* p, const acdc_settings* s) {
       s->max_epochs < 0 || !(s->gap_target >= 0) || s->shrinking_probability < 0 ||
       s->shrinking_probability > 1 || s->shrink_eps < 0 || s->shrink_eps >= 1 ||
       s->precision < ACDC_PREC_AUTO || s->precision > ACDC_PREC_FP64 || !(s->polish_rel_gap >= 0) ||
-      !(s->hot_threshold >= 0) || s->row_eso < 0 || s->row_eso > 1)
+      !(s->hot_threshold >= 0))
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid settings value");
   p->s = *s;
   // q-shrinking and its screened evaluations cover losses 0 and 2 only.
@@ -370,7 +365,6 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
   STEP(dalloc(&d.rhs64, rhs_len, &d.bytes));
   STEP(dalloc(&d.col_sq, n, &d.bytes));
   STEP(dalloc(&d.active, n, &d.bytes));
-  STEP(dalloc(&d.active_scale, n, &d.bytes));
   STEP(dalloc(&d.xbuf, n, &d.bytes));
   STEP(dalloc(&d.x64, n, &d.bytes));
   STEP(dalloc(&d.rowcnt, m, &d.bytes));
@@ -379,7 +373,6 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
     STEP(dalloc(&d.r_ref, m, &d.bytes));
     STEP(dalloc(&d.viol, n, &d.bytes));
     STEP(dalloc(&d.hot, n, &d.bytes));
-    STEP(dalloc(&d.hot_scale, n, &d.bytes));
     STEP(dalloc(&d.row_flag, m, &d.bytes));
     STEP(cudaMemsetAsync(d.row_flag, 0, m, st));
   }
@@ -579,24 +572,9 @@ int evaluate_impl(acdc_problem* p, acdc_eval* out, float* ms, bool screened = fa
   ACDC_CK(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
   ACDC_CK(ctx, launch_refresh(e, ctx->stream));
   ACDC_CK(ctx, launch_gap(e, ctx->stream));
-  // Draws in flight per tier while shrinking: q tau_active on the active list,
-  // min(q tau_active / 2, |H|) on the hot list.
-  const double tau_shrink = p->s.tau_active > 0 ? p->s.tau_active : p->s.tau;
-  const double tau_a = std::max(1.0, p->s.shrinking_probability * tau_shrink);
-  if (build_active) {
-    ACDC_CK(ctx, launch_active_omega(e, p->d.rowcnt, ctx->stream));
-    ACDC_CK(ctx, launch_tier_scale(p->d.meta, p->d.vals, p->d.idx, p->d.active,
-                                   p->d.counters + CNT_ACTIVE, p->d.n, p->d.rowcnt, tau_a, 0,
-                                   p->beta, p->d.active_scale, ctx->stream));
-  }
+  if (build_active) ACDC_CK(ctx, launch_active_omega(e, p->d.rowcnt, ctx->stream));
   const bool hot = e.viol != nullptr;
-  if (hot) {
-    ACDC_CK(ctx, launch_hot_set(e, ctx->stream));
-    ACDC_CK(ctx, launch_tier_scale(p->d.meta, p->d.vals, p->d.idx, p->d.hot,
-                                   p->d.counters + CNT_HOT, p->d.n, p->d.rowcnt,
-                                   0.5 * p->s.shrinking_probability * tau_shrink, 1, p->beta,
-                                   p->d.hot_scale, ctx->stream));
-  }
+  if (hot) ACDC_CK(ctx, launch_hot_set(e, ctx->stream));
   ACDC_CK(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
   ACDC_CK(ctx, cudaMemcpyAsync(p->h_eval, p->d.eval_out, sizeof(double) * 16,
                                cudaMemcpyDeviceToHost, ctx->stream));
@@ -615,6 +593,8 @@ int evaluate_impl(acdc_problem* p, acdc_eval* out, float* ms, bool screened = fa
     // |A| active columns, whose rows hold at most omega_A of them.
     const double a = p->h_eval[9];
     p->omega_active = std::max<int64_t>(1, (int64_t)p->h_counters[CNT_OMEGA_ACTIVE]);
+    const double tau_shrink = p->s.tau_active > 0 ? p->s.tau_active : p->s.tau;
+    const double tau_a = std::max(1.0, p->s.shrinking_probability * tau_shrink);
     const double beta_a =
         a > 1 ? 1.0 + ((double)p->omega_active - 1.0) * (tau_a - 1.0) / (a - 1.0) : 1.0;
     p->li_scale_shrink = p->beta / std::max(p->beta, beta_a);
@@ -627,6 +607,7 @@ int evaluate_impl(acdc_problem* p, acdc_eval* out, float* ms, bool screened = fa
     // active-set draws; ESO over the hot columns, whose rows hold at most
     // omega_H of them.
     const int64_t h = std::min<int64_t>((int64_t)p->h_counters[CNT_HOT], p->d.n);
+    const double tau_shrink = p->s.tau_active > 0 ? p->s.tau_active : p->s.tau;
     if (h > 0) {
       p->hot_count = h;
       p->hot_q = std::min(0.5 * p->s.shrinking_probability, (double)h / tau_shrink);
@@ -808,29 +789,6 @@ extern "C" int acdc_debug_sample(acdc_ctx* ctx, uint64_t seed, uint64_t k0, uint
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   cudaFree(d);
   if (e != cudaSuccess) return acdc_cuda_error(ctx, e, "acdc_debug_sample");
-  return ACDC_OK;
-}
-
-extern "C" int acdc_debug_tier(acdc_problem* p, int32_t tier, int64_t cap, int32_t* list,
-                               float* scale, int64_t* count) {
-  if (!p || !count || cap < 0 || (cap > 0 && (!list || !scale)) || tier < 0 || tier > 1)
-    return ACDC_EINVAL;
-  acdc_ctx* ctx = p->ctx;
-  const DevProblem& d = p->d;
-  const int32_t* dl = tier == 0 ? d.active : d.hot;
-  const float* ds = tier == 0 ? d.active_scale : d.hot_scale;
-  if (!dl || !ds) return acdc_set_error(ctx, ACDC_EUNSUPPORTED, "no such list for this loss");
-  unsigned long long c = 0;
-  ACDC_CK(ctx, cudaMemcpyAsync(&c, d.counters + (tier == 0 ? CNT_ACTIVE : CNT_HOT), sizeof(c),
-                               cudaMemcpyDeviceToHost, ctx->stream));
-  ACDC_CK(ctx, cudaStreamSynchronize(ctx->stream));
-  *count = (int64_t)std::min<unsigned long long>(c, (unsigned long long)d.n);
-  const int64_t k = std::min<int64_t>(*count, cap);
-  if (k > 0) {
-    ACDC_CK(ctx, cudaMemcpyAsync(list, dl, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, ctx->stream));
-    ACDC_CK(ctx, cudaMemcpyAsync(scale, ds, sizeof(float) * k, cudaMemcpyDeviceToHost, ctx->stream));
-    ACDC_CK(ctx, cudaStreamSynchronize(ctx->stream));
-  }
   return ACDC_OK;
 }
 

@@ -1293,72 +1293,6 @@ cudaError_t launch_hot_set(const EvalParams& p, cudaStream_t st) {
   return e;
 }
 
-// Row-wise ESO step scales of a tier's list (declared in acdc_internal.cuh).
-// Lane l of warp w takes entry 32Wk + Wl + w, so the long columns that sit
-// together in the list spread over the warps; a lane sums a short column
-// alone, the warp the long ones.
-__global__ void k_tier_scale(const int4* __restrict__ meta, const float* __restrict__ vals,
-                             const int32_t* __restrict__ idx, const int32_t* __restrict__ list,
-                             const unsigned long long* count, int64_t n,
-                             const int32_t* __restrict__ rowcnt, double draws, int cap_by_count,
-                             double beta, float* __restrict__ scale) {
-  const int lane = threadIdx.x & 31;
-  const int64_t cnt = (int64_t)min(*count, (unsigned long long)n);
-  if (cnt <= 0) return;
-  const double t_draws = cap_by_count ? fmin(draws, (double)cnt) : draws;
-  const double f = cnt > 1 && t_draws > 1.0 ? (t_draws - 1.0) / ((double)cnt - 1.0) : 0.0;
-  const int64_t step = (int64_t)gridDim.x * blockDim.x;
-  const int64_t nw = step >> 5, gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  for (int64_t base = 0; base < cnt; base += step) {
-    const int64_t t = base + lane * nw + gw;
-    const bool valid = t < cnt;
-    const int4 mt = valid ? meta[list[t]] : make_int4(0, 0, 0, 0);
-    const int64_t start = (int64_t)(uint32_t)mt.x << 2;
-    double s2 = 0.0, v2 = 0.0;
-    if (valid && mt.y <= kLaneLen) {
-      for (int32_t e = 0; e < mt.y; ++e) {
-        const double a = (double)vals[start + e];
-        const double w = (double)max(1, rowcnt[idx[start + e]]);
-        s2 += a * a;
-        v2 += a * a * (1.0 + (w - 1.0) * f);
-      }
-    }
-    unsigned longs = __ballot_sync(ACDC_FULL_MASK, valid && mt.y > kLaneLen);
-    while (longs) {
-      const int src = __ffs(longs) - 1;
-      longs &= longs - 1;
-      const int64_t s0 = (int64_t)(uint32_t)__shfl_sync(ACDC_FULL_MASK, mt.x, src) << 2;
-      const int32_t len = __shfl_sync(ACDC_FULL_MASK, mt.y, src);
-      double ls = 0.0, lv = 0.0;
-      for (int32_t e = lane; e < len; e += 32) {
-        const double a = (double)vals[s0 + e];
-        const double w = (double)max(1, rowcnt[idx[s0 + e]]);
-        ls += a * a;
-        lv += a * a * (1.0 + (w - 1.0) * f);
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        ls += __shfl_xor_sync(ACDC_FULL_MASK, ls, o);
-        lv += __shfl_xor_sync(ACDC_FULL_MASK, lv, o);
-      }
-      if (lane == src) {
-        s2 = ls;
-        v2 = lv;
-      }
-    }
-    if (valid) scale[t] = v2 > 0.0 ? (float)fmin(1.0, beta * s2 / v2) : 1.0f;
-  }
-}
-
-cudaError_t launch_tier_scale(const int4* meta, const float* vals, const int32_t* idx,
-                              const int32_t* list, const unsigned long long* count, int64_t n,
-                              const int32_t* rowcnt, double draws, int cap_by_count, double beta,
-                              float* scale, cudaStream_t st) {
-  k_tier_scale<<<152 * 4, 256, 0, st>>>(meta, vals, idx, list, count, n, rowcnt, draws,
-                                        cap_by_count, beta, scale);
-  return cudaGetLastError();
-}
-
 // ---- batched rounds ----
 namespace {
 

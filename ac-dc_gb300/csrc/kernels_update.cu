@@ -16,7 +16,7 @@
 //   x_j   += delta;  r += c delta a_j                 (red.global.add)
 // with Li = 1/(beta ||a_j||^2), beta the ESO parameter for tau.
 //
-// Memory pipeline.  The column metadata of update s + 2D and the first 128
+// Memory pipeline.  The column metadata of update s + 2D + 1 and the first 128
 // entries (values and row indices) of update s + D are copied into the warp's
 // shared-memory ring with cp.async while update s runs: lane l copies entries
 // 4l..4l+3 as one 16-byte transfer of values and one of indices (the device
@@ -35,10 +35,12 @@
 namespace {
 
 constexpr int kChunk = 128;          // updates taken from the work counter at a time
-constexpr int kD = 4;                // entry copies in flight per warp
+constexpr int kD = 3;                // entry copies in flight per warp
 constexpr int kDS = kD + 1;          // entry slots (the slot being written is never the one read)
-constexpr int kDM = 2 * kD;          // metadata prefetch distance
+constexpr int kDM = 2 * kD + 1;      // metadata prefetch distance
 constexpr int kMS = kDM + 1;         // metadata slots
+static_assert((kDS & (kDS - 1)) == 0 && (kMS & (kMS - 1)) == 0,
+              "ring slots are taken modulo a power of two");
 constexpr int kMaxWarps = 8;         // warps per block
 
 struct WarpRing {
@@ -46,7 +48,6 @@ struct WarpRing {
   int4 idx[kDS][32];
   int4 meta[kMS];
   int32_t coords[kChunk];  // coordinates of the current chunk of updates
-  float scale[kChunk];     // their list step scales (0: the tier's li_scale)
 };
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -78,24 +79,18 @@ __device__ __forceinline__ T column_sum(T v, uint32_t len) {
 
 // Coordinate of update k.  With shrinking, word 2 picks the tier (hot set below
 // hot_q32, active set below shrink_q32, else all coordinates) and word 3 the
-// entry of the list; a hot-set draw is returned with bit 31 set.  sc receives
-// the list entry's step scale where the tier has per-entry scales, else 0.
+// entry of the list; a hot-set draw is returned with bit 31 set.
 constexpr int32_t kHotBit = (int32_t)0x80000000u;
 constexpr int32_t kCoordMask = 0x7fffffff;
 
 __device__ __forceinline__ int32_t draw_coord(const UpdateParams& p, uint64_t k,
-                                              int32_t active_cnt, int32_t hot_cnt, float& sc) {
+                                              int32_t active_cnt, int32_t hot_cnt) {
   acdc_u32x4 o = acdc_philox4x32_10((uint32_t)k, (uint32_t)(k >> 32), ACDC_STREAM_SAMPLER, 0u,
                                     (uint32_t)p.seed, (uint32_t)(p.seed >> 32));
-  sc = 0.f;
   if (active_cnt > 0 && o.v[2] < p.shrink_q32) {
-    if (hot_cnt > 0 && o.v[2] < p.hot_q32) {
-      const uint32_t t = __umulhi(o.v[3], (uint32_t)hot_cnt);
-      if (p.hot_scale) sc = __ldg(p.hot_scale + t);
-      return __ldg(p.hot + t) | kHotBit;
-    }
-    const uint32_t t = __umulhi(o.v[3], (uint32_t)active_cnt);
-    if (p.active_scale) sc = __ldg(p.active_scale + t);
+    if (hot_cnt > 0 && o.v[2] < p.hot_q32)
+      return __ldg(p.hot + __umulhi(o.v[3], (uint32_t)hot_cnt)) | kHotBit;
+    uint32_t t = __umulhi(o.v[3], (uint32_t)active_cnt);
     return __ldg(p.active + t);
   }
   uint64_t u = ((uint64_t)o.v[0] << 32) | (uint64_t)o.v[1];
@@ -163,6 +158,17 @@ __device__ __forceinline__ T gather_dot_head(const T* r, const Chunk& c, uint32_
   return a;
 }
 
+// The same for the first chunk, whose lanes past the column may hold stale
+// ring contents: only entries below len are written.
+template <typename T>
+__device__ __forceinline__ void scatter_head(T* r, const Chunk& c, T coef, uint32_t e0,
+                                             uint32_t len) {
+  if (e0 < len) atomicAdd(r + c.i.x, coef * (T)c.v.x);
+  if (e0 + 1u < len) atomicAdd(r + c.i.y, coef * (T)c.v.y);
+  if (e0 + 2u < len) atomicAdd(r + c.i.z, coef * (T)c.v.z);
+  if (e0 + 3u < len) atomicAdd(r + c.i.w, coef * (T)c.v.w);
+}
+
 template <typename T>
 __device__ __forceinline__ void scatter(T* r, const Chunk& c, T coef, bool live) {
   if (!live) return;
@@ -187,8 +193,6 @@ __device__ __forceinline__ void issue_entries(WarpRing& w, const UpdateParams& p
     cp_async16(&w.idx[dslot][lane], p.idx + src);
   }
 }
-
-__device__ __forceinline__ int ring_next(int s, int size) { return s + 1 == size ? 0 : s + 1; }
 
 // One warp's share of an update launch; rank is the block's position among the
 // blocks serving this problem (the grid for one problem, a block range for one
@@ -222,13 +226,11 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
 #pragma unroll
     for (int q = 0; q < kChunk / 32; ++q) {
       const int s = 32 * q + lane;
-      float sc = 0.f;
-      w.coords[s] = s < cnt ? draw_coord(p, k_base + base + (uint64_t)s, active_cnt, hot_cnt, sc) : 0;
-      w.scale[s] = sc;
+      w.coords[s] = s < cnt ? draw_coord(p, k_base + base + (uint64_t)s, active_cnt, hot_cnt) : 0;
     }
     __syncwarp();
 
-    // Prologue: metadata of updates 0..2D-1, then entries of updates 0..D-1,
+    // Prologue: metadata of updates 0..kDM-1, then entries of updates 0..D-1,
     // one commit group per update so that wait_group(D-1) below always means
     // "the copies of update s have landed".
     for (int t = 0; t < kDM && t < cnt; ++t) issue_meta(w, p, w.coords[t] & kCoordMask, t, lane);
@@ -241,12 +243,15 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
       cp_async_commit();
     }
 
-    // Ring positions: update s reads meta slot ms and entry slot ds; the refill
-    // writes entries of s+D into slot (s+D) mod kDS and meta of s+2D into slot
-    // (s+2D) mod kMS, which are the slots update s-1 used.
-    int ms = 0, ds = 0, ms_d = kD % kMS, ds_d = kD % kDS, ms_2d = kDM % kMS;
+    // Ring positions: update s reads meta slot s mod kMS and entry slot
+    // s mod kDS; the refill writes entries of s+D into slot (s+D) mod kDS and
+    // meta of s+kDM into slot (s+kDM) mod kMS, which are the slots update s-1
+    // used.
     uint32_t chunk_read = 0, chunk_nz = 0, chunk_scat = 0;
     for (int s = 0; s < cnt; ++s) {
+      const int ms = s & (kMS - 1), ds = s & (kDS - 1);
+      const int ms_d = (s + kD) & (kMS - 1), ds_d = (s + kD) & (kDS - 1);
+      const int ms_2d = (s + kDM) & (kMS - 1);
       cp_async_wait<kD - 1>();
       __syncwarp();  // copies of update s visible; every lane is done with update s-1
       const int32_t cj = w.coords[s];
@@ -260,22 +265,17 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
       const uint64_t start = (uint64_t)(uint32_t)mt.x << 2;
       const uint32_t len = (uint32_t)mt.y;
       const uint32_t e0 = 4u * (uint32_t)lane;
-      const bool live0 = e0 < len;
-      Chunk c0;
-      c0.v = live0 ? w.vals[ds][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
-      c0.i = live0 ? w.idx[ds][lane] : make_int4(0, 0, 0, 0);
+      Chunk c0;  // lanes past the column read stale slots, never used below
+      c0.v = w.vals[ds][lane];
+      c0.i = w.idx[ds][lane];
+      // g = a_j^T r: the gathers of the first 128 entries are issued before the
+      // refill below, whose bookkeeping then runs while they are in flight.
+      T acc = gather_dot_head<LOSS, T>(r, c0, e0, len);
       // Refill: entries of update s + D, metadata of update s + 2D.
       if (s + kD < cnt) issue_entries(w, p, ms_d, ds_d, lane);
       if (s + kDM < cnt) issue_meta(w, p, w.coords[s + kDM] & kCoordMask, ms_2d, lane);
       cp_async_commit();
-      ms = ring_next(ms, kMS);
-      ds = ring_next(ds, kDS);
-      ms_d = ring_next(ms_d, kMS);
-      ds_d = ring_next(ds_d, kDS);
-      ms_2d = ring_next(ms_2d, kMS);
 
-      // g = a_j^T r.
-      T acc = gather_dot_head<LOSS, T>(r, c0, e0, len);
       if (len > 128u) {
         Chunk a = load_chunk(p, start, len, 128u, lane);
         for (uint32_t off = 128u; off < len; off += 128u) {
@@ -286,8 +286,7 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
       }
       const T g = column_sum<T>(acc, len);
 
-      const float sc = w.scale[s];
-      const T li = (T)__int_as_float(mt.z) * (sc != 0.f ? (T)sc : (cj < 0 ? li_scale_hot : li_scale));
+      const T li = (T)__int_as_float(mt.z) * (cj < 0 ? li_scale_hot : li_scale);
       T delta, coef;
       if (LOSS == ACDC_LOSS_L1_SQUARE) {
         const T z = xj - li * g;
@@ -319,7 +318,7 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
       if (delta != T(0)) {
         chunk_nz++;
         chunk_scat += len;
-        scatter<T>(r, c0, coef, live0);
+        scatter_head<T>(r, c0, coef, e0, len);
         for (uint32_t off = 128u; off < len; off += 128u) {
           Chunk a = load_chunk(p, start, len, off, lane);
           scatter<T>(r, a, coef, off + e0 < len);
@@ -431,7 +430,7 @@ cudaError_t launch_batch_update(const BatchDev& b, int update_blocks, cudaStream
   return cudaGetLastError();
 }
 
-// Four 46 KB blocks per SM need the shared-memory side of the L1 carveout.
+// Four 37 KB blocks per SM need the shared-memory side of the L1 carveout.
 cudaError_t update_kernels_init() {
   const int carve = cudaSharedmemCarveoutMaxShared;
   const cudaFuncAttribute a = cudaFuncAttributePreferredSharedMemoryCarveout;

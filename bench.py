@@ -103,9 +103,6 @@ def parse_args():
     ap.add_argument("--serve-requests", type=int, default=128,
                     help="requests of the serving sample (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=1000.0)
-    ap.add_argument("--row-eso", type=int, default=1, choices=[0, 1],
-                    help="step sizes of the active and hot tiers: 1 per-column row-wise ESO "
-                         "weights, 0 one ESO parameter per tier")
     ap.add_argument("--probe-launches", action="store_true",
                     help="profiling aid: run one uniform-draw update launch (refresh_every "
                          "epochs) and one active-set launch (active_passes |A|/q updates) on "
@@ -123,17 +120,26 @@ def probe_launches(w):
     s = settings_for(w)
     s.hot_threshold = 0.0
     p = acdc.Problem(ctx, inst, s)
-    p.run_updates(w["refresh_every"] * inst.n)
-    p.synchronize()
+
+    def timed(count):
+        # host clock around one launch with the stream drained on both sides
+        # (includes the launch overhead, a few microseconds)
+        p.synchronize()
+        t = time.perf_counter()
+        p.run_updates(count)
+        p.synchronize()
+        return (time.perf_counter() - t) * 1e3
+
+    t1 = timed(w["refresh_every"] * inst.n)
     first = p.stats()
     ev = p.evaluate()
     count = int(w["active_passes"] * ev["active"] / 0.9)
     p.reset_stats()
-    p.run_updates(count)
-    p.synchronize()
+    t2 = timed(count)
     second = p.stats()
-    print(json.dumps({"workload": w.get("name"), "uniform_launch": first,
-                      "active_launch": dict(second, active_set=ev["active"])}), flush=True)
+    print(json.dumps({"workload": w.get("name"), "uniform_launch": dict(first, host_ms=t1),
+                      "active_launch": dict(second, active_set=ev["active"], host_ms=t2)}),
+          flush=True)
     p.close()
     ctx.close()
     return 0
@@ -454,7 +460,6 @@ def run_ours(args, w):
     inst = generate(w, pinned=True)
     t_gen = time.time() - t_gen
     s = settings_for(w)
-    s.row_eso = args.row_eso
     ctx = acdc.Context(local)
     p = acdc.Problem(ctx, inst, s)
     info = p.info()
@@ -570,7 +575,7 @@ def run_ours(args, w):
     else:
         solver_keys = {"gap_target_relative": w["gap"], "q_shrinking": 0.9,
                        "tau_active": w["tau_active"], "active_passes": w["active_passes"],
-                       "screened_eval": 1, "hot_threshold": 0.1, "row_eso": args.row_eso}
+                       "screened_eval": 1, "hot_threshold": 0.1}
     if rank == 0:
         line = {
             "metric": METRICS[w.get("loss", "lasso")], "value": value, "unit": "s", "n_gpus": world,

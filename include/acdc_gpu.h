@@ -94,15 +94,7 @@ typedef struct acdc_settings {
                                      pass (and active-set rebuild) runs whenever
                                      that bound reaches (1 - eps/2) lambda.  The
                                      certificate stays a valid duality gap.       */
-  int32_t row_eso;                /* with q-shrinking, 1 (default): an active-set
-                                     or hot-set draw of column j steps with
-                                     1/max(beta ||a_j||^2, sum_i beta_i A_ij^2),
-                                     beta_i = 1 + (w_i - 1)(t - 1)/(c - 1), where
-                                     w_i counts the tier's columns with an entry
-                                     in row i, c is the tier's size and t its
-                                     draws in flight; 0: one ESO parameter per
-                                     tier from the largest w_i                    */
-  int32_t reserved;
+  int32_t reserved[2];
   double hot_threshold;           /* Lasso with shrinking and screened_eval: after
                                      each evaluation the active columns whose KKT
                                      violation exceeds hot_threshold times the
@@ -258,14 +250,6 @@ int acdc_synchronize(acdc_problem* p);
  * against acdc_sample_coordinate (acdc_host.h). */
 int acdc_debug_sample(acdc_ctx* ctx, uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
                       int64_t* out);
-
-/* Diagnostic: the active list (tier 0) or the hot list (tier 1) that the last
- * evaluation with q-shrinking built, with the row-wise ESO step scale of each
- * entry (see acdc_settings.row_eso).  list and scale receive min(*count, cap)
- * entries; *count is the list's length.  No counterpart in the reference, whose
- * shrinking fields are not implemented. */
-int acdc_debug_tier(acdc_problem* p, int32_t tier, int64_t cap, int32_t* list, float* scale,
-                    int64_t* count);
 
 /* acdc_debug_sample without any allocation (no counterpart in the reference,
  * whose sampler is a host GSL call), for callers that must not allocate device

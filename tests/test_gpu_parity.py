@@ -187,13 +187,12 @@ def test_int32_column_pointers_and_warm_start(ctx):
     assert r.converged and r.epochs <= 2
 
 
-@pytest.mark.parametrize("row_eso", [0, 1])
-def test_shrinking_keeps_the_solution(ctx, row_eso):
+def test_shrinking_keeps_the_solution(ctx):
     inst = acdc.gen_lasso(3000, 30000, nnz_per_col=15, n_star=150, lambda_frac=0.1, seed=81)
     x_o, ev_o = oracle_optimum(inst)
     p = acdc.Problem(ctx, inst, tau=256, warps_per_block=8, gap_target=1e-7, refresh_every=2,
                      max_epochs=3000, use_shrinking=1, shrinking_probability=0.9,
-                     shrinking_starting_iter=2, seed=4, row_eso=row_eso)
+                     shrinking_starting_iter=2, seed=4)
     r = p.solve()
     assert r.converged, (r.eval.rel_gap, r.epochs, r.fp64_epochs)
     assert r.eval.active > 0
@@ -228,51 +227,6 @@ def test_screened_evaluations_certify_the_gap(ctx, precision):
     assert rq.converged and rq.stats.screened_evals == 0
     assert abs(rq.eval.primal - ev_o["primal"]) <= 1e-6 * abs(ev_o["primal"])
     q.close()
-    p.close()
-
-
-def tier_scales(inst, lst, draws, cap_by_count, beta):
-    """Row-wise ESO step scales of a tier list, in numpy: w_i counts the list's
-    columns with an entry in row i, beta_i = 1 + (w_i - 1)(t - 1)/(c - 1) and
-    scale_j = min(1, beta ||a_j||^2 / sum_i beta_i A_ij^2) on the FP32 values."""
-    cp, ri = inst.col_ptr, inst.row_idx
-    v = inst.vals.astype(np.float32).astype(np.float64)
-    w = np.zeros(inst.m, np.int64)
-    for j in lst:
-        w[ri[cp[j]:cp[j + 1]]] += 1
-    c = len(lst)
-    t = min(draws, c) if cap_by_count else draws
-    f = (t - 1.0) / (c - 1.0) if c > 1 and t > 1 else 0.0
-    out = np.ones(c)
-    for k, j in enumerate(lst):
-        a2 = v[cp[j]:cp[j + 1]] ** 2
-        v2 = (a2 * (1.0 + (np.maximum(w[ri[cp[j]:cp[j + 1]]], 1) - 1.0) * f)).sum()
-        if v2 > 0:
-            out[k] = min(1.0, beta * a2.sum() / v2)
-    return out
-
-
-def test_row_eso_tier_scales_match_numpy(ctx):
-    """After an evaluation with q-shrinking, the active and hot lists carry
-    step scales from per-row counts of their own columns (tau-nice ESO with a
-    beta_i per row); checked entry by entry against numpy."""
-    inst = acdc.gen_lasso(4000, 40000, nnz_mode=acdc.NNZ_ZIPF, zipf_s=1.5, nnz_min=1,
-                          nnz_max=400, nnz_mean=12.0, n_star=60, lambda_frac=0.1, seed=84)
-    tau_a, q = 64, 0.9
-    p = acdc.Problem(ctx, inst, tau=256, warps_per_block=8, gap_target=1e-12, refresh_every=2,
-                     max_epochs=8, use_shrinking=1, shrinking_probability=q,
-                     shrinking_starting_iter=2, seed=5, tau_active=tau_a, active_passes=10)
-    p.solve()
-    p.evaluate()  # full pass: rebuilds both lists and their scales
-    beta = p.info().sigma
-    act, sa = p.debug_tier(0)
-    hot, sh = p.debug_tier(1)
-    assert len(act) > 100 and len(hot) > 0
-    assert len(set(act.tolist())) == len(act) and set(hot.tolist()) <= set(act.tolist())
-    np.testing.assert_allclose(sa, tier_scales(inst, act, max(1.0, q * tau_a), 0, beta), rtol=2e-6)
-    np.testing.assert_allclose(sh, tier_scales(inst, hot, 0.5 * q * tau_a, 1, beta), rtol=2e-6)
-    assert sa.min() > 0 and sa.max() <= 1 and sh.min() > 0 and sh.max() <= 1
-    assert sa.min() < 1  # some active rows are shared: the weights bite
     p.close()
 
 
