@@ -56,6 +56,16 @@ class SolveResult(C.Structure):
                 ("stats", Stats), ("device_ms", D), ("fp64_epochs", I32), ("reserved", I32)]
 
 
+class TraceRow(C.Structure):
+    _fields_ = [("updates", U64), ("primal", D), ("gap", D), ("rel_gap", D), ("active", I64),
+                ("hot", I64), ("omega_active", I64), ("omega_hot", I64), ("update_ms", C.c_float),
+                ("eval_ms", C.c_float), ("shrink", I32), ("fp64", I32), ("screened", I32),
+                ("reserved", I32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
 class ProblemInfo(C.Structure):
     _fields_ = [("m", I64), ("n", I64), ("nnz", I64), ("nnz_padded", I64), ("omega", I64),
                 ("sigma", D), ("lambda_", D), ("device_bytes", I64), ("loss", I32), ("tau", I32),
@@ -140,6 +150,7 @@ def gpu_lib():
         L.acdc_recompute_residuals.argtypes = [VP]
         L.acdc_evaluate.argtypes = [VP, C.POINTER(Eval)]
         L.acdc_solve.argtypes = [VP, C.POINTER(SolveResult)]
+        L.acdc_solve_traced.argtypes = [VP, C.POINTER(SolveResult), VP, I64, C.POINTER(I64)]
         L.acdc_problem_reset.argtypes = [VP]
         L.acdc_get_x.argtypes = [VP, VP]
         L.acdc_set_x.argtypes = [VP, VP]
@@ -478,6 +489,14 @@ class Problem:
         r = SolveResult()
         self.ctx.check(self.L.acdc_solve(self.h, C.byref(r)))
         return r
+
+    def solve_traced(self, cap=100000):
+        """acdc_solve_traced: (result, list of per-evaluation row dicts)."""
+        r = SolveResult()
+        rows = (TraceRow * cap)()
+        n = I64(0)
+        self.ctx.check(self.L.acdc_solve_traced(self.h, C.byref(r), rows, cap, C.byref(n)))
+        return r, [rows[i].as_dict() for i in range(min(n.value, cap))]
 
     def reset(self):
         self.ctx.check(self.L.acdc_problem_reset(self.h))

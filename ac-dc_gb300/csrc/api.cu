@@ -635,9 +635,38 @@ extern "C" int acdc_evaluate(acdc_problem* p, acdc_eval* out) {
 }
 
 extern "C" int acdc_solve(acdc_problem* p, acdc_solve_result* out) {
-  if (!p || !out) return ACDC_EINVAL;
+  return acdc_solve_traced(p, out, nullptr, 0, nullptr);
+}
+
+extern "C" int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_trace_row* rows,
+                                 int64_t cap, int64_t* n_rows) {
+  if (!p || !out || cap < 0 || (cap > 0 && !rows)) return ACDC_EINVAL;
   acdc_ctx* ctx = p->ctx;
   std::memset(out, 0, sizeof(*out));
+  int64_t n_trace = 0;
+  auto trace = [&](uint64_t updates, const acdc_eval& e, float upd_ms, float ev_ms, bool shrink,
+                   bool fp64, bool screened) {
+    if (n_trace < cap) {
+      acdc_trace_row& t = rows[n_trace];
+      std::memset(&t, 0, sizeof(t));
+      t.updates = updates;
+      t.primal = e.primal;
+      t.gap = e.gap;
+      t.rel_gap = e.rel_gap;
+      t.active = e.active;
+      t.hot = p->hot_count;
+      t.omega_active = p->omega_active;
+      t.omega_hot = p->hot_count > 0 ? (int64_t)p->h_counters[CNT_OMEGA_HOT] : 0;
+      t.update_ms = upd_ms;
+      t.eval_ms = ev_ms;
+      t.shrink = shrink ? 1 : 0;
+      t.fp64 = fp64 ? 1 : 0;
+      t.screened = screened ? 1 : 0;
+    }
+    ++n_trace;
+    if (n_rows) *n_rows = n_trace;
+  };
+  if (n_rows) *n_rows = 0;
   auto t0 = std::chrono::steady_clock::now();
   ACDC_CK(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
   int rc = ACDC_OK;
@@ -645,8 +674,10 @@ extern "C" int acdc_solve(acdc_problem* p, acdc_solve_result* out) {
   if (p->s.precision == ACDC_PREC_FP32) rc = leave_fp64(p);
   if (rc != ACDC_OK) return rc;
   acdc_eval ev;
-  rc = evaluate_impl(p, &ev, nullptr);
+  float ev_ms = 0;
+  rc = evaluate_impl(p, &ev, &ev_ms);
   if (rc != ACDC_OK) return rc;
+  trace(0, ev, 0.f, ev_ms, false, p->fp64_mode, false);
   // Work is counted in updates; an epoch is n of them.
   const uint64_t n = (uint64_t)p->d.n;
   const uint64_t budget = (uint64_t)p->s.max_epochs * n;
@@ -684,8 +715,12 @@ extern "C" int acdc_solve(acdc_problem* p, acdc_solve_result* out) {
     if (p->fp64_mode) done_fp64 += count;
     p->updates_done += count;
     p->epochs_done = (int64_t)(p->updates_done / n);
-    rc = evaluate_impl(p, &ev, nullptr, screen);
+    const bool screened_now = screen && p->screen_valid;
+    rc = evaluate_impl(p, &ev, &ev_ms, screen);
     if (rc != ACDC_OK) return rc;
+    float bulk_ms = 0;
+    ACDC_CK(ctx, cudaEventElapsedTime(&bulk_ms, ctx->ev[0], ctx->ev[1]));
+    float extra_ms = 0;
     if (screen) {
       // The bound of the inactive columns: past (1 - eps/2) lambda the next
       // evaluation is a full one (new reference residual and active set); past
@@ -693,13 +728,12 @@ extern "C" int acdc_solve(acdc_problem* p, acdc_solve_result* out) {
       const double bound = p->h_eval[11];
       if (bound >= (1.0 - 0.5 * p->s.shrink_eps) * p->lambda) p->screen_valid = false;
       if (bound >= p->lambda && !converged(p->s, ev)) {
-        rc = evaluate_impl(p, &ev, nullptr);
+        rc = evaluate_impl(p, &ev, &extra_ms);
         if (rc != ACDC_OK) return rc;
       }
     }
-    float t = 0;
-    ACDC_CK(ctx, cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]));
-    p->stats.update_ms += t;
+    trace(done, ev, bulk_ms, ev_ms + extra_ms, shrink, u.fp64 != 0, screened_now && extra_ms == 0);
+    p->stats.update_ms += bulk_ms;
     if (ev.rel_gap < 0.5 * best) {
       best = ev.rel_gap;
       last_gain = done;

@@ -223,6 +223,31 @@ int acdc_evaluate(acdc_problem* p, acdc_eval* out);
  * target or max_epochs. */
 int acdc_solve(acdc_problem* p, acdc_solve_result* out);
 
+/* One row per evaluation of a solve: the reference's Solver prints one log row
+ * per bulk of updates (Solver.h:23-77, getResultLogRow); row 0 is the
+ * evaluation before the first bulk. */
+typedef struct acdc_trace_row {
+  uint64_t updates;         /* updates of this solve call before the evaluation   */
+  double primal;            /* P at the evaluation                                */
+  double gap;               /* P - D                                              */
+  double rel_gap;           /* (P - D) / max(1, |P|)                              */
+  int64_t active;           /* active-set size (q-shrinking), else 0              */
+  int64_t hot;              /* hot-set size, else 0                               */
+  int64_t omega_active;     /* max active columns in one row                      */
+  int64_t omega_hot;        /* max hot columns in one row                         */
+  float update_ms;          /* device time of the bulk before the evaluation      */
+  float eval_ms;            /* device time of the evaluation                      */
+  int32_t shrink;           /* 1: the bulk drew from the active (and hot) set     */
+  int32_t fp64;             /* 1: the bulk ran with FP64 x and residual           */
+  int32_t screened;         /* 1: the evaluation was a screened one               */
+  int32_t reserved;
+} acdc_trace_row;
+
+/* acdc_solve that also records its evaluations: rows receives the first cap of
+ * them and *n_rows (if not null) their number, which may exceed cap. */
+int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_trace_row* rows,
+                      int64_t cap, int64_t* n_rows);
+
 /* Restarts the solve on the resident data: x = 0, residual refreshed, sampler
  * counter 0, FP32 stage, active set cleared (the state the engine constructor
  * leaves, MulticoreEngineExecutor.h:25-66). */

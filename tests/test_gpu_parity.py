@@ -230,6 +230,30 @@ def test_screened_evaluations_certify_the_gap(ctx, precision):
     p.close()
 
 
+def test_solve_trace_records_every_evaluation(ctx):
+    """acdc_solve_traced: one row per evaluation (row 0 before any update), the
+    last row the solve's final certificate, work counters increasing; the same
+    solve without a trace ends at the same state (the trace only reads)."""
+    inst = acdc.gen_lasso(4000, 40000, nnz_mode=acdc.NNZ_ZIPF, zipf_s=1.5, nnz_min=3,
+                          nnz_max=400, nnz_mean=12.0, n_star=60, lambda_frac=0.1, seed=83)
+    kw = dict(tau=256, warps_per_block=8, gap_target=1e-7, refresh_every=2, max_epochs=5000,
+              use_shrinking=1, shrinking_probability=0.9, shrinking_starting_iter=2, seed=5,
+              tau_active=64, active_passes=10, precision=acdc.PREC_FP64)
+    p = acdc.Problem(ctx, inst, **kw)
+    r, rows = p.solve_traced()
+    assert r.converged and len(rows) >= 3
+    assert rows[0]["updates"] == 0 and rows[0]["update_ms"] == 0
+    assert all(b["updates"] > a["updates"] for a, b in zip(rows, rows[1:]))
+    assert rows[-1]["rel_gap"] == r.eval.rel_gap and rows[-1]["primal"] == r.eval.primal
+    assert rows[-1]["updates"] == r.stats.updates
+    assert any(t["shrink"] for t in rows) and any(t["screened"] for t in rows)
+    assert any(t["hot"] > 0 and t["omega_hot"] >= 1 for t in rows)
+    assert sum(t["update_ms"] for t in rows) > 0
+    _, few = p.solve_traced(cap=1)  # converged already: one evaluation, no bulk
+    assert len(few) == 1 and few[0]["updates"] == 0
+    p.close()
+
+
 def test_invalid_inputs_are_rejected(ctx):
     inst = acdc.gen_lasso(50, 80, nnz_per_col=3, n_star=5, seed=1)
     bad = acdc.Instance(inst.loss, inst.m, inst.n, inst.col_ptr, inst.row_idx.copy(), inst.vals,
