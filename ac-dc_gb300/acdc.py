@@ -18,7 +18,7 @@ OK, EINVAL, ENOMEM, EUNSUPPORTED, ECUDA, ETIMEOUT, EDEVICE, EBUSY, ENOTFOUND, EN
     0, -1, -2, -3, -4, -5, -6, -7, -8, -9)
 LOSS_L1_SQUARE, LOSS_L2_SQUARE, LOSS_SVM_DUAL, LOSS_LOGISTIC = 0, 1, 2, 3
 NNZ_FIXED, NNZ_ZIPF, NNZ_UNIFORM = 0, 1, 2
-PREC_AUTO, PREC_FP32, PREC_FP64, PREC_FP32_X64 = 0, 1, 2, 3
+PREC_AUTO, PREC_FP32, PREC_FP64 = 0, 1, 2
 
 I32, I64, U64, D = C.c_int32, C.c_int64, C.c_uint64, C.c_double
 VP = C.c_void_p

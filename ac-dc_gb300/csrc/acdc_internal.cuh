@@ -85,7 +85,6 @@ struct UpdateParams {
   int32_t n_warps;      // tau
   int32_t loss;
   int32_t fp64;         // 1: x and r in FP64 (x64, r64)
-  int32_t x64acc = 0;   // 1 (with fp64 = 0): x and the step in FP64 (x64), r in FP32
   uint64_t k_base;      // sampler counter of the launch's first update (batched launches)
 };
 
@@ -222,7 +221,6 @@ struct acdc_problem {
   uint64_t updates_done = 0;
   bool active_valid = false;
   bool fp64_mode = false;   // x and r kept in FP64 (polish stage or precision FP64)
-  bool x64acc = false;      // x kept in FP64 with the FP32 residual (precision FP32_X64)
   // Step scale while sampling from the active set: beta / max(beta, beta_A) with
   // beta_A the ESO parameter of q*tau draws over the active columns.
   double li_scale_shrink = 1.0;
@@ -241,8 +239,6 @@ struct acdc_problem {
 };
 
 // ---- helpers shared by the translation units ----
-// Where x and the working residual live (0: x32, r32; 1: x64, r32; 2: x64, r64).
-int acdc_set_x_mode(acdc_problem* p, int mode);
 int acdc_set_error(acdc_ctx* ctx, int code, const std::string& msg);
 int acdc_cuda_error(acdc_ctx* ctx, cudaError_t e, const char* what);
 

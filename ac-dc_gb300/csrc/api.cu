@@ -173,7 +173,7 @@ EvalParams eval_params(acdc_problem* p, bool build_active) {
   e.lambda = p->lambda;
   e.shrink_thresh = (1.0 - p->s.shrink_eps) * p->lambda;
   e.loss = p->loss;
-  e.x64 = (p->fp64_mode || p->x64acc) ? p->d.x64 : nullptr;
+  e.x64 = p->fp64_mode ? p->d.x64 : nullptr;
   e.x32 = p->d.x32;
   e.long_cols = p->d.long_cols;
   e.n_long = p->d.n_long;
@@ -213,7 +213,6 @@ UpdateParams update_params(acdc_problem* p, uint64_t count, bool shrink) {
   u.r64 = p->d.r64;
   u.x32 = p->d.x32;
   u.fp64 = p->fp64_mode ? 1 : 0;
-  u.x64acc = (!p->fp64_mode && p->x64acc) ? 1 : 0;
   double q = p->s.shrinking_probability;
   if (!shrink || q <= 0)
     u.shrink_q32 = 0;
@@ -256,8 +255,7 @@ int apply_settings(acdc_problem* p, const acdc_settings* s) {
       s->refresh_every < 1 ||
       s->max_epochs < 0 || !(s->gap_target >= 0) || s->shrinking_probability < 0 ||
       s->shrinking_probability > 1 || s->shrink_eps < 0 || s->shrink_eps >= 1 ||
-      s->precision < ACDC_PREC_AUTO || s->precision > ACDC_PREC_FP32_X64 ||
-      !(s->polish_rel_gap >= 0) ||
+      s->precision < ACDC_PREC_AUTO || s->precision > ACDC_PREC_FP64 || !(s->polish_rel_gap >= 0) ||
       !(s->hot_threshold >= 0))
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid settings value");
   p->s = *s;
@@ -486,7 +484,6 @@ extern "C" int acdc_problem_reset(acdc_problem* p) {
   acdc_ctx* ctx = p->ctx;
   ACDC_CK(ctx, cudaMemsetAsync(p->d.xbuf, 0, sizeof(double) * p->d.n, ctx->stream));
   p->fp64_mode = false;
-  p->x64acc = false;
   ACDC_CK(ctx, launch_set_x(p->d, false, ctx->stream));
   p->k_next = 0;
   p->epochs_done = 0;
@@ -508,36 +505,24 @@ extern "C" int acdc_problem_set_settings(acdc_problem* p, const acdc_settings* s
   return apply_settings(p, s);
 }
 
-// Where x and the working residual live: 0 = x32 and r32, 1 = x64 and r32
-// (precision FP32_X64), 2 = x64 and r64 (the FP64 polish stage or precision
-// FP64).  Moving to x64 copies x exactly; moving back to x32 rounds it.  The
-// residuals are refreshed from the resulting x, so the working one equals
-// A x - b (in its precision) for the x the next update reads.
-int acdc_set_x_mode(acdc_problem* p, int mode) {
-  const int cur = p->fp64_mode ? 2 : (p->x64acc ? 1 : 0);
-  if (cur == mode) return ACDC_OK;
-  if (cur == 0) ACDC_CK(p->ctx, launch_x32_to_x64(p->d, p->ctx->stream));
-  if (mode == 0) ACDC_CK(p->ctx, launch_x64_to_x32(p->d, p->ctx->stream));
-  p->fp64_mode = mode == 2;
-  p->x64acc = mode == 1;
-  EvalParams e = eval_params(p, false);
-  ACDC_CK(p->ctx, launch_refresh(e, p->ctx->stream));
+namespace {
+// Polish-mode transitions.  Entering copies x exactly (FP32 -> FP64); the FP64
+// residual of the last refresh already equals A x - b for that x.  Leaving
+// rounds x to FP32 and refreshes both residuals from it.
+int enter_fp64(acdc_problem* p) {
+  if (p->fp64_mode) return ACDC_OK;
+  ACDC_CK(p->ctx, launch_x32_to_x64(p->d, p->ctx->stream));
+  p->fp64_mode = true;
   return ACDC_OK;
 }
 
-namespace {
-int enter_fp64(acdc_problem* p) { return acdc_set_x_mode(p, 2); }
-int leave_fp64(acdc_problem* p) { return p->fp64_mode ? acdc_set_x_mode(p, 0) : ACDC_OK; }
-
-// The mode a solve or a bulk starts in: FP64 and FP32_X64 fix it, FP32 keeps
-// x32, AUTO starts from x32 (or stays in a polish stage already entered).
-int sync_precision(acdc_problem* p) {
-  switch (p->s.precision) {
-    case ACDC_PREC_FP64: return acdc_set_x_mode(p, 2);
-    case ACDC_PREC_FP32: return acdc_set_x_mode(p, 0);
-    case ACDC_PREC_FP32_X64: return acdc_set_x_mode(p, 1);
-    default: return p->x64acc ? acdc_set_x_mode(p, 0) : ACDC_OK;
-  }
+int leave_fp64(acdc_problem* p) {
+  if (!p->fp64_mode) return ACDC_OK;
+  ACDC_CK(p->ctx, launch_x64_to_x32(p->d, p->ctx->stream));
+  p->fp64_mode = false;
+  EvalParams e = eval_params(p, false);
+  ACDC_CK(p->ctx, launch_refresh(e, p->ctx->stream));
+  return ACDC_OK;
 }
 }  // namespace
 
@@ -558,8 +543,6 @@ extern "C" int acdc_problem_set_lambda(acdc_problem* p, double lambda) {
 extern "C" int acdc_run_updates(acdc_problem* p, uint64_t n_updates) {
   if (!p) return ACDC_EINVAL;
   acdc_ctx* ctx = p->ctx;
-  int rc = sync_precision(p);
-  if (rc != ACDC_OK) return rc;
   UpdateParams u = update_params(p, n_updates, shrink_now(p));
   ACDC_CK(ctx, launch_update(u, p->k_next, p->s.warps_per_block, ctx->stream));
   p->k_next += n_updates;
@@ -686,7 +669,9 @@ extern "C" int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_t
   if (n_rows) *n_rows = 0;
   auto t0 = std::chrono::steady_clock::now();
   ACDC_CK(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
-  int rc = sync_precision(p);
+  int rc = ACDC_OK;
+  if (p->s.precision == ACDC_PREC_FP64) rc = enter_fp64(p);
+  if (p->s.precision == ACDC_PREC_FP32) rc = leave_fp64(p);
   if (rc != ACDC_OK) return rc;
   acdc_eval ev;
   float ev_ms = 0;
@@ -771,7 +756,7 @@ extern "C" int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_t
 extern "C" int acdc_get_x(acdc_problem* p, double* x) {
   if (!p || !x) return ACDC_EINVAL;
   acdc_ctx* ctx = p->ctx;
-  ACDC_CK(ctx, launch_get_x(p->d, p->fp64_mode || p->x64acc, ctx->stream));
+  ACDC_CK(ctx, launch_get_x(p->d, p->fp64_mode, ctx->stream));
   ACDC_CK(ctx, cudaMemcpyAsync(x, p->d.xbuf, sizeof(double) * p->d.n, cudaMemcpyDeviceToHost,
                                ctx->stream));
   ACDC_CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -783,7 +768,7 @@ extern "C" int acdc_set_x(acdc_problem* p, const double* x) {
   acdc_ctx* ctx = p->ctx;
   ACDC_CK(ctx, cudaMemcpyAsync(p->d.xbuf, x, sizeof(double) * p->d.n, cudaMemcpyHostToDevice,
                                ctx->stream));
-  ACDC_CK(ctx, launch_set_x(p->d, p->fp64_mode || p->x64acc, ctx->stream));
+  ACDC_CK(ctx, launch_set_x(p->d, p->fp64_mode, ctx->stream));
   ACDC_CK(ctx, cudaStreamSynchronize(ctx->stream));
   p->active_valid = false;
   p->screen_valid = false;
@@ -871,7 +856,7 @@ extern "C" int acdc_test_accuracy(acdc_problem* p, int64_t n_test, const int64_t
     w64 = p->d.r64;
     w_len = p->d.m;
   } else {
-    if (p->fp64_mode || p->x64acc)
+    if (p->fp64_mode)
       w64 = p->d.x64;
     else
       w32 = p->d.x32;

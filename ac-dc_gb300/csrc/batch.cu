@@ -90,12 +90,7 @@ int prepare(acdc_problem* p, const SolveOpts& o, int wpb_cap) {
   else if (o.autotune)
     s.tau = autotune_tau(p->d.n, p->omega, 1.3);
   s.warps_per_block = std::min(wpb_cap, s.tau);
-  // The batched rounds keep x in x32 (or in x64 with r64 for the FP64 polish):
-  // FP32_X64 runs as FP32 here.
-  if (s.precision == ACDC_PREC_FP32_X64) s.precision = ACDC_PREC_FP32;
-  int rc = acdc_problem_set_settings(p, &s);
-  if (rc == ACDC_OK && p->x64acc) rc = acdc_set_x_mode(p, 0);
-  return rc;
+  return acdc_problem_set_settings(p, &s);
 }
 
 // Device tables and per-slot state of one set of problems solved together.

@@ -24,7 +24,8 @@
 // the copies of update s (cp.async.wait_group D-1), so D updates' worth of DRAM
 // traffic is in flight per warp while it waits on its L2 gathers of r.  x_j (in
 // x32 or x64) and r are read when the update runs (ld.global.cg, L2), so the sequence of
-// updates a warp performs reads exactly the state its own previous updates left.
+// updates a warp performs reads exactly the state its own previous updates left;
+// x_j's line is only prefetched into L2, with the metadata.
 // Entries beyond the first 128 of a long column are streamed with direct loads.
 //
 // Precision: T = float keeps x and r in FP32 (the bulk mode); T = double keeps
@@ -182,9 +183,17 @@ __device__ __forceinline__ void scatter(T* r, const Chunk& c, T coef, bool live)
   if (c.v.w != 0.f) atomicAdd(r + c.i.w, coef * (T)c.v.w);
 }
 
-__device__ __forceinline__ void issue_meta(WarpRing& w, const UpdateParams& p, int32_t j, int slot,
-                                           int lane) {
+__device__ __forceinline__ void prefetch_l2(const void* g) {
+  asm volatile("prefetch.global.L2 [%0];\n" ::"l"(g));
+}
+
+// Metadata of column j into ring slot `slot`, and x_j (xb: x32 or x64, xsz
+// bytes per coordinate) pulled into L2 so that the update's own read of x_j,
+// made when it runs, hits L2 instead of DRAM.
+__device__ __forceinline__ void issue_meta(WarpRing& w, const UpdateParams& p, const char* xb,
+                                           int xsz, int32_t j, int slot, int lane) {
   if (lane == 0) cp_async16(&w.meta[slot], p.meta + j);
+  if (lane == 1) prefetch_l2(xb + (size_t)j * (size_t)xsz);
 }
 
 __device__ __forceinline__ void issue_entries(WarpRing& w, const UpdateParams& p, int mslot,
@@ -200,11 +209,8 @@ __device__ __forceinline__ void issue_entries(WarpRing& w, const UpdateParams& p
 
 // One warp's share of an update launch; rank is the block's position among the
 // blocks serving this problem (the grid for one problem, a block range for one
-// slot of a batch).  T is the type of the residual and its arithmetic, TX that
-// of the coordinates and the step: TX = double with T = float keeps x in x64
-// and computes the step in FP64 from the FP32 gather, so that steps far below
-// x's FP32 spacing still land.
-template <int LOSS, typename T, typename TX = T>
+// slot of a batch).
+template <int LOSS, typename T>
 __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t k_base,
                                                  int64_t rank, WarpRing* rings) {
   const int lane = threadIdx.x & 31;
@@ -213,15 +219,16 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
   if (gwarp >= p.n_warps) return;
   WarpRing& w = rings[wib];
   T* r = reinterpret_cast<T*>(sizeof(T) == 8 ? (void*)p.r64 : (void*)p.r);
+  const char* xb = sizeof(T) == 8 ? (const char*)p.x64 : (const char*)p.x32;
   unsigned long long* work = p.counters + CNT_WORK;
   const int32_t active_cnt =
       p.shrink_q32 ? (int32_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n) : 0;
   const int32_t hot_cnt =
       p.hot_q32 ? (int32_t)min(p.counters[CNT_HOT], (unsigned long long)p.n) : 0;
-  const TX lam = (TX)p.lambda_d;
-  const TX inv_ln = (TX)p.inv_lambda_n_d;
-  const TX li_scale = (TX)p.li_scale;
-  const TX li_scale_hot = (TX)p.li_scale_hot;
+  const T lam = (T)p.lambda_d;
+  const T inv_ln = (T)p.inv_lambda_n_d;
+  const T li_scale = (T)p.li_scale;
+  const T li_scale_hot = (T)p.li_scale_hot;
   unsigned long long n_upd = 0, n_nz = 0, n_read = 0, n_scat = 0;
 
   for (;;) {
@@ -240,7 +247,8 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
     // Prologue: metadata of updates 0..kDM-1, then entries of updates 0..D-1,
     // one commit group per update so that wait_group(D-1) below always means
     // "the copies of update s have landed".
-    for (int t = 0; t < kDM && t < cnt; ++t) issue_meta(w, p, w.coords[t] & kCoordMask, t, lane);
+    for (int t = 0; t < kDM && t < cnt; ++t)
+      issue_meta(w, p, xb, (int)sizeof(T), w.coords[t] & kCoordMask, t, lane);
     cp_async_commit();
     cp_async_wait<0>();
     __syncwarp();
@@ -264,8 +272,8 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
       const int32_t cj = w.coords[s];
       const int32_t j = cj & kCoordMask;
       const int4 mt = w.meta[ms];
-      TX xj;
-      if constexpr (sizeof(TX) == 8)
+      T xj;
+      if constexpr (sizeof(T) == 8)
         xj = __ldcg(p.x64 + j);
       else
         xj = __ldcg(p.x32 + j);
@@ -277,12 +285,12 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
       c0.i = w.idx[ds][lane];
       // Refill: entries of update s + D, metadata of update s + 2D.
       if (s + kD < cnt) issue_entries(w, p, ms_d, ds_d, lane);
-      if (s + kDM < cnt) issue_meta(w, p, w.coords[s + kDM] & kCoordMask, ms_2d, lane);
+      if (s + kDM < cnt)
+        issue_meta(w, p, xb, (int)sizeof(T), w.coords[s + kDM] & kCoordMask, ms_2d, lane);
       cp_async_commit();
 
-      // g = a_j^T r.  (Issuing these gathers before the refill above, or
-      // prefetching x_j into L2 with the record, shortens uniform-draw launches
-      // but lengthens active-set ones, which dominate the solve.)
+      // g = a_j^T r.  (Issuing these gathers before the refill above shortens
+      // uniform-draw launches but lengthens active-set ones, which dominate.)
       T acc = gather_dot_head<LOSS, T>(r, c0, e0, len);
       if (len > 128u) {
         Chunk a = load_chunk(p, start, len, 128u, lane);
@@ -292,15 +300,15 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
           a = b;
         }
       }
-      const TX g = (TX)column_sum<T>(acc, len);
+      const T g = column_sum<T>(acc, len);
 
-      const TX li = (TX)__int_as_float(mt.z) * (cj < 0 ? li_scale_hot : li_scale);
-      TX delta, coef;
+      const T li = (T)__int_as_float(mt.z) * (cj < 0 ? li_scale_hot : li_scale);
+      T delta, coef;
       if (LOSS == ACDC_LOSS_L1_SQUARE) {
-        const TX z = xj - li * g;
-        TX a = fabs(z) - lam * li;
-        a = a < TX(0) ? TX(0) : a;
-        const TX xn = z > TX(0) ? a : (z < TX(0) ? -a : TX(0));
+        const T z = xj - li * g;
+        T a = fabs(z) - lam * li;
+        a = a < T(0) ? T(0) : a;
+        const T xn = z > T(0) ? a : (z < T(0) ? -a : T(0));
         delta = xn - xj;
         coef = delta;
       } else if (LOSS == ACDC_LOSS_L2_SQUARE) {
@@ -311,29 +319,28 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
         // MulticoreL2SquareRegLogisticLoss.h:88-115 with the label folded into the
         // values: gradient -sum_i v_i sigma(r_i) + lambda x_j, half step, and
         // r_i += -delta v_i.
-        delta = -li * (lam * xj - g) / TX(2);
+        delta = -li * (lam * xj - g) / T(2);
         coef = -delta;
       } else {
-        const TX y = li < TX(0) ? TX(-1) : TX(1);
-        delta = (TX(1) - g * y) * lam * fabs(li);
+        const T y = li < T(0) ? T(-1) : T(1);
+        delta = (T(1) - g * y) * lam * fabs(li);
         if (delta < -xj)
           delta = -xj;
-        else if (delta > TX(1) - xj)
-          delta = TX(1) - xj;
+        else if (delta > T(1) - xj)
+          delta = T(1) - xj;
         coef = delta * y * inv_ln;
       }
       chunk_read += len;
-      if (delta != TX(0)) {
+      if (delta != T(0)) {
         chunk_nz++;
         chunk_scat += len;
-        const T c = (T)coef;
-        scatter_head<T>(r, c0, c, e0, len);
+        scatter_head<T>(r, c0, coef, e0, len);
         for (uint32_t off = 128u; off < len; off += 128u) {
           Chunk a = load_chunk(p, start, len, off, lane);
-          scatter<T>(r, a, c, off + e0 < len);
+          scatter<T>(r, a, coef, off + e0 < len);
         }
         if (lane == 0) {
-          if constexpr (sizeof(TX) == 8)
+          if constexpr (sizeof(T) == 8)
             atomicAdd(p.x64 + j, delta);
           else
             atomicAdd(p.x32 + j, delta);
@@ -355,10 +362,10 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
   }
 }
 
-template <int LOSS, typename T, typename TX = T>
+template <int LOSS, typename T>
 __global__ void __launch_bounds__(256, 4) k_pcdm_update(UpdateParams p, uint64_t k_base) {
   __shared__ WarpRing rings[kMaxWarps];
-  pcdm_update_body<LOSS, T, TX>(p, k_base, blockIdx.x, rings);
+  pcdm_update_body<LOSS, T>(p, k_base, blockIdx.x, rings);
 }
 
 // Batched launch: each block serves one slot at rank blockIdx.x - first block
@@ -409,22 +416,22 @@ cudaError_t launch_update(const UpdateParams& p, uint64_t k_base, int warps_per_
   if (e != cudaSuccess) return e;
   const int blocks = (p.n_warps + warps_per_block - 1) / warps_per_block;
   dim3 grid(blocks), block(warps_per_block * 32);
-#define ACDC_LAUNCH(L, T, TX) k_pcdm_update<L, T, TX><<<grid, block, 0, st>>>(p, k_base)
-#define ACDC_LOSSES(T, TX)                                                  \
-  switch (p.loss) {                                                         \
-    case ACDC_LOSS_L1_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L1_SQUARE, T, TX); break; \
-    case ACDC_LOSS_L2_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L2_SQUARE, T, TX); break; \
-    case ACDC_LOSS_SVM_DUAL: ACDC_LAUNCH(ACDC_LOSS_SVM_DUAL, T, TX); break;   \
-    default: ACDC_LAUNCH(ACDC_LOSS_LOGISTIC, T, TX); break;                 \
-  }
+#define ACDC_LAUNCH(L, T) k_pcdm_update<L, T><<<grid, block, 0, st>>>(p, k_base)
   if (p.fp64) {
-    ACDC_LOSSES(double, double)
-  } else if (p.x64acc) {
-    ACDC_LOSSES(float, double)
+    switch (p.loss) {
+      case ACDC_LOSS_L1_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L1_SQUARE, double); break;
+      case ACDC_LOSS_L2_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L2_SQUARE, double); break;
+      case ACDC_LOSS_SVM_DUAL: ACDC_LAUNCH(ACDC_LOSS_SVM_DUAL, double); break;
+      default: ACDC_LAUNCH(ACDC_LOSS_LOGISTIC, double); break;
+    }
   } else {
-    ACDC_LOSSES(float, float)
+    switch (p.loss) {
+      case ACDC_LOSS_L1_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L1_SQUARE, float); break;
+      case ACDC_LOSS_L2_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L2_SQUARE, float); break;
+      case ACDC_LOSS_SVM_DUAL: ACDC_LAUNCH(ACDC_LOSS_SVM_DUAL, float); break;
+      default: ACDC_LAUNCH(ACDC_LOSS_LOGISTIC, float); break;
+    }
   }
-#undef ACDC_LOSSES
 #undef ACDC_LAUNCH
   return cudaGetLastError();
 }
@@ -451,10 +458,6 @@ cudaError_t update_kernels_init() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L2_SQUARE, double>, a, carve);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_LOGISTIC, float>, a, carve);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_LOGISTIC, double>, a, carve);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L1_SQUARE, float, double>, a, carve);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_SVM_DUAL, float, double>, a, carve);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L2_SQUARE, float, double>, a, carve);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_LOGISTIC, float, double>, a, carve);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_L1_SQUARE, float>, a, carve);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_L1_SQUARE, double>, a, carve);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_SVM_DUAL, float>, a, carve);

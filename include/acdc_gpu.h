@@ -108,15 +108,11 @@ typedef struct acdc_settings {
 
 /* precision: FP32 x and residual with FP64 refresh and gap (FP32), the same
  * with the updates switched to FP64 x and residual once the relative gap falls
- * below polish_rel_gap (AUTO, the default), FP64 throughout (FP64), or the
- * FP32 residual, gathers and scatters with x and the step in FP64 (FP32_X64:
- * a step far below x_j's FP32 spacing still lands, so the certificate is not
- * held at the FP32 iterate's resolution).  The matrix values are stored in
- * FP32 in every mode.  The batched paths run FP32_X64 as FP32. */
+ * below polish_rel_gap (AUTO, the default), or FP64 throughout (FP64).  The
+ * matrix values are stored in FP32 in every mode. */
 #define ACDC_PREC_AUTO 0
 #define ACDC_PREC_FP32 1
 #define ACDC_PREC_FP64 2
-#define ACDC_PREC_FP32_X64 3
 
 /* FP64 evaluation of the current iterate (after an FP64 refresh).  The duality
  * gaps of losses 0, 1 and 3 are this library's (the reference reports a gap

@@ -143,46 +143,6 @@ def test_svm_solution_parity(ctx):
     assert np.all((a >= 0) & (a <= 1))
 
 
-def with_f32_values(inst):
-    return acdc.Instance(inst.loss, inst.m, inst.n, inst.col_ptr, inst.row_idx, f32_values(inst),
-                         inst.rhs, inst.lam)
-
-
-@pytest.mark.parametrize("loss", [acdc.LOSS_L1_SQUARE, acdc.LOSS_SVM_DUAL])
-def test_fp32_residual_with_fp64_coordinates(ctx, loss):
-    """Precision FP32_X64: FP32 residual, gathers and scatters with x and the step
-    in FP64.  It reaches a 1e-8 certificate without the FP64 polish (no epoch
-    in FP64 mode) and the oracle's optimum on the same FP32-rounded values; a
-    later FP32 solve continues from x rounded to FP32."""
-    if loss == acdc.LOSS_L1_SQUARE:
-        inst = acdc.gen_lasso(3000, 30000, nnz_per_col=15, n_star=150, lambda_frac=0.1, seed=81)
-        kw = dict(gap_target=1e-8, gap_relative=1)
-    else:
-        inst = acdc.gen_svm(2000, 40000, nnz_median=120, nnz_sigma=0.8, w_star_nnz=800, lam=1e-3,
-                            seed=61)
-        kw = dict(gap_target=1e-8, gap_relative=0)
-    x_o, ev_o = oracle_optimum(with_f32_values(inst), target=1e-12)
-    p = acdc.Problem(ctx, inst, tau=64, warps_per_block=8, refresh_every=2, max_epochs=20000,
-                     seed=8, precision=acdc.PREC_FP32_X64, **kw)
-    r = p.solve()
-    assert r.converged, (r.eval.rel_gap, r.eval.gap, r.epochs)
-    assert r.fp64_epochs == 0
-    assert abs(r.eval.primal - ev_o["primal"]) <= 1e-8 * abs(ev_o["primal"])
-    x = p.get_x()
-    if loss == acdc.LOSS_L1_SQUARE:
-        assert set(np.nonzero(x)[0]) == set(np.nonzero(x_o)[0])
-        assert np.abs(x - x_o).max() <= 1e-5
-    else:
-        assert np.all((x >= 0) & (x <= 1))
-    assert not np.array_equal(x, x.astype(np.float32).astype(np.float64))  # x is FP64
-    p.set_settings(p.settings, precision=acdc.PREC_FP32, gap_target=1e-6)
-    r2 = p.solve()
-    assert r2.converged and r2.epochs <= 2
-    x2 = p.get_x()
-    assert np.array_equal(x2, x2.astype(np.float32).astype(np.float64))  # rounded to FP32
-    p.close()
-
-
 def test_long_and_empty_columns(ctx):
     """Columns longer than one 128-entry chunk, empty columns and a dense row."""
     m, n = 3000, 400
