@@ -24,8 +24,7 @@
 // the copies of update s (cp.async.wait_group D-1), so D updates' worth of DRAM
 // traffic is in flight per warp while it waits on its L2 gathers of r.  x_j (in
 // x32 or x64) and r are read when the update runs (ld.global.cg, L2), so the sequence of
-// updates a warp performs reads exactly the state its own previous updates left;
-// x_j's line is only prefetched into L2, with the metadata.
+// updates a warp performs reads exactly the state its own previous updates left.
 // Entries beyond the first 128 of a long column are streamed with direct loads.
 //
 // Precision: T = float keeps x and r in FP32 (the bulk mode); T = double keeps
@@ -183,17 +182,9 @@ __device__ __forceinline__ void scatter(T* r, const Chunk& c, T coef, bool live)
   if (c.v.w != 0.f) atomicAdd(r + c.i.w, coef * (T)c.v.w);
 }
 
-__device__ __forceinline__ void prefetch_l2(const void* g) {
-  asm volatile("prefetch.global.L2 [%0];\n" ::"l"(g));
-}
-
-// Metadata of column j into ring slot `slot`, and x_j (xb: x32 or x64, xsz
-// bytes per coordinate) pulled into L2 so that the update's own read of x_j,
-// made when it runs, hits L2 instead of DRAM.
-__device__ __forceinline__ void issue_meta(WarpRing& w, const UpdateParams& p, const char* xb,
-                                           int xsz, int32_t j, int slot, int lane) {
+__device__ __forceinline__ void issue_meta(WarpRing& w, const UpdateParams& p, int32_t j, int slot,
+                                           int lane) {
   if (lane == 0) cp_async16(&w.meta[slot], p.meta + j);
-  if (lane == 1) prefetch_l2(xb + (size_t)j * (size_t)xsz);
 }
 
 __device__ __forceinline__ void issue_entries(WarpRing& w, const UpdateParams& p, int mslot,
@@ -219,7 +210,6 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
   if (gwarp >= p.n_warps) return;
   WarpRing& w = rings[wib];
   T* r = reinterpret_cast<T*>(sizeof(T) == 8 ? (void*)p.r64 : (void*)p.r);
-  const char* xb = sizeof(T) == 8 ? (const char*)p.x64 : (const char*)p.x32;
   unsigned long long* work = p.counters + CNT_WORK;
   const int32_t active_cnt =
       p.shrink_q32 ? (int32_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n) : 0;
@@ -247,8 +237,7 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
     // Prologue: metadata of updates 0..kDM-1, then entries of updates 0..D-1,
     // one commit group per update so that wait_group(D-1) below always means
     // "the copies of update s have landed".
-    for (int t = 0; t < kDM && t < cnt; ++t)
-      issue_meta(w, p, xb, (int)sizeof(T), w.coords[t] & kCoordMask, t, lane);
+    for (int t = 0; t < kDM && t < cnt; ++t) issue_meta(w, p, w.coords[t] & kCoordMask, t, lane);
     cp_async_commit();
     cp_async_wait<0>();
     __syncwarp();
@@ -285,12 +274,12 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
       c0.i = w.idx[ds][lane];
       // Refill: entries of update s + D, metadata of update s + 2D.
       if (s + kD < cnt) issue_entries(w, p, ms_d, ds_d, lane);
-      if (s + kDM < cnt)
-        issue_meta(w, p, xb, (int)sizeof(T), w.coords[s + kDM] & kCoordMask, ms_2d, lane);
+      if (s + kDM < cnt) issue_meta(w, p, w.coords[s + kDM] & kCoordMask, ms_2d, lane);
       cp_async_commit();
 
-      // g = a_j^T r.  (Issuing these gathers before the refill above shortens
-      // uniform-draw launches but lengthens active-set ones, which dominate.)
+      // g = a_j^T r.  (Issuing these gathers before the refill above, or
+      // prefetching x_j into L2 with the record, shortens uniform-draw launches
+      // but lengthens active-set ones, which dominate the solve.)
       T acc = gather_dot_head<LOSS, T>(r, c0, e0, len);
       if (len > 128u) {
         Chunk a = load_chunk(p, start, len, 128u, lane);
