@@ -256,7 +256,7 @@ int apply_settings(acdc_problem* p, const acdc_settings* s) {
       s->max_epochs < 0 || !(s->gap_target >= 0) || s->shrinking_probability < 0 ||
       s->shrinking_probability > 1 || s->shrink_eps < 0 || s->shrink_eps >= 1 ||
       s->precision < ACDC_PREC_AUTO || s->precision > ACDC_PREC_FP64 || !(s->polish_rel_gap >= 0) ||
-      !(s->hot_threshold >= 0))
+      !(s->hot_threshold >= 0) || s->polish_stall_epochs < 0)
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid settings value");
   p->s = *s;
   // q-shrinking and its screened evaluations cover losses 0 and 2 only.
@@ -686,9 +686,11 @@ extern "C" int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_t
   uint64_t last_gain = 0;  // updates done when the gap last halved
   while (!converged(p->s, ev) && done < budget) {
     // AUTO: the FP32 iterate bounds the certificate near 1e-7 relative (higher
-    // for badly scaled columns); finish in FP64 once the gap is small or has
-    // not halved over ten epochs of updates.
-    const bool stalled = done - last_gain >= 10 * n && ev.rel_gap < 1e-2;
+    // for badly scaled columns, or where x_j's FP32 spacing is coarse against
+    // the KKT tolerance); finish in FP64 once the gap is small or has not
+    // halved over polish_stall_epochs (default 10) epochs of updates.
+    const uint64_t stall = p->s.polish_stall_epochs > 0 ? (uint64_t)p->s.polish_stall_epochs : 10u;
+    const bool stalled = done - last_gain >= stall * n && ev.rel_gap < 1e-2;
     if (p->s.precision == ACDC_PREC_AUTO && !p->fp64_mode &&
         (ev.rel_gap <= p->s.polish_rel_gap || stalled)) {
       rc = enter_fp64(p);

@@ -94,7 +94,10 @@ typedef struct acdc_settings {
                                      pass (and active-set rebuild) runs whenever
                                      that bound reaches (1 - eps/2) lambda.  The
                                      certificate stays a valid duality gap.       */
-  int32_t reserved[2];
+  int32_t polish_stall_epochs;     /* AUTO: also switch to FP64 once the relative
+                                     gap (below 1e-2) has not halved over this
+                                     many epochs; 0 = 10                          */
+  int32_t reserved;
   double hot_threshold;           /* Lasso with shrinking and screened_eval: after
                                      each evaluation the active columns whose KKT
                                      violation exceeds hot_threshold times the
