@@ -24,6 +24,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/acdc_gpu.h"
 #include "acdc_philox.h"
@@ -203,6 +204,13 @@ struct acdc_ctx {
   int device = 0;
   int sm_count = 0;
   cudaStream_t stream = nullptr;
+  cudaMemPool_t pool = nullptr;  // device memory of the context's problems and tables
+  // Pinned host slots (16 doubles of evaluation results + CNT_SLOTS counters
+  // each) handed to problems: cut from blocks allocated once, so creating and
+  // destroying a problem makes no pinned allocation (cudaFreeHost would wait
+  // for the device).
+  std::vector<double*> host_free;
+  std::vector<void*> host_blocks;
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   std::string last_error;
   int64_t live_problems = 0;  // problems (and servers) created on this context
@@ -239,6 +247,17 @@ struct acdc_problem {
 };
 
 // ---- helpers shared by the translation units ----
+// Device memory of a context: stream-ordered allocations on its stream from its
+// own pool, which keeps freed blocks for reuse.  Once the pool has grown, an
+// allocation or a free is neither a driver call nor a device-wide
+// synchronisation (a cudaFree synchronises the device), which matters for the
+// server, whose requests come and go while other solves run.
+cudaError_t acdc_dev_alloc(acdc_ctx* ctx, void** p, size_t bytes);
+void acdc_dev_free(acdc_ctx* ctx, void* p);
+// A pinned host slot of kHostSlotDoubles doubles, and its return.
+constexpr int kHostSlotDoubles = 16 + CNT_SLOTS;
+cudaError_t acdc_host_slot_take(acdc_ctx* ctx, double** slot);
+void acdc_host_slot_give(acdc_ctx* ctx, double* slot);
 int acdc_set_error(acdc_ctx* ctx, int code, const std::string& msg);
 int acdc_cuda_error(acdc_ctx* ctx, cudaError_t e, const char* what);
 

@@ -76,9 +76,23 @@ extern "C" int acdc_ctx_create(int device, acdc_ctx** out) {
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) {
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    e = cudaMemPoolCreate(&ctx->pool, &props);
+  }
+  if (e == cudaSuccess) {
+    // keep freed blocks in the pool until the context goes away
+    uint64_t keep = UINT64_MAX;
+    e = cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
   if (e == cudaSuccess) e = update_kernels_init();
   if (e != cudaSuccess) {
+    if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     delete ctx;
     return ACDC_ECUDA;
   }
@@ -91,11 +105,41 @@ extern "C" int acdc_ctx_destroy(acdc_ctx* ctx) {
   if (ctx->live_problems > 0)
     return acdc_set_error(ctx, ACDC_EBUSY, "destroy every problem of the context first");
   cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);  // frees in flight complete
   for (int i = 0; i < 6; ++i)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
+  for (void* b : ctx->host_blocks) cudaFreeHost(b);
   delete ctx;
   return ACDC_OK;
+}
+
+cudaError_t acdc_dev_alloc(acdc_ctx* ctx, void** p, size_t bytes) {
+  return cudaMallocFromPoolAsync(p, bytes > 0 ? bytes : 1, ctx->pool, ctx->stream);
+}
+
+void acdc_dev_free(acdc_ctx* ctx, void* p) {
+  if (p) cudaFreeAsync(p, ctx->stream);
+}
+
+cudaError_t acdc_host_slot_take(acdc_ctx* ctx, double** slot) {
+  if (ctx->host_free.empty()) {
+    constexpr int kPerBlock = 64;
+    void* block = nullptr;
+    cudaError_t e = cudaMallocHost(&block, sizeof(double) * kHostSlotDoubles * kPerBlock);
+    if (e != cudaSuccess) return e;
+    ctx->host_blocks.push_back(block);
+    for (int i = kPerBlock - 1; i >= 0; --i)
+      ctx->host_free.push_back(static_cast<double*>(block) + (size_t)i * kHostSlotDoubles);
+  }
+  *slot = ctx->host_free.back();
+  ctx->host_free.pop_back();
+  return cudaSuccess;
+}
+
+void acdc_host_slot_give(acdc_ctx* ctx, double* slot) {
+  if (slot) ctx->host_free.push_back(slot);
 }
 
 // ---- problem ----
@@ -103,33 +147,33 @@ extern "C" int acdc_ctx_destroy(acdc_ctx* ctx) {
 namespace {
 
 template <typename T>
-cudaError_t dalloc(T** p, int64_t count, int64_t* bytes) {
+cudaError_t dalloc(acdc_ctx* ctx, T** p, int64_t count, int64_t* bytes) {
   size_t b = sizeof(T) * (size_t)(count > 0 ? count : 1);
   *bytes += (int64_t)b;
-  return cudaMalloc((void**)p, b);
+  return acdc_dev_alloc(ctx, (void**)p, b);
 }
 
-void free_problem_buffers(DevProblem& d) {
-  cudaFree(d.meta);
-  cudaFree(d.x32);
-  cudaFree(d.vals);
-  cudaFree(d.idx);
-  cudaFree(d.r32);
-  cudaFree(d.r64);
-  cudaFree(d.rhs64);
-  cudaFree(d.col_sq);
-  cudaFree(d.active);
-  cudaFree(d.xbuf);
-  cudaFree(d.x64);
-  cudaFree(d.rowcnt);
-  cudaFree(d.long_cols);
-  cudaFree(d.r_ref);
-  cudaFree(d.viol);
-  cudaFree(d.hot);
-  cudaFree(d.row_flag);
-  cudaFree(d.part);
-  cudaFree(d.eval_out);
-  cudaFree(d.counters);
+void free_problem_buffers(acdc_ctx* ctx, DevProblem& d) {
+  acdc_dev_free(ctx, d.meta);
+  acdc_dev_free(ctx, d.x32);
+  acdc_dev_free(ctx, d.vals);
+  acdc_dev_free(ctx, d.idx);
+  acdc_dev_free(ctx, d.r32);
+  acdc_dev_free(ctx, d.r64);
+  acdc_dev_free(ctx, d.rhs64);
+  acdc_dev_free(ctx, d.col_sq);
+  acdc_dev_free(ctx, d.active);
+  acdc_dev_free(ctx, d.xbuf);
+  acdc_dev_free(ctx, d.x64);
+  acdc_dev_free(ctx, d.rowcnt);
+  acdc_dev_free(ctx, d.long_cols);
+  acdc_dev_free(ctx, d.r_ref);
+  acdc_dev_free(ctx, d.viol);
+  acdc_dev_free(ctx, d.hot);
+  acdc_dev_free(ctx, d.row_flag);
+  acdc_dev_free(ctx, d.part);
+  acdc_dev_free(ctx, d.eval_out);
+  acdc_dev_free(ctx, d.counters);
   d = DevProblem();
 }
 
@@ -307,13 +351,12 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
   int64_t* s_scratch = nullptr;
   int64_t stage_bytes = 0;
   auto fail = [&](int code) {
-    cudaFree(s_colptr);
-    cudaFree(s_rows);
-    cudaFree(s_vals);
-    cudaFree(s_scratch);
-    free_problem_buffers(d);
-    if (p->h_eval) cudaFreeHost(p->h_eval);
-    if (p->h_counters) cudaFreeHost(p->h_counters);
+    acdc_dev_free(ctx, s_colptr);
+    acdc_dev_free(ctx, s_rows);
+    acdc_dev_free(ctx, s_vals);
+    acdc_dev_free(ctx, s_scratch);
+    free_problem_buffers(ctx, d);
+    acdc_host_slot_give(ctx, p->h_eval);
     delete p;
     return code;
   };
@@ -322,12 +365,12 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
     cudaError_t _e = (call);                                \
     if (_e != cudaSuccess) return fail(acdc_cuda_error(ctx, _e, #call)); \
   } while (0)
-  STEP(cudaMallocHost((void**)&p->h_eval, sizeof(double) * 16));
-  STEP(cudaMallocHost((void**)&p->h_counters, sizeof(unsigned long long) * CNT_SLOTS));
-  STEP(dalloc(&d.counters, CNT_SLOTS, &d.bytes));
+  STEP(acdc_host_slot_take(ctx, &p->h_eval));
+  p->h_counters = reinterpret_cast<unsigned long long*>(p->h_eval + 16);
+  STEP(dalloc(ctx, &d.counters, CNT_SLOTS, &d.bytes));
   STEP(cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long) * CNT_SLOTS, st));
-  STEP(dalloc(&s_colptr, n + 1, &stage_bytes));
-  STEP(dalloc(&s_scratch, scratch_len, &stage_bytes));
+  STEP(dalloc(ctx, &s_colptr, n + 1, &stage_bytes));
+  STEP(dalloc(ctx, &s_scratch, scratch_len, &stage_bytes));
   if (col_ptr64) {
     STEP(cudaMemcpyAsync(s_colptr, col_ptr64, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st));
   } else {
@@ -337,8 +380,8 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
     STEP(launch_widen_i32(tmp, s_colptr, n + 1, st));
   }
   if (nnz > 0) {
-    STEP(dalloc(&s_rows, nnz, &stage_bytes));
-    STEP(dalloc(&s_vals, nnz, &stage_bytes));
+    STEP(dalloc(ctx, &s_rows, nnz, &stage_bytes));
+    STEP(dalloc(ctx, &s_vals, nnz, &stage_bytes));
     STEP(cudaMemcpyAsync(s_rows, row_idx, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, st));
     STEP(cudaMemcpyAsync(s_vals, vals, sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
   }
@@ -355,29 +398,29 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
     return fail(acdc_set_error(ctx, ACDC_EINVAL, "matrix too large for 32-bit column starts"));
   d.nnz_pad = units * 4;
   const int64_t rhs_len = loss == ACDC_LOSS_SVM_DUAL ? n : m;
-  STEP(dalloc(&d.meta, n, &d.bytes));
-  STEP(dalloc(&d.x32, n, &d.bytes));
+  STEP(dalloc(ctx, &d.meta, n, &d.bytes));
+  STEP(dalloc(ctx, &d.x32, n, &d.bytes));
   STEP(cudaMemsetAsync(d.x32, 0, sizeof(float) * n, st));
-  STEP(dalloc(&d.vals, d.nnz_pad, &d.bytes));
-  STEP(dalloc(&d.idx, d.nnz_pad, &d.bytes));
-  STEP(dalloc(&d.r32, m, &d.bytes));
-  STEP(dalloc(&d.r64, m, &d.bytes));
-  STEP(dalloc(&d.rhs64, rhs_len, &d.bytes));
-  STEP(dalloc(&d.col_sq, n, &d.bytes));
-  STEP(dalloc(&d.active, n, &d.bytes));
-  STEP(dalloc(&d.xbuf, n, &d.bytes));
-  STEP(dalloc(&d.x64, n, &d.bytes));
-  STEP(dalloc(&d.rowcnt, m, &d.bytes));
-  if (loss == ACDC_LOSS_LOGISTIC) STEP(dalloc(&d.r_ref, m, &d.bytes));  // row weights
+  STEP(dalloc(ctx, &d.vals, d.nnz_pad, &d.bytes));
+  STEP(dalloc(ctx, &d.idx, d.nnz_pad, &d.bytes));
+  STEP(dalloc(ctx, &d.r32, m, &d.bytes));
+  STEP(dalloc(ctx, &d.r64, m, &d.bytes));
+  STEP(dalloc(ctx, &d.rhs64, rhs_len, &d.bytes));
+  STEP(dalloc(ctx, &d.col_sq, n, &d.bytes));
+  STEP(dalloc(ctx, &d.active, n, &d.bytes));
+  STEP(dalloc(ctx, &d.xbuf, n, &d.bytes));
+  STEP(dalloc(ctx, &d.x64, n, &d.bytes));
+  STEP(dalloc(ctx, &d.rowcnt, m, &d.bytes));
+  if (loss == ACDC_LOSS_LOGISTIC) STEP(dalloc(ctx, &d.r_ref, m, &d.bytes));  // row weights
   if (loss == ACDC_LOSS_L1_SQUARE) {
-    STEP(dalloc(&d.r_ref, m, &d.bytes));
-    STEP(dalloc(&d.viol, n, &d.bytes));
-    STEP(dalloc(&d.hot, n, &d.bytes));
-    STEP(dalloc(&d.row_flag, m, &d.bytes));
+    STEP(dalloc(ctx, &d.r_ref, m, &d.bytes));
+    STEP(dalloc(ctx, &d.viol, n, &d.bytes));
+    STEP(dalloc(ctx, &d.hot, n, &d.bytes));
+    STEP(dalloc(ctx, &d.row_flag, m, &d.bytes));
     STEP(cudaMemsetAsync(d.row_flag, 0, m, st));
   }
-  STEP(dalloc(&d.part, (int64_t)ACDC_RED_BLOCKS * ACDC_NPART, &d.bytes));
-  STEP(dalloc(&d.eval_out, 16, &d.bytes));
+  STEP(dalloc(ctx, &d.part, (int64_t)ACDC_RED_BLOCKS * ACDC_NPART, &d.bytes));
+  STEP(dalloc(ctx, &d.eval_out, 16, &d.bytes));
   STEP(cudaMemsetAsync(d.part, 0, sizeof(double) * ACDC_RED_BLOCKS * ACDC_NPART, st));
   STEP(cudaMemcpyAsync(d.rhs64, rhs, sizeof(double) * rhs_len, cudaMemcpyHostToDevice, st));
   STEP(launch_layout_fill(s_colptr, s_rows, s_vals, m, n, s_scratch, d, loss, st));
@@ -390,20 +433,20 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
   STEP(cudaMemsetAsync(omega_slot, 0, sizeof(unsigned long long), st));
   STEP(launch_max_i32(counts, m, omega_slot, st));
   // Columns too long for the thread-per-column gap pass.
-  STEP(dalloc(&d.long_cols, n, &d.bytes));
+  STEP(dalloc(ctx, &d.long_cols, n, &d.bytes));
   STEP(launch_list_long(d, d.long_cols, d.counters + CNT_NLONG, st));
   rc = check_status_word(p);
   if (rc != ACDC_OK) return fail(rc);
   // The reference starts its running maximum at 1 (MultiCoreSolver.cpp:24).
   p->omega = std::max<int64_t>(1, (int64_t)p->h_counters[CNT_GMAX_BITS]);
   d.n_long = (int64_t)p->h_counters[CNT_NLONG];
-  STEP(cudaFree(s_colptr));
+  acdc_dev_free(ctx, s_colptr);
   s_colptr = nullptr;
-  STEP(cudaFree(s_rows));
+  acdc_dev_free(ctx, s_rows);
   s_rows = nullptr;
-  STEP(cudaFree(s_vals));
+  acdc_dev_free(ctx, s_vals);
   s_vals = nullptr;
-  STEP(cudaFree(s_scratch));
+  acdc_dev_free(ctx, s_scratch);
   s_scratch = nullptr;
 #undef STEP
   acdc_settings s;
@@ -451,12 +494,13 @@ extern "C" int acdc_problem_create_i32(acdc_ctx* ctx, int32_t loss, int64_t m, i
 
 extern "C" int acdc_problem_destroy(acdc_problem* p) {
   if (!p) return ACDC_EINVAL;
-  cudaSetDevice(p->ctx->device);
-  cudaStreamSynchronize(p->ctx->stream);
-  free_problem_buffers(p->d);
-  if (p->h_eval) cudaFreeHost(p->h_eval);
-  if (p->h_counters) cudaFreeHost(p->h_counters);
-  p->ctx->live_problems--;
+  acdc_ctx* ctx = p->ctx;
+  cudaSetDevice(ctx->device);
+  // copies into the problem's pinned slot must land before the slot is reused
+  cudaStreamSynchronize(ctx->stream);
+  free_problem_buffers(ctx, p->d);
+  acdc_host_slot_give(ctx, p->h_eval);
+  ctx->live_problems--;
   delete p;
   return ACDC_OK;
 }
@@ -818,12 +862,12 @@ extern "C" int acdc_debug_sample(acdc_ctx* ctx, uint64_t seed, uint64_t k0, uint
                                  int64_t n, int64_t* out) {
   if (!ctx || (count > 0 && !out) || n <= 0) return ACDC_EINVAL;
   int64_t* d = nullptr;
-  ACDC_CK(ctx, cudaMalloc((void**)&d, sizeof(int64_t) * (count > 0 ? count : 1)));
+  ACDC_CK(ctx, acdc_dev_alloc(ctx, (void**)&d, sizeof(int64_t) * (count > 0 ? count : 1)));
   cudaError_t e = launch_debug_sample(seed, k0, count, n, d, ctx->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(out, d, sizeof(int64_t) * count, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-  cudaFree(d);
+  acdc_dev_free(ctx, d);
   if (e != cudaSuccess) return acdc_cuda_error(ctx, e, "acdc_debug_sample");
   return ACDC_OK;
 }
@@ -869,11 +913,11 @@ extern "C" int acdc_test_accuracy(acdc_problem* p, int64_t n_test, const int64_t
   double *d_vals = nullptr, *d_lab = nullptr;
   unsigned long long* d_good = nullptr;
   unsigned long long good = 0;
-  cudaError_t e = cudaMalloc((void**)&d_ptr, sizeof(int64_t) * (n_test + 1));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&d_idx, sizeof(int32_t) * (nnz > 0 ? nnz : 1));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&d_vals, sizeof(double) * (nnz > 0 ? nnz : 1));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&d_lab, sizeof(double) * n_test);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&d_good, sizeof(unsigned long long));
+  cudaError_t e = acdc_dev_alloc(ctx, (void**)&d_ptr, sizeof(int64_t) * (n_test + 1));
+  if (e == cudaSuccess) e = acdc_dev_alloc(ctx, (void**)&d_idx, sizeof(int32_t) * (nnz > 0 ? nnz : 1));
+  if (e == cudaSuccess) e = acdc_dev_alloc(ctx, (void**)&d_vals, sizeof(double) * (nnz > 0 ? nnz : 1));
+  if (e == cudaSuccess) e = acdc_dev_alloc(ctx, (void**)&d_lab, sizeof(double) * n_test);
+  if (e == cudaSuccess) e = acdc_dev_alloc(ctx, (void**)&d_good, sizeof(unsigned long long));
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(d_ptr, row_ptr, sizeof(int64_t) * (n_test + 1), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && nnz > 0)
@@ -887,11 +931,11 @@ extern "C" int acdc_test_accuracy(acdc_problem* p, int64_t n_test, const int64_t
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(&good, d_good, sizeof(good), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  cudaFree(d_ptr);
-  cudaFree(d_idx);
-  cudaFree(d_vals);
-  cudaFree(d_lab);
-  cudaFree(d_good);
+  acdc_dev_free(ctx, d_ptr);
+  acdc_dev_free(ctx, d_idx);
+  acdc_dev_free(ctx, d_vals);
+  acdc_dev_free(ctx, d_lab);
+  acdc_dev_free(ctx, d_good);
   if (e != cudaSuccess) return acdc_cuda_error(ctx, e, "acdc_test_accuracy");
   *accuracy = (double)good / (double)n_test;
   return ACDC_OK;

@@ -46,10 +46,11 @@ double now_seconds() {
 }
 
 template <typename T>
-cudaError_t upload(T** dst, const std::vector<T>& src, cudaStream_t st) {
-  cudaError_t e = cudaMalloc((void**)dst, sizeof(T) * std::max<size_t>(1, src.size()));
+cudaError_t upload(acdc_ctx* ctx, T** dst, const std::vector<T>& src) {
+  cudaError_t e = acdc_dev_alloc(ctx, (void**)dst, sizeof(T) * std::max<size_t>(1, src.size()));
   if (e == cudaSuccess && !src.empty())
-    e = cudaMemcpyAsync(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice, st);
+    e = cudaMemcpyAsync(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice,
+                        ctx->stream);
   return e;
 }
 
@@ -97,7 +98,13 @@ int prepare(acdc_problem* p, const SolveOpts& o, int wpb_cap) {
 class BatchEngine {
  public:
   explicit BatchEngine(acdc_ctx* ctx) : ctx_(ctx) {}
-  ~BatchEngine() { release(); }
+  ~BatchEngine() {
+    release();
+    if (h_live_) {
+      cudaStreamSynchronize(ctx_->stream);  // the last copy into h_live_ has landed
+      cudaFreeHost(h_live_);
+    }
+  }
 
   // Slot i solves problems[i] along lambdas[i*path .. i*path+path-1].
   int build(const std::vector<acdc_problem*>& probs, const std::vector<double>& lambdas, int path,
@@ -112,9 +119,9 @@ class BatchEngine {
     std::vector<SlotCtl> ctl((size_t)count);
     std::vector<int32_t> ublk_slot, ublk_first((size_t)count), eblk_slot, eblk_first((size_t)count),
         eblk_count((size_t)count);
-    ACDC_CK(ctx_, upload(&lambdas_, lambdas, st));
+    ACDC_CK(ctx_, upload(ctx_, &lambdas_, lambdas));
     const size_t rows = (size_t)count * path * ACDC_BATCH_RESULT_LEN;
-    ACDC_CK(ctx_, cudaMalloc((void**)&results_, sizeof(double) * std::max<size_t>(1, rows)));
+    ACDC_CK(ctx_, acdc_dev_alloc(ctx_, (void**)&results_, sizeof(double) * std::max<size_t>(1, rows)));
     ACDC_CK(ctx_, cudaMemsetAsync(results_, 0, sizeof(double) * std::max<size_t>(1, rows), st));
     for (int i = 0; i < count; ++i) {
       acdc_problem* p = probs[(size_t)i];
@@ -196,15 +203,15 @@ class BatchEngine {
       for (int b = 0; b < eblk_count[(size_t)i]; ++b) eblk_slot.push_back(i);
       ACDC_CK(ctx_, cudaMemsetAsync(p->d.counters + CNT_WORK, 0, sizeof(unsigned long long), st));
     }
-    ACDC_CK(ctx_, upload(&up_dev_, up_, st));
-    ACDC_CK(ctx_, upload(&ep_dev_, ep, st));
-    ACDC_CK(ctx_, upload(&ctl_dev_, ctl, st));
-    ACDC_CK(ctx_, upload(&ublk_slot_, ublk_slot, st));
-    ACDC_CK(ctx_, upload(&ublk_first_, ublk_first, st));
-    ACDC_CK(ctx_, upload(&eblk_slot_, eblk_slot, st));
-    ACDC_CK(ctx_, upload(&eblk_first_, eblk_first, st));
-    ACDC_CK(ctx_, upload(&eblk_count_, eblk_count, st));
-    ACDC_CK(ctx_, upload(&live_, std::vector<int32_t>{count}, st));
+    ACDC_CK(ctx_, upload(ctx_, &up_dev_, up_));
+    ACDC_CK(ctx_, upload(ctx_, &ep_dev_, ep));
+    ACDC_CK(ctx_, upload(ctx_, &ctl_dev_, ctl));
+    ACDC_CK(ctx_, upload(ctx_, &ublk_slot_, ublk_slot));
+    ACDC_CK(ctx_, upload(ctx_, &ublk_first_, ublk_first));
+    ACDC_CK(ctx_, upload(ctx_, &eblk_slot_, eblk_slot));
+    ACDC_CK(ctx_, upload(ctx_, &eblk_first_, eblk_first));
+    ACDC_CK(ctx_, upload(ctx_, &eblk_count_, eblk_count));
+    ACDC_CK(ctx_, upload(ctx_, &live_, std::vector<int32_t>{count}));
     if (!h_live_) ACDC_CK(ctx_, cudaMallocHost((void**)&h_live_, sizeof(int32_t)));
     *h_live_ = count;
     bd_.up = up_dev_;
@@ -292,26 +299,22 @@ class BatchEngine {
   }
 
   void release() {
-    cudaFree(up_dev_);
-    cudaFree(ep_dev_);
-    cudaFree(ctl_dev_);
-    cudaFree(ublk_slot_);
-    cudaFree(ublk_first_);
-    cudaFree(eblk_slot_);
-    cudaFree(eblk_first_);
-    cudaFree(eblk_count_);
-    cudaFree(live_);
-    cudaFree(lambdas_);
-    cudaFree(results_);
+    acdc_dev_free(ctx_, up_dev_);
+    acdc_dev_free(ctx_, ep_dev_);
+    acdc_dev_free(ctx_, ctl_dev_);
+    acdc_dev_free(ctx_, ublk_slot_);
+    acdc_dev_free(ctx_, ublk_first_);
+    acdc_dev_free(ctx_, eblk_slot_);
+    acdc_dev_free(ctx_, eblk_first_);
+    acdc_dev_free(ctx_, eblk_count_);
+    acdc_dev_free(ctx_, live_);
+    acdc_dev_free(ctx_, lambdas_);
+    acdc_dev_free(ctx_, results_);
     up_dev_ = nullptr;
     ep_dev_ = nullptr;
     ctl_dev_ = nullptr;
     ublk_slot_ = ublk_first_ = eblk_slot_ = eblk_first_ = eblk_count_ = live_ = nullptr;
     lambdas_ = results_ = nullptr;
-    if (h_live_) {
-      cudaFreeHost(h_live_);
-      h_live_ = nullptr;
-    }
     count_ = 0;
   }
 
@@ -460,6 +463,12 @@ int64_t footprint_of(int64_t m, int64_t n, int64_t nnz) {
 }
 }  // namespace
 
+struct acdc_server;
+namespace {
+void admit_one(acdc_server* s, Request* r, const int64_t* col_ptr, const int32_t* row_idx,
+               const double* vals, const double* rhs);
+}  // namespace
+
 struct acdc_server {
   acdc_ctx* ctx = nullptr;
   acdc_server_options opt{};
@@ -503,11 +512,6 @@ extern "C" int acdc_server_submit(acdc_server* s, const acdc_request* req, int64
   r->loss = req->loss;
   r->m = req->m;
   r->n = req->n;
-  r->col_ptr.assign(req->col_ptr, req->col_ptr + req->n + 1);
-  r->row_idx.assign(req->row_idx, req->row_idx + nnz);
-  r->vals.assign(req->vals, req->vals + nnz);
-  const int64_t rhs_len = req->loss == ACDC_LOSS_L1_SQUARE ? req->m : req->n;
-  r->rhs.assign(req->rhs, req->rhs + rhs_len);
   r->lambda = req->lambda;
   r->gap_target = req->gap_target;
   r->seed = req->seed;
@@ -515,8 +519,23 @@ extern "C" int acdc_server_submit(acdc_server* s, const acdc_request* req, int64
   r->res.state = 0;
   r->res.submit_time = now_seconds();
   *ticket = r->ticket;
-  s->queue.push_back(r.get());
+  Request* rp = r.get();
   s->all[r->ticket] = std::move(r);
+  // Admitted at once when nothing waits ahead of it and a slot and the memory
+  // are free: the device copy is made from the caller's arrays.  Otherwise the
+  // request is copied (the caller's arrays are only read during this call) and
+  // waits in arrival order.
+  if (s->queue.empty() && (int32_t)s->resident.size() < s->opt.max_slots &&
+      s->used_bytes + fp <= s->opt.memory_budget_bytes) {
+    admit_one(s, rp, req->col_ptr, req->row_idx, req->vals, req->rhs);
+    return ACDC_OK;
+  }
+  rp->col_ptr.assign(req->col_ptr, req->col_ptr + req->n + 1);
+  rp->row_idx.assign(req->row_idx, req->row_idx + nnz);
+  rp->vals.assign(req->vals, req->vals + nnz);
+  const int64_t rhs_len = req->loss == ACDC_LOSS_L1_SQUARE ? req->m : req->n;
+  rp->rhs.assign(req->rhs, req->rhs + rhs_len);
+  s->queue.push_back(rp);
   return ACDC_OK;
 }
 
@@ -560,30 +579,41 @@ int retire_finished(acdc_server* s) {
   return ACDC_OK;
 }
 
+// Creates the device problem of request r from the given arrays and makes it
+// resident (or records the failure).
+void admit_one(acdc_server* s, Request* r, const int64_t* col_ptr, const int32_t* row_idx,
+               const double* vals, const double* rhs) {
+  acdc_problem* p = nullptr;
+  int rc = acdc_problem_create(s->ctx, r->loss, r->m, r->n, col_ptr, row_idx, vals, rhs,
+                               r->lambda, &p);
+  r->res.start_time = now_seconds();
+  if (rc != ACDC_OK) {
+    r->res.state = 3;
+    r->res.status = rc;
+    r->res.finish_time = r->res.start_time;
+    return;
+  }
+  p->s.seed = r->seed;
+  r->prob = p;
+  r->res.state = 1;
+  s->used_bytes += r->footprint;
+  s->resident.push_back(r);
+  s->dirty = true;
+}
+
 // Admits queued requests in arrival order while slots and memory allow.
 void admit(acdc_server* s) {
   while (!s->queue.empty() && (int32_t)s->resident.size() < s->opt.max_slots) {
     Request* r = s->queue.front();
     if (s->used_bytes + r->footprint > s->opt.memory_budget_bytes) break;
     s->queue.pop_front();
-    acdc_problem* p = nullptr;
-    int rc = acdc_problem_create(s->ctx, r->loss, r->m, r->n, r->col_ptr.data(),
-                                 r->row_idx.empty() ? nullptr : r->row_idx.data(),
-                                 r->vals.empty() ? nullptr : r->vals.data(), r->rhs.data(),
-                                 r->lambda, &p);
-    r->res.start_time = now_seconds();
-    if (rc != ACDC_OK) {
-      r->res.state = 3;
-      r->res.status = rc;
-      r->res.finish_time = r->res.start_time;
-      continue;
-    }
-    p->s.seed = r->seed;
-    r->prob = p;
-    r->res.state = 1;
-    s->used_bytes += r->footprint;
-    s->resident.push_back(r);
-    s->dirty = true;
+    admit_one(s, r, r->col_ptr.data(), r->row_idx.empty() ? nullptr : r->row_idx.data(),
+              r->vals.empty() ? nullptr : r->vals.data(), r->rhs.data());
+    // the host copy is no longer needed
+    std::vector<int64_t>().swap(r->col_ptr);
+    std::vector<int32_t>().swap(r->row_idx);
+    std::vector<double>().swap(r->vals);
+    std::vector<double>().swap(r->rhs);
   }
 }
 }  // namespace

@@ -362,8 +362,11 @@ typedef struct acdc_request_result {
 } acdc_request_result;
 
 int acdc_server_create(acdc_ctx* ctx, const acdc_server_options* opt, acdc_server** out);
-/* Copies the request's arrays; returns a ticket.  ACDC_EBUSY if the request can
- * never fit the memory budget. */
+/* Returns a ticket; the request's arrays are read only during the call.  When
+ * no request waits ahead of it and a slot and the memory budget are free, the
+ * request is admitted at once (its device copy made from the caller's arrays,
+ * state 1); otherwise its arrays are copied and it waits in arrival order
+ * (state 0).  ACDC_EBUSY if the request can never fit the memory budget. */
 int acdc_server_submit(acdc_server* s, const acdc_request* req, int64_t* ticket);
 /* Runs one scheduling round: admits queued requests that fit, advances every
  * resident request by quantum_epochs, retires converged ones.  Returns the
