@@ -103,6 +103,8 @@ def parse_args():
     ap.add_argument("--serve-requests", type=int, default=128,
                     help="requests of the serving sample (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=1000.0)
+    ap.add_argument("--serve-quantum", type=int, default=2,
+                    help="rounds per server step (acdc_server_options.quantum_epochs)")
     ap.add_argument("--probe-launches", action="store_true",
                     help="profiling aid: run one uniform-draw update launch (refresh_every "
                          "epochs) and one active-set launch (active_passes |A|/q updates) on "
@@ -220,16 +222,16 @@ def latency_summary(lat_s, span_s, conv, count):
             "converged": int(conv), "span_s": span_s}
 
 
-def run_serving(ctx, count, rate):
+def run_serving(ctx, count, rate, quantum=2):
     """Continuous batching (acdc_server_*) against the plain path (one request at
     a time through acdc_batch_solve_path with plain = 1) on the same arrivals;
     latency = finish - arrival, host monotonic clock."""
     import acdc
     import numpy as np
     reqs, arr = serve_sample(count, rate)
-    out = {"workload": "serve_mix_70_30", "requests": count, "rate_per_s": rate,
+    out = {"workload": "serve_mix_70_30", "requests": count, "rate_per_s": rate, "quantum_rounds": quantum,
            "gap_target": 1e-6, "nnz": int(sum(x.nnz for x in reqs))}
-    srv = acdc.Server(ctx, memory_budget_bytes=120 << 30, max_slots=256, quantum_rounds=2,
+    srv = acdc.Server(ctx, memory_budget_bytes=120 << 30, max_slots=256, quantum_rounds=quantum,
                       max_epochs=3000, use_shrinking=1)
     start = time.monotonic()
     tickets, nxt = {}, 0
@@ -569,7 +571,7 @@ def run_ours(args, w):
         if args.batch_instances > 0:
             batched = run_batched(ctx, args.batch_instances, args.batch_max_epochs)
         if args.serve_requests > 0:
-            serving = run_serving(ctx, args.serve_requests, args.serve_rate)
+            serving = run_serving(ctx, args.serve_requests, args.serve_rate, args.serve_quantum)
     if is_svm(w):
         solver_keys = {"gap_target_absolute": w["gap"], "q_shrinking": 0, "lambda": w["lam"]}
     else:
