@@ -143,6 +143,8 @@ def gpu_lib():
         L.acdc_ctx_destroy.argtypes = [VP]
         L.acdc_problem_create.argtypes = [VP, I32, I64, I64, VP, VP, VP, VP, D, C.POINTER(VP)]
         L.acdc_problem_create_i32.argtypes = [VP, I32, I64, I64, VP, VP, VP, VP, D, C.POINTER(VP)]
+        L.acdc_problem_create_rows.argtypes = [VP, I32, I64, I64, VP, VP, VP, VP, D,
+                                               C.POINTER(VP)]
         L.acdc_problem_destroy.argtypes = [VP]
         L.acdc_problem_info_get.argtypes = [VP, C.POINTER(ProblemInfo)]
         L.acdc_problem_set_settings.argtypes = [VP, C.POINTER(Settings)]
@@ -439,14 +441,20 @@ def default_settings(loss=LOSS_L1_SQUARE, **kw):
 
 
 class Problem:
-    """One problem resident on the device (x, residual and sampler state)."""
+    """One problem resident on the device (x, residual and sampler state).
 
-    def __init__(self, ctx, inst, settings=None, **kw):
+    With rows=True, inst holds A by rows: col_ptr is the row pointer (m + 1
+    entries) and row_idx the column indices (acdc_problem_create_rows)."""
+
+    def __init__(self, ctx, inst, settings=None, rows=False, **kw):
         self.ctx, self.L = ctx, ctx.L
         self.m, self.n, self.loss = inst.m, inst.n, inst.loss
         h = VP()
         cp = inst.col_ptr
-        if cp.dtype == np.int32:
+        if rows:
+            cp = np.ascontiguousarray(cp, np.int64)
+            fn = self.L.acdc_problem_create_rows
+        elif cp.dtype == np.int32:
             fn = self.L.acdc_problem_create_i32
         else:
             cp = np.ascontiguousarray(cp, np.int64)

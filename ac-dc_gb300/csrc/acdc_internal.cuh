@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -305,6 +306,15 @@ cudaError_t launch_test_accuracy(int64_t n_test, const int64_t* row_ptr, const i
                                  cudaStream_t st);
 // Hot list from the violations of the last evaluation; zeroes CNT_HOT first.
 cudaError_t launch_hot_set(const EvalParams& p, cudaStream_t st);
+// Compressed rows (m x n, row_ptr on the device) -> compressed columns with
+// the entries of each column in row order (transpose.cu).  col is checked
+// (an index outside [0, n) sets DEV_ERR_BAD_INDEX in *status) and, like val,
+// overwritten; scratch holds rows_to_columns_scratch_bytes bytes.
+int64_t rows_to_columns_scratch_bytes(int64_t m, int64_t n, int64_t nnz);
+cudaError_t launch_rows_to_columns(const int64_t* row_ptr, int32_t* col, double* val, int64_t m,
+                                   int64_t n, int64_t nnz, char* scratch, int64_t* col_ptr,
+                                   int32_t* rows_out, double* vals_out,
+                                   unsigned long long* status, cudaStream_t st);
 cudaError_t launch_debug_sample(uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
                                 int64_t* out, cudaStream_t st);
 // Batched round: update, refresh, gap and control kernels over every live slot.

@@ -315,20 +315,40 @@ int apply_settings(acdc_problem* p, const acdc_settings* s) {
   return ACDC_OK;
 }
 
+// Matrix given by rows (acdc_problem_create_rows): row_ptr[0..m], the column
+// index and value of every entry.
+struct RowsInput {
+  const int64_t* row_ptr;
+  const int32_t* col_idx;
+  const double* vals;
+};
+
 int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t* col_ptr64,
                 const int32_t* col_ptr32, const int32_t* row_idx, const double* vals,
-                const double* rhs, double lambda, acdc_problem** out) {
+                const double* rhs, double lambda, acdc_problem** out,
+                const RowsInput* by_rows = nullptr) {
   if (!ctx || !out) return ACDC_EINVAL;
   *out = nullptr;
   if (loss < ACDC_LOSS_L1_SQUARE || loss > ACDC_LOSS_LOGISTIC)
     return acdc_set_error(ctx, ACDC_EINVAL, "unknown loss code");
   if (m <= 0 || n <= 0 || m > INT32_MAX || n > INT32_MAX || !(lambda > 0) || !rhs ||
-      (!col_ptr64 && !col_ptr32))
+      (!by_rows && !col_ptr64 && !col_ptr32) || (by_rows && !by_rows->row_ptr))
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid sizes, lambda or null pointer");
-  const int64_t c0 = col_ptr64 ? col_ptr64[0] : col_ptr32[0];
-  const int64_t nnz = col_ptr64 ? col_ptr64[n] : col_ptr32[n];
-  if (c0 != 0 || nnz < 0) return acdc_set_error(ctx, ACDC_EINVAL, "col_ptr must start at 0 and end at nnz >= 0");
-  if (nnz > 0 && (!row_idx || !vals)) return acdc_set_error(ctx, ACDC_EINVAL, "null row_idx or vals");
+  int64_t nnz = 0;
+  if (by_rows) {
+    const int64_t* rp = by_rows->row_ptr;
+    if (rp[0] != 0) return acdc_set_error(ctx, ACDC_EINVAL, "row_ptr must start at 0");
+    for (int64_t i = 0; i < m; ++i)
+      if (rp[i + 1] < rp[i]) return acdc_set_error(ctx, ACDC_EINVAL, "decreasing row_ptr");
+    nnz = rp[m];
+    if (nnz > 0 && (!by_rows->col_idx || !by_rows->vals))
+      return acdc_set_error(ctx, ACDC_EINVAL, "null col_idx or vals");
+  } else {
+    const int64_t c0 = col_ptr64 ? col_ptr64[0] : col_ptr32[0];
+    nnz = col_ptr64 ? col_ptr64[n] : col_ptr32[n];
+    if (c0 != 0 || nnz < 0) return acdc_set_error(ctx, ACDC_EINVAL, "col_ptr must start at 0 and end at nnz >= 0");
+    if (nnz > 0 && (!row_idx || !vals)) return acdc_set_error(ctx, ACDC_EINVAL, "null row_idx or vals");
+  }
   ACDC_CK(ctx, cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
 
@@ -371,7 +391,35 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
   STEP(cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long) * CNT_SLOTS, st));
   STEP(dalloc(ctx, &s_colptr, n + 1, &stage_bytes));
   STEP(dalloc(ctx, &s_scratch, scratch_len, &stage_bytes));
-  if (col_ptr64) {
+  if (by_rows) {
+    // Upload the rows and transpose them on the device into the staging arrays.
+    int64_t* r_ptr = nullptr;
+    int32_t* r_col = nullptr;
+    double* r_val = nullptr;
+    char* t_scratch = nullptr;
+    cudaError_t e = dalloc(ctx, &r_ptr, m + 1, &stage_bytes);
+    if (e == cudaSuccess) e = dalloc(ctx, &r_col, nnz, &stage_bytes);
+    if (e == cudaSuccess) e = dalloc(ctx, &r_val, nnz, &stage_bytes);
+    if (e == cudaSuccess) e = dalloc(ctx, &t_scratch, rows_to_columns_scratch_bytes(m, n, nnz), &stage_bytes);
+    if (e == cudaSuccess) e = dalloc(ctx, &s_rows, nnz, &stage_bytes);
+    if (e == cudaSuccess) e = dalloc(ctx, &s_vals, nnz, &stage_bytes);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(r_ptr, by_rows->row_ptr, sizeof(int64_t) * (m + 1), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && nnz > 0)
+      e = cudaMemcpyAsync(r_col, by_rows->col_idx, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && nnz > 0)
+      e = cudaMemcpyAsync(r_val, by_rows->vals, sizeof(double) * nnz, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = launch_rows_to_columns(r_ptr, r_col, r_val, m, n, nnz, t_scratch, s_colptr, s_rows,
+                                 s_vals, d.counters + CNT_STATUS, st);
+    acdc_dev_free(ctx, r_ptr);
+    acdc_dev_free(ctx, r_col);
+    acdc_dev_free(ctx, r_val);
+    acdc_dev_free(ctx, t_scratch);
+    if (e != cudaSuccess) return fail(acdc_cuda_error(ctx, e, "rows to columns"));
+    rc = check_status_word(p);  // column indices out of range
+    if (rc != ACDC_OK) return fail(rc);
+  } else if (col_ptr64) {
     STEP(cudaMemcpyAsync(s_colptr, col_ptr64, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st));
   } else {
     // Stage the int32 pointers in the scratch area and widen them on the device.
@@ -379,7 +427,7 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
     STEP(cudaMemcpyAsync(tmp, col_ptr32, sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, st));
     STEP(launch_widen_i32(tmp, s_colptr, n + 1, st));
   }
-  if (nnz > 0) {
+  if (nnz > 0 && !by_rows) {
     STEP(dalloc(ctx, &s_rows, nnz, &stage_bytes));
     STEP(dalloc(ctx, &s_vals, nnz, &stage_bytes));
     STEP(cudaMemcpyAsync(s_rows, row_idx, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, st));
@@ -490,6 +538,14 @@ extern "C" int acdc_problem_create_i32(acdc_ctx* ctx, int32_t loss, int64_t m, i
                                        const double* vals, const double* rhs, double lambda,
                                        acdc_problem** out) {
   return create_impl(ctx, loss, m, n, nullptr, col_ptr, row_idx, vals, rhs, lambda, out);
+}
+
+extern "C" int acdc_problem_create_rows(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n,
+                                        const int64_t* row_ptr, const int32_t* col_idx,
+                                        const double* vals, const double* rhs, double lambda,
+                                        acdc_problem** out) {
+  RowsInput r{row_ptr, col_idx, vals};
+  return create_impl(ctx, loss, m, n, nullptr, nullptr, nullptr, nullptr, rhs, lambda, out, &r);
 }
 
 extern "C" int acdc_problem_destroy(acdc_problem* p) {

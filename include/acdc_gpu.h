@@ -200,6 +200,17 @@ int acdc_problem_create(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const
 int acdc_problem_create_i32(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n,
                             const int32_t* col_ptr, const int32_t* row_idx, const double* vals,
                             const double* rhs, double lambda, acdc_problem** out);
+/* The same matrix A (m x n) given by rows: row_ptr[0..m] (row i's entries at
+ * row_ptr[i]..row_ptr[i+1]-1), their column indices col_idx (0-based, < n)
+ * and values.  The device turns the rows into its column layout, keeping each
+ * column's entries in row order: the transposition the reference makes on the
+ * host for the logistic loss (getCSR_from_CSC, helpers/matrix_conversions.h:65-104,
+ * at frontends/solvers/MultiCoreSolver.cpp:89-93), so LIBSVM rows (samples x
+ * features, labels as rhs) go in as read.  A column index outside [0, n)
+ * returns ACDC_EDEVICE. */
+int acdc_problem_create_rows(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n,
+                             const int64_t* row_ptr, const int32_t* col_idx, const double* vals,
+                             const double* rhs, double lambda, acdc_problem** out);
 int acdc_problem_destroy(acdc_problem* p);
 int acdc_problem_info_get(acdc_problem* p, acdc_problem_info* info);
 
