@@ -14,6 +14,7 @@
 // parsed but not used by this path.
 #include <getopt.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <iostream>
@@ -67,21 +68,10 @@ bool load(int loss, const std::string& a, const std::string& b, double lambda,
     inst.m = (int)d;
     inst.n = (int)n;
     if (loss == 3) {
-      // MultiCoreSolver.cpp:80-105: the samples become the rows of a CSC matrix
-      // over the features (m = samples, n = features).
-      std::vector<int> cnt((size_t)d + 1, 0);
-      for (int64_t e = 0; e < nnz; ++e) cnt[(size_t)ci[(size_t)e] + 1]++;
-      for (int64_t f = 0; f < d; ++f) cnt[(size_t)f + 1] += cnt[(size_t)f];
-      inst.A_csc_col_ptr.assign(cnt.begin(), cnt.end());
-      inst.A_csc_row_idx.assign((size_t)nnz, 0);
-      inst.A_csc_values.assign((size_t)nnz, 0.0);
-      std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-      for (int64_t i = 0; i < n; ++i)
-        for (int64_t e = rp[(size_t)i]; e < rp[(size_t)i + 1]; ++e) {
-          const int f = ci[(size_t)e];
-          inst.A_csc_row_idx[(size_t)fill[(size_t)f]] = (int)i;
-          inst.A_csc_values[(size_t)fill[(size_t)f]++] = inst.A_csr_values[(size_t)e];
-        }
+      // MultiCoreSolver.cpp:80-105 turns the samples into the rows of a CSC
+      // matrix over the features (m = samples, n = features).  Here the sample
+      // rows stay as read: the engine transposes them on the device
+      // (acdc_problem_create_rows) instead of getCSR_from_CSC on the host.
       inst.m = (int)n;
       inst.n = (int)d;
     }
@@ -135,12 +125,17 @@ int main(int argc, char* argv[]) {
   std::cout << "Data loaded with size: " << instance.m << " x " << instance.n << std::endl;
   // omega = largest number of entries in one residual row (MultiCoreSolver.cpp:32-38, 55-62;
   // for -f 3 the longest sample, :98-103)
-  const std::vector<int>& idx =
-      settings.lossFunction == 2 ? instance.A_csr_col_idx : instance.A_csc_row_idx;
-  std::vector<int> rows((size_t)instance.m, 0);
   double omega = 1;
-  for (int r : idx)
-    if (++rows[(size_t)r] > omega) omega = rows[(size_t)r];
+  if (settings.lossFunction == 3) {
+    for (int i = 0; i < instance.m; ++i)
+      omega = std::max<double>(omega, instance.A_csr_row_ptr[(size_t)i + 1] - instance.A_csr_row_ptr[(size_t)i]);
+  } else {
+    const std::vector<int>& idx =
+        settings.lossFunction == 2 ? instance.A_csr_col_idx : instance.A_csc_row_idx;
+    std::vector<int> rows((size_t)instance.m, 0);
+    for (int r : idx)
+      if (++rows[(size_t)r] > omega) omega = rows[(size_t)r];
+  }
   instance.omega = omega;
   instance.sigma = 1 + (omega - 1) * (settings.totalThreads - 1) / (instance.n - 1.0);
   std::cout << "Omega: " << omega << std::endl;

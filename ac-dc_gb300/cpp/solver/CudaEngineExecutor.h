@@ -64,21 +64,31 @@ class CudaEngineExecutor : public AbstractEngineExecutor<L, D> {
     check(acdc_ctx_create(opt.device, &ctx_), "acdc_ctx_create");
     // Losses 0, 1 and 3 read the CSC arrays (for 3 after MultiCoreSolver.cpp:80-105
     // turned the samples into rows), the SVM dual the CSR by sample
-    // (MulticoreEngineExecutor.h:32-58).
-    const bool csc = loss_ != ACDC_LOSS_SVM_DUAL;
+    // (MulticoreEngineExecutor.h:32-58).  For loss 3 without the CSC arrays the
+    // sample rows (A_csr_*, m = samples) are transposed on the device.
+    const int64_t n = (int64_t)inst.n;
+    const bool rows = loss_ == ACDC_LOSS_LOGISTIC && inst.A_csc_col_ptr.empty();
+    const bool csc = loss_ != ACDC_LOSS_SVM_DUAL && !rows;
     const std::vector<L>& ptr = csc ? inst.A_csc_col_ptr : inst.A_csr_row_ptr;
     const std::vector<L>& idx = csc ? inst.A_csc_row_idx : inst.A_csr_col_idx;
     const std::vector<D>& val = csc ? inst.A_csc_values : inst.A_csr_values;
-    const int64_t n = (int64_t)inst.n;
-    if ((int64_t)ptr.size() != n + 1) throw std::runtime_error("column pointers do not match n");
+    const int64_t ptr_len = rows ? (int64_t)inst.m + 1 : n + 1;
+    if ((int64_t)ptr.size() != ptr_len) throw std::runtime_error("pointer array does not match the sizes");
     std::vector<int64_t> cp(ptr.begin(), ptr.end());
     std::vector<int32_t> ri(idx.begin(), idx.end());
     std::vector<double> va(val.begin(), val.end());
     std::vector<double> rhs(inst.b.begin(), inst.b.end());
-    check(acdc_problem_create(ctx_, loss_, (int64_t)inst.m, n, cp.data(),
-                              ri.empty() ? nullptr : ri.data(), va.empty() ? nullptr : va.data(),
-                              rhs.data(), (double)inst.lambda, &prob_),
-          "acdc_problem_create");
+    if (rows)
+      check(acdc_problem_create_rows(ctx_, loss_, (int64_t)inst.m, n, cp.data(),
+                                     ri.empty() ? nullptr : ri.data(),
+                                     va.empty() ? nullptr : va.data(), rhs.data(),
+                                     (double)inst.lambda, &prob_),
+            "acdc_problem_create_rows");
+    else
+      check(acdc_problem_create(ctx_, loss_, (int64_t)inst.m, n, cp.data(),
+                                ri.empty() ? nullptr : ri.data(), va.empty() ? nullptr : va.data(),
+                                rhs.data(), (double)inst.lambda, &prob_),
+            "acdc_problem_create");
     acdc_settings st;
     acdc_settings_default(&st);
     st.loss = loss_;
