@@ -300,7 +300,7 @@ int apply_settings(acdc_problem* p, const acdc_settings* s) {
       s->max_epochs < 0 || !(s->gap_target >= 0) || s->shrinking_probability < 0 ||
       s->shrinking_probability > 1 || s->shrink_eps < 0 || s->shrink_eps >= 1 ||
       s->precision < ACDC_PREC_AUTO || s->precision > ACDC_PREC_FP64 || !(s->polish_rel_gap >= 0) ||
-      !(s->hot_threshold >= 0) || s->polish_stall_epochs < 0)
+      !(s->hot_threshold >= 0) || s->polish_stall_epochs < 0 || s->hot_sweeps < 0)
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid settings value");
   p->s = *s;
   // q-shrinking and its screened evaluations cover losses 0 and 2 only.
@@ -817,6 +817,21 @@ extern "C" int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_t
     if (p->fp64_mode) done_fp64 += count;
     p->updates_done += count;
     p->epochs_done = (int64_t)(p->updates_done / n);
+    if (shrink && p->s.hot_sweeps > 0 && p->hot_count > 0) {
+      // One warp through the hot list with exact steps: Li = 1/(beta ||a||^2)
+      // scaled by beta, nothing else in flight.
+      const uint64_t sweep = (uint64_t)p->s.hot_sweeps * (uint64_t)p->hot_count;
+      UpdateParams h = update_params(p, sweep, true);
+      h.shrink_q32 = 0xffffffffu;
+      h.hot_q32 = 0xffffffffu;
+      h.li_scale_hot = p->beta;
+      h.n_warps = 1;
+      ACDC_CK(ctx, launch_update(h, p->k_next, 1, ctx->stream));
+      p->k_next += sweep;
+      done += sweep;
+      if (p->fp64_mode) done_fp64 += sweep;
+      p->updates_done += sweep;
+    }
     const bool screened_now = screen && p->screen_valid;
     rc = evaluate_impl(p, &ev, &ev_ms, screen);
     if (rc != ACDC_OK) return rc;

@@ -97,7 +97,11 @@ typedef struct acdc_settings {
   int32_t polish_stall_epochs;     /* AUTO: also switch to FP64 once the relative
                                      gap (below 1e-2) has not halved over this
                                      many epochs; 0 = 10                          */
-  int32_t reserved;
+  int32_t hot_sweeps;             /* with the hot set: before each evaluation, one
+                                     warp makes hot_sweeps * |H| updates drawn from
+                                     the hot list with the exact step 1/||a_j||^2
+                                     (nothing else in flight), so the evaluation
+                                     sees the hot columns settled; 0 = off        */
   double hot_threshold;           /* Lasso with shrinking and screened_eval: after
                                      each evaluation the active columns whose KKT
                                      violation exceeds hot_threshold times the
