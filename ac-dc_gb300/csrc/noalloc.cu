@@ -1,13 +1,14 @@
 // acdc_debug_sample_noalloc: the sampler diagnostic of acdc_debug_sample
 // without any allocation.  acdc_debug_sample takes its device output buffer
-// from cudaMalloc on every call; this variant writes the draws into a fixed
-// device array of this file and copies them out of it.
+// from the context's memory pool on every call; this variant writes the draws
+// into a fixed device array of this file and copies them out of it.
 //
 // Who needs it: a caller that must not allocate device memory while it runs.
-// Two examples are a process whose device memory the server's admission budget
-// has already handed to resident problems, where a cudaMalloc may fail, and a
-// caller checking the sampler while solves run on other streams, where
-// cudaFree would synchronise the whole device and stall them.
+// One example is a process whose device memory the server's admission budget
+// has already handed to resident problems: any new allocation may fail there,
+// or grow the pool past the budget.  Another is a caller checking the sampler
+// while solves run, which wants no allocation call on their stream (growing
+// the pool is a driver call).
 //
 // Scratch: ACDC_NOALLOC_MAX_SAMPLES int64 draws (512 KiB) and one status word,
 // both file-scope __device__ arrays of this module.  Their device addresses

@@ -297,10 +297,10 @@ int acdc_debug_sample(acdc_ctx* ctx, uint64_t seed, uint64_t k0, uint64_t count,
 /* acdc_debug_sample without any allocation (no counterpart in the reference,
  * whose sampler is a host GSL call), for callers that must not allocate device
  * memory while they run: one whose memory is already committed to resident
- * problems (a cudaMalloc may fail), or one checking the sampler beside running
- * solves (cudaFree would synchronise the device and stall them).  The draws go
- * to a fixed device array of
- * ACDC_NOALLOC_MAX_SAMPLES entries (512 KiB) instead of a per-call cudaMalloc;
+ * problems (an allocation may fail, or grow the context's pool past the
+ * budget), or one checking the sampler beside running solves that wants no
+ * allocation call on their stream.  The draws go to a fixed device array of
+ * ACDC_NOALLOC_MAX_SAMPLES entries (512 KiB) instead of a per-call allocation;
  * count beyond that returns ACDC_EINVAL.  The first call on a device looks up
  * the array's address (cudaGetSymbolAddress, may load the module): make it
  * before any stream capture.  One array per device: calls that overlap on a

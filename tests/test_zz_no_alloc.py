@@ -1,7 +1,7 @@
 """acdc_debug_sample_noalloc against acdc_debug_sample.  The no-allocation
 variant serves callers that must not allocate device memory while they run (a
 process whose memory is committed to resident problems, or one checking the
-sampler beside running solves, where cudaFree would synchronise the device).
+sampler beside running solves that wants no allocation call on their stream).
 Through the C-ABI it must return the same draws as the allocating entry point
 on two calls in a row (the fixed scratch keeps the previous call's contents),
 and refuse counts beyond its scratch.  Collected last, so a run that stops at
