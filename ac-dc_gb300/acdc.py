@@ -30,7 +30,7 @@ class Settings(C.Structure):
                 ("max_epochs", I32), ("use_shrinking", I32), ("shrinking_starting_iter", I32),
                 ("shrinking_probability", D), ("shrink_eps", D), ("precision", I32),
                 ("tau_active", I32), ("polish_rel_gap", D), ("active_passes", I32),
-                ("screened_eval", I32), ("polish_stall_epochs", I32), ("hot_sweeps", I32),
+                ("screened_eval", I32), ("polish_stall_epochs", I32), ("hot_polish_sweeps", I32),
                 ("hot_threshold", D)]
 
 

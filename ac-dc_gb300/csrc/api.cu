@@ -61,6 +61,7 @@ extern "C" void acdc_settings_default(acdc_settings* s) {
   s->polish_rel_gap = 1e-5;
   s->screened_eval = 1;
   s->hot_threshold = 0.1;
+  s->hot_polish_sweeps = 16;
 }
 
 // ---- context ----
@@ -300,7 +301,7 @@ int apply_settings(acdc_problem* p, const acdc_settings* s) {
       s->max_epochs < 0 || !(s->gap_target >= 0) || s->shrinking_probability < 0 ||
       s->shrinking_probability > 1 || s->shrink_eps < 0 || s->shrink_eps >= 1 ||
       s->precision < ACDC_PREC_AUTO || s->precision > ACDC_PREC_FP64 || !(s->polish_rel_gap >= 0) ||
-      !(s->hot_threshold >= 0) || s->polish_stall_epochs < 0 || s->hot_sweeps < 0)
+      !(s->hot_threshold >= 0) || s->polish_stall_epochs < 0 || s->hot_polish_sweeps < 0)
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid settings value");
   p->s = *s;
   // q-shrinking and its screened evaluations cover losses 0 and 2 only.
@@ -817,21 +818,6 @@ extern "C" int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_t
     if (p->fp64_mode) done_fp64 += count;
     p->updates_done += count;
     p->epochs_done = (int64_t)(p->updates_done / n);
-    if (shrink && p->s.hot_sweeps > 0 && p->hot_count > 0) {
-      // One warp through the hot list with exact steps: Li = 1/(beta ||a||^2)
-      // scaled by beta, nothing else in flight.
-      const uint64_t sweep = (uint64_t)p->s.hot_sweeps * (uint64_t)p->hot_count;
-      UpdateParams h = update_params(p, sweep, true);
-      h.shrink_q32 = 0xffffffffu;
-      h.hot_q32 = 0xffffffffu;
-      h.li_scale_hot = p->beta;
-      h.n_warps = 1;
-      ACDC_CK(ctx, launch_update(h, p->k_next, 1, ctx->stream));
-      p->k_next += sweep;
-      done += sweep;
-      if (p->fp64_mode) done_fp64 += sweep;
-      p->updates_done += sweep;
-    }
     const bool screened_now = screen && p->screen_valid;
     rc = evaluate_impl(p, &ev, &ev_ms, screen);
     if (rc != ACDC_OK) return rc;
@@ -846,6 +832,40 @@ extern "C" int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_t
       if (bound >= (1.0 - 0.5 * p->s.shrink_eps) * p->lambda) p->screen_valid = false;
       if (bound >= p->lambda && !converged(p->s, ev)) {
         rc = evaluate_impl(p, &ev, &extra_ms);
+        if (rc != ACDC_OK) return rc;
+      }
+    }
+    if (p->s.hot_polish_sweeps > 0 && shrink && !p->fp64_mode && p->hot_count > 0 &&
+        !converged(p->s, ev) && ev.rel_gap < p->s.polish_rel_gap) {
+      // FP64 polish of the hot columns for the certificate.  The FP32 iterate
+      // moves x_j only in steps of its FP32 spacing, which can leave the few
+      // hot columns' KKT violations just above what the target needs.  So:
+      // x64 = x32 exactly (r64 of the evaluation above is exact for it), one
+      // warp of exact steps over the hot list in FP64 with nothing else in
+      // flight, then a new evaluation.  Kept if it meets the target; otherwise
+      // x goes back to FP32 (rounded) and the bulks continue.
+      rc = enter_fp64(p);
+      if (rc != ACDC_OK) return rc;
+      const uint64_t sweep = (uint64_t)p->s.hot_polish_sweeps * (uint64_t)p->hot_count;
+      UpdateParams h = update_params(p, sweep, true);
+      h.shrink_q32 = 0xffffffffu;
+      h.hot_q32 = 0xffffffffu;
+      h.li_scale_hot = p->beta;
+      h.n_warps = 1;
+      ACDC_CK(ctx, launch_update(h, p->k_next, 1, ctx->stream));
+      p->k_next += sweep;
+      done += sweep;
+      done_fp64 += sweep;
+      p->updates_done += sweep;
+      acdc_eval ev2;
+      float ms2 = 0;
+      rc = evaluate_impl(p, &ev2, &ms2, screen);
+      if (rc != ACDC_OK) return rc;
+      extra_ms += ms2;
+      if (converged(p->s, ev2)) {
+        ev = ev2;
+      } else {
+        rc = leave_fp64(p);
         if (rc != ACDC_OK) return rc;
       }
     }

@@ -577,7 +577,8 @@ def run_ours(args, w):
     else:
         solver_keys = {"gap_target_relative": w["gap"], "q_shrinking": 0.9,
                        "tau_active": w["tau_active"], "active_passes": w["active_passes"],
-                       "screened_eval": 1, "hot_threshold": 0.1}
+                       "screened_eval": 1, "hot_threshold": 0.1,
+                       "hot_polish_sweeps": 16, "polish_rel_gap": 1e-5}
     if rank == 0:
         line = {
             "metric": METRICS[w.get("loss", "lasso")], "value": value, "unit": "s", "n_gpus": world,
@@ -589,7 +590,7 @@ def run_ours(args, w):
             "config": dict(solver_keys, **{
                        "workload": args.workload, "m": w["m"], "n": w["n"], "nnz": inst.nnz,
                        "tau": w["tau"], "refresh_every": w["refresh_every"],
-                       "precision": "fp32 bulk, fp64 refresh and gap",
+                       "precision": "fp32 bulk; fp64 refresh, gap and hot-column polish",
                        "updates": int(updates), "update_launches": int(launches),
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (no flush)", "omega": info.omega,

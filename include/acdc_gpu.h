@@ -97,11 +97,16 @@ typedef struct acdc_settings {
   int32_t polish_stall_epochs;     /* AUTO: also switch to FP64 once the relative
                                      gap (below 1e-2) has not halved over this
                                      many epochs; 0 = 10                          */
-  int32_t hot_sweeps;             /* with the hot set: before each evaluation, one
-                                     warp makes hot_sweeps * |H| updates drawn from
-                                     the hot list with the exact step 1/||a_j||^2
-                                     (nothing else in flight), so the evaluation
-                                     sees the hot columns settled; 0 = off        */
+  int32_t hot_polish_sweeps;      /* with the hot set and x in FP32: at each
+                                     evaluation whose relative gap is below
+                                     polish_rel_gap, x is copied to FP64, one
+                                     warp makes hot_polish_sweeps * |H| updates
+                                     drawn from the hot list with the exact step
+                                     1/||a_j||^2 in FP64 (nothing else in
+                                     flight) and the gap is evaluated again: kept
+                                     if it meets the target (the solution is then
+                                     the FP64 x), else x is rounded back to FP32
+                                     and the bulks go on.  0 = off, default 16    */
   double hot_threshold;           /* Lasso with shrinking and screened_eval: after
                                      each evaluation the active columns whose KKT
                                      violation exceeds hot_threshold times the
