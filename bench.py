@@ -190,7 +190,7 @@ def run_batched(ctx, count, max_epochs):
     return out
 
 
-def serve_sample(count, rate, seed=0xACDC0004, scale=0.25):
+def serve_sample(count, rate, seed=0xACDC0004, scale=0.25, pinned=True):
     """Requests of the serving workload: 70% Lasso of the lambda-path mix's size
     distribution (m, n scaled by `scale`, lambda = lambda_max / 2), 30% SVM duals
     from the SVM generator scaled down (samples log-uniform in [1,000, 50,000 x
@@ -205,11 +205,13 @@ def serve_sample(count, rate, seed=0xACDC0004, scale=0.25):
             m, n = acdc.mix_sizes(seed, i, m_lo=500, m_hi=int(50000 * scale), n_lo=1000,
                                   n_hi=int(200000 * scale))
             reqs.append(acdc.gen_lasso(m, n, nnz_mode=acdc.NNZ_UNIFORM, nnz_min=5, nnz_max=50,
-                                       n_star=max(1, n // 100), lambda_frac=0.5, seed=seed + i))
+                                       n_star=max(1, n // 100), lambda_frac=0.5, seed=seed + i,
+                                       pinned=pinned))
         else:
             _, ns = acdc.mix_sizes(seed + 0x10, i, n_lo=1000, n_hi=int(50000 * scale))
             reqs.append(acdc.gen_svm(ns, 10 * ns, nnz_median=100, nnz_sigma=0.8,
-                                     w_star_nnz=max(10, ns // 20), lam=1e-3, seed=seed + 0x10 + i))
+                                     w_star_nnz=max(10, ns // 20), lam=1e-3, seed=seed + 0x10 + i,
+                                     pinned=pinned))
     arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
     return reqs, arrivals
 
@@ -230,6 +232,7 @@ def run_serving(ctx, count, rate, quantum=2):
     import numpy as np
     reqs, arr = serve_sample(count, rate)
     out = {"workload": "serve_mix_70_30", "requests": count, "rate_per_s": rate, "quantum_rounds": quantum,
+           "request_buffers": "pinned host memory (both paths)",
            "gap_target": 1e-6, "nnz": int(sum(x.nnz for x in reqs))}
     srv = acdc.Server(ctx, memory_budget_bytes=120 << 30, max_slots=256, quantum_rounds=quantum,
                       max_epochs=3000, use_shrinking=1)
