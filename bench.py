@@ -100,9 +100,9 @@ def parse_args():
     ap.add_argument("--batch-instances", type=int, default=8,
                     help="instances of the batched lambda-path sample (0 = skip)")
     ap.add_argument("--batch-max-epochs", type=int, default=300)
-    ap.add_argument("--serve-requests", type=int, default=128,
+    ap.add_argument("--serve-requests", type=int, default=256,
                     help="requests of the serving sample (0 = skip)")
-    ap.add_argument("--serve-rate", type=float, default=1000.0)
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--serve-quantum", type=int, default=2,
                     help="rounds per server step (acdc_server_options.quantum_epochs)")
     ap.add_argument("--probe-launches", action="store_true",
