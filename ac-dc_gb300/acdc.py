@@ -89,6 +89,15 @@ class ServerOptions(C.Structure):
                 ("max_epochs", I32), ("use_shrinking", I32), ("reserved", I32 * 6)]
 
 
+class ServerStats(C.Structure):
+    _fields_ = [("steps", I64), ("builds", I64), ("rounds", I64), ("admitted", I64),
+                ("retired", I64), ("admit_s", D), ("build_s", D), ("rounds_s", D),
+                ("retire_s", D)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class Request(C.Structure):
     _fields_ = [("loss", I32), ("reserved0", I32), ("m", I64), ("n", I64), ("col_ptr", VP),
                 ("row_idx", VP), ("vals", VP), ("rhs", VP), ("lambda_", D), ("gap_target", D),
@@ -164,6 +173,7 @@ def gpu_lib():
         L.acdc_debug_sample.argtypes = [VP, U64, U64, U64, I64, VP]
         L.acdc_test_accuracy.argtypes = [VP, I64, VP, VP, VP, VP, C.POINTER(D)]
         L.acdc_debug_sample_noalloc.argtypes = [VP, U64, U64, U64, I64, VP]
+        L.acdc_server_get_stats.argtypes = [VP, C.c_void_p]
         L.acdc_batch_solve_path.argtypes = [VP, I32, VP, VP, C.POINTER(BatchOptions), VP, VP]
         L.acdc_server_create.argtypes = [VP, C.POINTER(ServerOptions), C.POINTER(VP)]
         L.acdc_server_submit.argtypes = [VP, C.POINTER(Request), C.POINTER(I64)]
@@ -592,6 +602,11 @@ class Server:
         pend = I32()
         self.ctx.check(self.L.acdc_server_step(self.h, C.byref(pend)))
         return pend.value
+
+    def stats(self):
+        st = ServerStats()
+        self.ctx.check(self.L.acdc_server_get_stats(self.h, C.byref(st)))
+        return st.as_dict()
 
     def poll(self, ticket, want_x=False):
         res = RequestResult()

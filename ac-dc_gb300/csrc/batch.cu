@@ -266,10 +266,11 @@ class BatchEngine {
   }
 
   // Runs rounds without a graph (the slot set changes between calls).
-  int run_rounds(int rounds) {
+  int run_rounds(int rounds, int64_t* count = nullptr) {
     for (int r = 0; r < rounds && *h_live_ > 0; ++r) {
       ACDC_CK(ctx_, enqueue_round());
       ACDC_CK(ctx_, cudaStreamSynchronize(ctx_->stream));
+      if (count) ++*count;
     }
     return ACDC_OK;
   }
@@ -479,6 +480,7 @@ struct acdc_server {
   std::map<int64_t, std::unique_ptr<Request>> all;
   BatchEngine* engine = nullptr;
   bool dirty = true;                        // resident set changed since the last build
+  acdc_server_stats stats{};
 };
 
 extern "C" int acdc_server_create(acdc_ctx* ctx, const acdc_server_options* opt, acdc_server** out) {
@@ -573,6 +575,7 @@ int retire_finished(acdc_server* s) {
     r->res.finish_time = now_seconds();
     r->res.state = r->res.status == ACDC_OK ? 2 : 3;
     changed = true;
+    s->stats.retired++;
   }
   s->resident.swap(keep);
   if (changed) s->dirty = true;
@@ -583,10 +586,12 @@ int retire_finished(acdc_server* s) {
 // resident (or records the failure).
 void admit_one(acdc_server* s, Request* r, const int64_t* col_ptr, const int32_t* row_idx,
                const double* vals, const double* rhs) {
+  const double t0 = now_seconds();
   acdc_problem* p = nullptr;
   int rc = acdc_problem_create(s->ctx, r->loss, r->m, r->n, col_ptr, row_idx, vals, rhs,
                                r->lambda, &p);
   r->res.start_time = now_seconds();
+  s->stats.admit_s += r->res.start_time - t0;
   if (rc != ACDC_OK) {
     r->res.state = 3;
     r->res.status = rc;
@@ -599,6 +604,7 @@ void admit_one(acdc_server* s, Request* r, const int64_t* col_ptr, const int32_t
   s->used_bytes += r->footprint;
   s->resident.push_back(r);
   s->dirty = true;
+  s->stats.admitted++;
 }
 
 // Admits queued requests in arrival order while slots and memory allow.
@@ -636,16 +642,30 @@ extern "C" int acdc_server_step(acdc_server* s, int32_t* pending) {
         lams.push_back(r->lambda);
         targets.push_back(r->gap_target);
       }
+      const double t0 = now_seconds();
       int rc = s->engine->build(probs, lams, 1, o, &targets);
       if (rc) return rc;
       s->dirty = false;
+      s->stats.builds++;
+      s->stats.build_s += now_seconds() - t0;
     }
-    int rc = s->engine->run_rounds(s->opt.quantum_epochs);
+    double t0 = now_seconds();
+    int rc = s->engine->run_rounds(s->opt.quantum_epochs, &s->stats.rounds);
     if (rc) return rc;
+    double t1 = now_seconds();
+    s->stats.rounds_s += t1 - t0;
     rc = retire_finished(s);
     if (rc) return rc;
+    s->stats.retire_s += now_seconds() - t1;
   }
+  s->stats.steps++;
   if (pending) *pending = (int32_t)(s->queue.size() + s->resident.size());
+  return ACDC_OK;
+}
+
+extern "C" int acdc_server_get_stats(acdc_server* s, acdc_server_stats* out) {
+  if (!s || !out) return ACDC_EINVAL;
+  *out = s->stats;
   return ACDC_OK;
 }
 

@@ -254,6 +254,7 @@ def run_serving(ctx, count, rate, quantum=2):
         lat.append(res.finish_time - (start + arr[i]))
         fin.append(res.finish_time - start)
         conv += res.converged
+    out["server_stats"] = srv.stats()
     srv.close()
     out["server"] = latency_summary(lat, max(fin) - arr[0], conv, count)
     start = time.monotonic()

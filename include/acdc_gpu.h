@@ -398,6 +398,22 @@ int acdc_server_poll(acdc_server* s, int64_t ticket, acdc_request_result* res, d
 int acdc_server_release(acdc_server* s, int64_t ticket);
 int acdc_server_destroy(acdc_server* s);
 
+/* Where the server's host time went since its creation (seconds on the host
+ * monotonic clock; each phase includes the device work it waits for).  No
+ * counterpart in the reference, which has no server. */
+typedef struct acdc_server_stats {
+  int64_t steps;            /* acdc_server_step calls                             */
+  int64_t builds;           /* slot-table rebuilds (the resident set changed)     */
+  int64_t rounds;           /* rounds run                                         */
+  int64_t admitted;         /* requests made resident                             */
+  int64_t retired;          /* requests finished and released from the device    */
+  double admit_s;           /* device copies and layouts of admitted requests    */
+  double build_s;           /* slot-table rebuilds                                */
+  double rounds_s;          /* rounds                                             */
+  double retire_s;          /* result collection, x read-back, device release     */
+} acdc_server_stats;
+int acdc_server_get_stats(acdc_server* s, acdc_server_stats* out);
+
 #ifdef __cplusplus
 }
 #endif
