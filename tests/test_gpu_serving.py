@@ -62,6 +62,10 @@ def test_each_result_is_the_same_alone_and_in_the_mix(ctx):
         assert res.submit_time <= res.start_time <= res.finish_time
         r_alone, x_alone = alone(ctx, inst)
         check_same(res, x, r_alone, x_alone, inst)
+    st = server.stats()
+    assert st["admitted"] == st["retired"] == len(insts)
+    assert st["steps"] >= 2 and st["builds"] >= 2 and st["rounds"] >= st["builds"]
+    assert min(st["admit_s"], st["build_s"], st["rounds_s"], st["retire_s"]) > 0
     for t in tickets:
         server.release(t)
     server.close()
