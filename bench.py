@@ -103,7 +103,7 @@ def parse_args():
     ap.add_argument("--serve-requests", type=int, default=256,
                     help="requests of the serving sample (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
-    ap.add_argument("--serve-quantum", type=int, default=2,
+    ap.add_argument("--serve-quantum", type=int, default=4,
                     help="rounds per server step (acdc_server_options.quantum_epochs)")
     ap.add_argument("--probe-launches", action="store_true",
                     help="profiling aid: run one uniform-draw update launch (refresh_every "
@@ -224,7 +224,7 @@ def latency_summary(lat_s, span_s, conv, count):
             "converged": int(conv), "span_s": span_s}
 
 
-def run_serving(ctx, count, rate, quantum=2):
+def run_serving(ctx, count, rate, quantum=4):
     """Continuous batching (acdc_server_*) against the plain path (one request at
     a time through acdc_batch_solve_path with plain = 1) on the same arrivals;
     latency = finish - arrival, host monotonic clock."""
