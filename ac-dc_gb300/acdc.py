@@ -31,7 +31,7 @@ class Settings(C.Structure):
                 ("shrinking_probability", D), ("shrink_eps", D), ("precision", I32),
                 ("tau_active", I32), ("polish_rel_gap", D), ("active_passes", I32),
                 ("screened_eval", I32), ("polish_stall_epochs", I32), ("hot_polish_sweeps", I32),
-                ("hot_threshold", D)]
+                ("hot_threshold", D), ("polish_active_passes", I32), ("reserved2", I32)]
 
 
 class Eval(C.Structure):

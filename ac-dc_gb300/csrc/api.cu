@@ -301,7 +301,8 @@ int apply_settings(acdc_problem* p, const acdc_settings* s) {
       s->max_epochs < 0 || !(s->gap_target >= 0) || s->shrinking_probability < 0 ||
       s->shrinking_probability > 1 || s->shrink_eps < 0 || s->shrink_eps >= 1 ||
       s->precision < ACDC_PREC_AUTO || s->precision > ACDC_PREC_FP64 || !(s->polish_rel_gap >= 0) ||
-      !(s->hot_threshold >= 0) || s->polish_stall_epochs < 0 || s->hot_polish_sweeps < 0)
+      !(s->hot_threshold >= 0) || s->polish_stall_epochs < 0 || s->hot_polish_sweeps < 0 ||
+      s->polish_active_passes < 0)
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid settings value");
   p->s = *s;
   // q-shrinking and its screened evaluations cover losses 0 and 2 only.
@@ -846,6 +847,17 @@ extern "C" int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_t
       // x goes back to FP32 (rounded) and the bulks continue.
       rc = enter_fp64(p);
       if (rc != ACDC_OK) return rc;
+      if (p->s.polish_active_passes > 0 && ev.active > 0) {
+        const double q = std::max(1e-3, p->s.shrinking_probability);
+        const uint64_t cnt =
+            (uint64_t)((double)p->s.polish_active_passes * (double)ev.active / q);
+        UpdateParams a = update_params(p, cnt, true);
+        ACDC_CK(ctx, launch_update(a, p->k_next, p->s.warps_per_block, ctx->stream));
+        p->k_next += cnt;
+        done += cnt;
+        done_fp64 += cnt;
+        p->updates_done += cnt;
+      }
       const uint64_t sweep = (uint64_t)p->s.hot_polish_sweeps * (uint64_t)p->hot_count;
       UpdateParams h = update_params(p, sweep, true);
       h.shrink_q32 = 0xffffffffu;

@@ -116,6 +116,11 @@ typedef struct acdc_settings {
                                      (at most half of the active-set draws,
                                      ESO-scaled for the hot set); 0 = off,
                                      default 0.1                                  */
+  int32_t polish_active_passes;   /* with hot_polish_sweeps: before the hot sweep,
+                                     this many passes (|A|/q updates each) of the
+                                     q-shrinking draws in FP64, tau_active in
+                                     flight; 0 = none                              */
+  int32_t reserved2;
 } acdc_settings;
 
 /* precision: FP32 x and residual with FP64 refresh and gap (FP32), the same
