@@ -62,6 +62,7 @@ extern "C" void acdc_settings_default(acdc_settings* s) {
   s->screened_eval = 1;
   s->hot_threshold = 0.1;
   s->hot_polish_sweeps = 16;
+  s->polish_active_passes = 2;
 }
 
 // ---- context ----
@@ -838,13 +839,14 @@ extern "C" int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_t
     }
     if (p->s.hot_polish_sweeps > 0 && shrink && !p->fp64_mode && p->hot_count > 0 &&
         !converged(p->s, ev) && ev.rel_gap < p->s.polish_rel_gap) {
-      // FP64 polish of the hot columns for the certificate.  The FP32 iterate
-      // moves x_j only in steps of its FP32 spacing, which can leave the few
-      // hot columns' KKT violations just above what the target needs.  So:
-      // x64 = x32 exactly (r64 of the evaluation above is exact for it), one
-      // warp of exact steps over the hot list in FP64 with nothing else in
-      // flight, then a new evaluation.  Kept if it meets the target; otherwise
-      // x goes back to FP32 (rounded) and the bulks continue.
+      // FP64 polish for the certificate.  The FP32 iterate moves x_j only in
+      // steps of its FP32 spacing, which can leave KKT violations just above
+      // what the target needs.  So: x64 = x32 exactly (r64 of the evaluation
+      // above is exact for it), polish_active_passes passes of the usual
+      // q-shrinking draws in FP64, one warp of exact steps over the hot list in
+      // FP64 with nothing else in flight, then a new evaluation.  Kept if it
+      // meets the target; otherwise x goes back to FP32 (rounded) and the
+      // bulks continue.
       rc = enter_fp64(p);
       if (rc != ACDC_OK) return rc;
       if (p->s.polish_active_passes > 0 && ev.active > 0) {

@@ -582,7 +582,8 @@ def run_ours(args, w):
         solver_keys = {"gap_target_relative": w["gap"], "q_shrinking": 0.9,
                        "tau_active": w["tau_active"], "active_passes": w["active_passes"],
                        "screened_eval": 1, "hot_threshold": 0.1,
-                       "hot_polish_sweeps": 16, "polish_rel_gap": 1e-5}
+                       "hot_polish_sweeps": 16, "polish_active_passes": 2,
+                       "polish_rel_gap": 1e-5}
     if rank == 0:
         line = {
             "metric": METRICS[w.get("loss", "lasso")], "value": value, "unit": "s", "n_gpus": world,

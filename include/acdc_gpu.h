@@ -119,7 +119,7 @@ typedef struct acdc_settings {
   int32_t polish_active_passes;   /* with hot_polish_sweeps: before the hot sweep,
                                      this many passes (|A|/q updates each) of the
                                      q-shrinking draws in FP64, tau_active in
-                                     flight; 0 = none                              */
+                                     flight; 0 = none, default 2                  */
   int32_t reserved2;
 } acdc_settings;
 
