@@ -730,6 +730,55 @@ int evaluate_impl(acdc_problem* p, acdc_eval* out, float* ms, bool screened = fa
 bool converged(const acdc_settings& s, const acdc_eval& ev) {
   return (s.gap_relative ? ev.rel_gap : ev.gap) <= s.gap_target;
 }
+
+// Launches one update bulk of u.count updates and counts them.
+int run_counted(acdc_problem* p, const UpdateParams& u, int warps_per_block, uint64_t* done,
+                uint64_t* done_fp64) {
+  ACDC_CK(p->ctx, launch_update(u, p->k_next, warps_per_block, p->ctx->stream));
+  p->k_next += u.count;
+  p->updates_done += u.count;
+  *done += u.count;
+  if (p->fp64_mode) *done_fp64 += u.count;
+  return ACDC_OK;
+}
+
+// FP64 polish for the certificate.  The FP32 iterate moves x_j only in steps
+// of its FP32 spacing, which can leave KKT violations just above what the
+// target needs.  So: x64 = x32 exactly (r64 of the evaluation just made is
+// exact for it), polish_active_passes passes of the usual q-shrinking draws in
+// FP64, one warp of exact steps over the hot list in FP64 with nothing else in
+// flight, then a new evaluation.  Kept (*ev replaced, x left in FP64) if it
+// meets the target; otherwise x goes back to FP32 (rounded) and the bulks
+// continue.  The new evaluation's time is added to *ms.
+int polish_for_certificate(acdc_problem* p, acdc_eval* ev, bool screen, uint64_t* done,
+                           uint64_t* done_fp64, float* ms) {
+  int rc = enter_fp64(p);
+  if (rc != ACDC_OK) return rc;
+  if (p->s.polish_active_passes > 0 && ev->active > 0) {
+    const double q = std::max(1e-3, p->s.shrinking_probability);
+    const uint64_t cnt = (uint64_t)((double)p->s.polish_active_passes * (double)ev->active / q);
+    rc = run_counted(p, update_params(p, cnt, true), p->s.warps_per_block, done, done_fp64);
+    if (rc != ACDC_OK) return rc;
+  }
+  // Hot draws only, one warp, Li = 1/(beta ||a||^2) scaled back by beta.
+  UpdateParams h = update_params(p, (uint64_t)p->s.hot_polish_sweeps * (uint64_t)p->hot_count, true);
+  h.shrink_q32 = 0xffffffffu;
+  h.hot_q32 = 0xffffffffu;
+  h.li_scale_hot = p->beta;
+  h.n_warps = 1;
+  rc = run_counted(p, h, 1, done, done_fp64);
+  if (rc != ACDC_OK) return rc;
+  acdc_eval ev2;
+  float ms2 = 0;
+  rc = evaluate_impl(p, &ev2, &ms2, screen);
+  if (rc != ACDC_OK) return rc;
+  *ms += ms2;
+  if (converged(p->s, ev2)) {
+    *ev = ev2;
+    return ACDC_OK;
+  }
+  return leave_fp64(p);
+}
 }  // namespace
 
 extern "C" int acdc_evaluate(acdc_problem* p, acdc_eval* out) {
@@ -839,49 +888,8 @@ extern "C" int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_t
     }
     if (p->s.hot_polish_sweeps > 0 && shrink && !p->fp64_mode && p->hot_count > 0 &&
         !converged(p->s, ev) && ev.rel_gap < p->s.polish_rel_gap) {
-      // FP64 polish for the certificate.  The FP32 iterate moves x_j only in
-      // steps of its FP32 spacing, which can leave KKT violations just above
-      // what the target needs.  So: x64 = x32 exactly (r64 of the evaluation
-      // above is exact for it), polish_active_passes passes of the usual
-      // q-shrinking draws in FP64, one warp of exact steps over the hot list in
-      // FP64 with nothing else in flight, then a new evaluation.  Kept if it
-      // meets the target; otherwise x goes back to FP32 (rounded) and the
-      // bulks continue.
-      rc = enter_fp64(p);
+      rc = polish_for_certificate(p, &ev, screen, &done, &done_fp64, &extra_ms);
       if (rc != ACDC_OK) return rc;
-      if (p->s.polish_active_passes > 0 && ev.active > 0) {
-        const double q = std::max(1e-3, p->s.shrinking_probability);
-        const uint64_t cnt =
-            (uint64_t)((double)p->s.polish_active_passes * (double)ev.active / q);
-        UpdateParams a = update_params(p, cnt, true);
-        ACDC_CK(ctx, launch_update(a, p->k_next, p->s.warps_per_block, ctx->stream));
-        p->k_next += cnt;
-        done += cnt;
-        done_fp64 += cnt;
-        p->updates_done += cnt;
-      }
-      const uint64_t sweep = (uint64_t)p->s.hot_polish_sweeps * (uint64_t)p->hot_count;
-      UpdateParams h = update_params(p, sweep, true);
-      h.shrink_q32 = 0xffffffffu;
-      h.hot_q32 = 0xffffffffu;
-      h.li_scale_hot = p->beta;
-      h.n_warps = 1;
-      ACDC_CK(ctx, launch_update(h, p->k_next, 1, ctx->stream));
-      p->k_next += sweep;
-      done += sweep;
-      done_fp64 += sweep;
-      p->updates_done += sweep;
-      acdc_eval ev2;
-      float ms2 = 0;
-      rc = evaluate_impl(p, &ev2, &ms2, screen);
-      if (rc != ACDC_OK) return rc;
-      extra_ms += ms2;
-      if (converged(p->s, ev2)) {
-        ev = ev2;
-      } else {
-        rc = leave_fp64(p);
-        if (rc != ACDC_OK) return rc;
-      }
     }
     trace(done, ev, bulk_ms, ev_ms + extra_ms, shrink, u.fp64 != 0, screened_now && extra_ms == 0);
     p->stats.update_ms += bulk_ms;
