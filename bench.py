@@ -147,44 +147,81 @@ def probe_launches(w):
     return 0
 
 
-def batch_sample(count, seed=0xACDC0003):
+def batch_sample(count, seed=0xACDC0003, only=None):
     """Instances of the batched lambda-path workload: m log-uniform in [500, 50,000],
     n log-uniform in [1,000, 200,000], 5..50 entries per column, each with the
-    16-point path lambda_max 0.5^k, k = 1..16."""
+    16-point path lambda_max 0.5^k, k = 1..16.  `only` restricts the sample to
+    those indices (a rank's shard); instance i is the same either way."""
     import acdc
     import numpy as np
     insts = []
-    for i in range(count):
+    for i in (range(count) if only is None else only):
         m, n = acdc.mix_sizes(seed, i)
         insts.append(acdc.gen_lasso(m, n, nnz_mode=acdc.NNZ_UNIFORM, nnz_min=5, nnz_max=50,
                                     n_star=max(1, n // 100), lambda_frac=1.0, seed=seed + i))
-    lams = np.array([[x.lam * 0.5 ** k for k in range(1, 17)] for x in insts])
+    lams = np.array([[x.lam * 0.5 ** k for k in range(1, 17)] for x in insts]).reshape(-1, 16)
     return insts, lams
 
 
-def run_batched(ctx, count, max_epochs):
-    """Batched solves/s of the lambda-path sample against the plain one-instance
-    path on the same instances (both with q-shrinking, gap 1e-6 per lambda)."""
+def shard_by_footprint(footprints, world):
+    """Independent instances dealt to `world` ranks by device footprint: largest
+    first, each to the rank with the least bytes so far (ties to the lower rank).
+    Returns one sorted index list per rank.  No data moves between ranks."""
+    loads = [0] * world
+    shards = [[] for _ in range(world)]
+    for i in sorted(range(len(footprints)), key=lambda k: (-footprints[k], k)):
+        r = min(range(world), key=lambda k: (loads[k], k))
+        shards[r].append(i)
+        loads[r] += footprints[i]
+    return [sorted(x) for x in shards]
+
+
+def batch_footprints(count, seed=0xACDC0003):
+    """Expected device bytes of the batched sample's instances from their sizes
+    alone (27.5 entries per column on average), so every rank can shard the
+    sample without generating it."""
     import acdc
-    insts, lams = batch_sample(count)
+    out = []
+    for i in range(count):
+        m, n = acdc.mix_sizes(seed, i)
+        out.append(20 * 27.5 * n + 136 * n + 32 * m)
+    return out
+
+
+def run_batched(ctx, count, max_epochs, rank=0, world=1, dist=None, dev=None):
+    """Batched solves/s of the lambda-path sample against the plain one-instance
+    path on the same instances (both with q-shrinking, gap 1e-6 per lambda).
+    With several ranks each solves its shard of the instances (dealt by
+    footprint, no collective on the data path); solves/s is all ranks' solves
+    over the slowest rank's time."""
+    import acdc
+    shards = shard_by_footprint(batch_footprints(count), world) if world > 1 else [list(range(count))]
+    mine = shards[rank]
+    insts, lams = batch_sample(count, only=mine)
     out = {"workload": "lasso_paths_mix", "instances": count, "lambdas_per_instance": 16,
            "solves": count * 16, "gap_target_relative": 1e-6, "max_epochs_per_lambda": max_epochs,
            "sizes": "m logU[500,5e4], n logU[1e3,2e5], 5..50 per column (the 512-instance "
                     "workload's distribution, first %d instances)" % count,
-           "nnz": int(sum(x.nnz for x in insts))}
+           "nnz": int(round(sum_over_ranks(dist, sum(x.nnz for x in insts), dev))),
+           "shards": [len(x) for x in shards],
+           "scaling": "strong: the sample's instances dealt to the ranks by footprint"}
     for plain in (0, 1):
         probs = [acdc.Problem(ctx, x) for x in insts]
         for q in probs:
             q.synchronize()
+        if dist is not None:
+            dist.barrier()
         t = time.perf_counter()
-        res, _ = acdc.batch_solve_path(ctx, probs, lams, gap_target=1e-6, max_epochs=max_epochs,
-                                       refresh_every=2, autotune=1, plain=plain, use_shrinking=1)
-        dt = time.perf_counter() - t
+        res, _ = (acdc.batch_solve_path(ctx, probs, lams, gap_target=1e-6, max_epochs=max_epochs,
+                                        refresh_every=2, autotune=1, plain=plain, use_shrinking=1)
+                  if probs else ([], None))
+        dt = max_over_ranks(dist, time.perf_counter() - t, dev)
         for q in probs:
             q.close()
         key = "plain" if plain else "batched"
         conv = sum(r.converged for row in res for r in row)
-        out[key] = {"seconds": dt, "solves_per_s": count * 16 / dt, "converged": int(conv),
+        conv = int(round(sum_over_ranks(dist, conv, dev)))
+        out[key] = {"seconds": dt, "solves_per_s": count * 16 / dt, "converged": conv,
                     "converged_per_s": conv / dt}
     out["speedup"] = out["batched"]["solves_per_s"] / out["plain"]["solves_per_s"]
     return out
@@ -299,6 +336,15 @@ def max_over_ranks(dist, value, device=None):
     import torch
     t = torch.tensor([value], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, value, device=None):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
 
 
@@ -571,11 +617,12 @@ def run_ours(args, w):
 
     p.close()
     batched = serving = None
-    if rank == 0 and not is_svm(w):
-        if args.batch_instances > 0:
-            batched = run_batched(ctx, args.batch_instances, args.batch_max_epochs)
-        if args.serve_requests > 0:
-            serving = run_serving(ctx, args.serve_requests, args.serve_rate, args.serve_quantum)
+    if not is_svm(w) and args.batch_instances > 0:
+        # every rank takes its shard of the instances
+        batched = run_batched(ctx, args.batch_instances, args.batch_max_epochs, rank, world, dist,
+                              dev)
+    if rank == 0 and not is_svm(w) and args.serve_requests > 0:
+        serving = run_serving(ctx, args.serve_requests, args.serve_rate, args.serve_quantum)
     if is_svm(w):
         solver_keys = {"gap_target_absolute": w["gap"], "q_shrinking": 0, "lambda": w["lam"]}
     else:
