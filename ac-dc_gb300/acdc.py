@@ -162,6 +162,10 @@ def gpu_lib():
         L.acdc_recompute_residuals.argtypes = [VP]
         L.acdc_evaluate.argtypes = [VP, C.POINTER(Eval)]
         L.acdc_solve.argtypes = [VP, C.POINTER(SolveResult)]
+        L.acdc_checkpoint_size.argtypes = [VP]
+        L.acdc_checkpoint_size.restype = I64
+        L.acdc_checkpoint_save.argtypes = [VP, VP, I64]
+        L.acdc_checkpoint_load.argtypes = [VP, VP, I64]
         L.acdc_solve_traced.argtypes = [VP, C.POINTER(SolveResult), VP, I64, C.POINTER(I64)]
         L.acdc_problem_reset.argtypes = [VP]
         L.acdc_get_x.argtypes = [VP, VP]
@@ -519,6 +523,18 @@ class Problem:
 
     def reset(self):
         self.ctx.check(self.L.acdc_problem_reset(self.h))
+
+    def checkpoint(self):
+        """acdc_checkpoint_save: the solver state as bytes."""
+        size = self.L.acdc_checkpoint_size(self.h)
+        buf = C.create_string_buffer(size)
+        self.ctx.check(self.L.acdc_checkpoint_save(self.h, buf, size))
+        return buf.raw
+
+    def restore(self, data):
+        """acdc_checkpoint_load from bytes made by checkpoint()."""
+        buf = C.create_string_buffer(bytes(data), len(data))
+        self.ctx.check(self.L.acdc_checkpoint_load(self.h, buf, len(data)))
 
     def get_x(self):
         x = np.zeros(self.n)

@@ -934,6 +934,61 @@ extern "C" int acdc_set_x(acdc_problem* p, const double* x) {
   return acdc_recompute_residuals(p);
 }
 
+namespace {
+// Checkpoint layout: this header, then x as n doubles.
+struct CheckpointHeader {
+  char magic[8];            // "ACDCCKP1"
+  int32_t loss, fp64;
+  int64_t m, n;
+  uint64_t k_next, updates_done;
+  int64_t epochs_done;
+  double lambda;
+};
+constexpr char kCheckpointMagic[8] = {'A', 'C', 'D', 'C', 'C', 'K', 'P', '1'};
+}  // namespace
+
+extern "C" int64_t acdc_checkpoint_size(const acdc_problem* p) {
+  if (!p) return 0;
+  return (int64_t)sizeof(CheckpointHeader) + (int64_t)sizeof(double) * p->d.n;
+}
+
+extern "C" int acdc_checkpoint_save(acdc_problem* p, void* buf, int64_t size) {
+  if (!p || !buf || size != acdc_checkpoint_size(p)) return ACDC_EINVAL;
+  CheckpointHeader h;
+  std::memset(&h, 0, sizeof(h));
+  std::memcpy(h.magic, kCheckpointMagic, sizeof(h.magic));
+  h.loss = p->loss;
+  h.fp64 = p->fp64_mode ? 1 : 0;
+  h.m = p->d.m;
+  h.n = p->d.n;
+  h.k_next = p->k_next;
+  h.updates_done = p->updates_done;
+  h.epochs_done = p->epochs_done;
+  h.lambda = p->lambda;
+  std::memcpy(buf, &h, sizeof(h));
+  return acdc_get_x(p, reinterpret_cast<double*>(static_cast<char*>(buf) + sizeof(h)));
+}
+
+extern "C" int acdc_checkpoint_load(acdc_problem* p, const void* buf, int64_t size) {
+  if (!p || !buf || size != acdc_checkpoint_size(p)) return ACDC_EINVAL;
+  CheckpointHeader h;
+  std::memcpy(&h, buf, sizeof(h));
+  if (std::memcmp(h.magic, kCheckpointMagic, sizeof(h.magic)) != 0 || h.loss != p->loss ||
+      h.m != p->d.m || h.n != p->d.n || !(h.lambda > 0))
+    return acdc_set_error(p->ctx, ACDC_EINVAL, "checkpoint of another problem");
+  int rc = ACDC_OK;
+  if (h.lambda != p->lambda) rc = acdc_problem_set_lambda(p, h.lambda);
+  if (rc != ACDC_OK) return rc;
+  p->fp64_mode = h.fp64 != 0;
+  rc = acdc_set_x(p, reinterpret_cast<const double*>(static_cast<const char*>(buf) + sizeof(h)));
+  if (rc != ACDC_OK) return rc;
+  p->k_next = h.k_next;
+  p->updates_done = h.updates_done;
+  p->epochs_done = h.epochs_done;
+  p->hot_count = 0;
+  return ACDC_OK;
+}
+
 extern "C" int acdc_get_residuals(acdc_problem* p, double* r) {
   if (!p || !r) return ACDC_EINVAL;
   acdc_ctx* ctx = p->ctx;

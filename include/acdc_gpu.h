@@ -283,6 +283,19 @@ int acdc_problem_reset(acdc_problem* p);
 
 int acdc_get_x(acdc_problem* p, double* x);        /* n entries (alpha for loss 2) */
 int acdc_set_x(acdc_problem* p, const double* x);  /* warm start; refreshes r      */
+
+/* Checkpoint and resume of a problem's solver state: x (FP64), the sampler's
+ * update counter, the updates and epochs done, lambda and the precision stage
+ * (FP32 or FP64 x).  acdc_checkpoint_size gives the bytes (0 for a null
+ * problem); acdc_checkpoint_save writes them to host memory; acdc_checkpoint_load
+ * restores them into a problem of the same loss and sizes, recomputing the
+ * residuals from x (the active and hot sets are rebuilt at its next
+ * evaluation), so that the updates continue from the same draw.  A buffer
+ * of another size, loss or shape returns ACDC_EINVAL.  The reference only dumps
+ * x per lambda (experiments/lasso_console_solver.cpp:164-171) and has no resume. */
+int64_t acdc_checkpoint_size(const acdc_problem* p);
+int acdc_checkpoint_save(acdc_problem* p, void* buf, int64_t size);
+int acdc_checkpoint_load(acdc_problem* p, const void* buf, int64_t size);
 int acdc_get_residuals(acdc_problem* p, double* r);/* m entries: Ax-b or w, FP32 working copy */
 int acdc_get_stats(acdc_problem* p, acdc_stats* s);
 /* 0-1 accuracy of the current model on n_test held-out samples given as CSR

@@ -287,6 +287,34 @@ def test_solve_trace_records_every_evaluation(ctx):
     p.close()
 
 
+def test_checkpoint_resumes_the_same_draws(ctx):
+    """acdc_checkpoint_save / _load: a problem restored from a checkpoint into a
+    fresh one continues with the same sampler counter, so one warp reproduces the
+    original continuation (to FP32 rounding of the recomputed residual); a
+    checkpoint of another shape or size is refused."""
+    inst = acdc.gen_lasso(600, 2500, nnz_per_col=8, n_star=30, lambda_frac=0.1, seed=21)
+    kw = dict(tau=1, warps_per_block=1, seed=9)
+    p = acdc.Problem(ctx, inst, **kw)
+    p.run_updates(3 * inst.n)
+    ck = p.checkpoint()
+    p.run_updates(2 * inst.n)
+    x1 = p.get_x()
+    q = acdc.Problem(ctx, inst, **kw)
+    q.restore(ck)
+    q.run_updates(2 * inst.n)
+    np.testing.assert_allclose(q.get_x(), x1, rtol=1e-5, atol=1e-7)
+    q.reset()
+    q.run_updates(2 * inst.n)
+    assert not np.allclose(q.get_x(), x1, atol=1e-7)
+    other = acdc.Problem(ctx, acdc.gen_lasso(600, 2400, nnz_per_col=8, n_star=30, seed=22))
+    for bad, target in ((ck, other), (ck[:-8], q), (b"X" + ck[1:], q)):
+        with pytest.raises(acdc.AcdcError) as e:
+            target.restore(bad)
+        assert e.value.code == acdc.EINVAL
+    for x in (p, q, other):
+        x.close()
+
+
 def test_invalid_inputs_are_rejected(ctx):
     inst = acdc.gen_lasso(50, 80, nnz_per_col=3, n_star=5, seed=1)
     bad = acdc.Instance(inst.loss, inst.m, inst.n, inst.col_ptr, inst.row_idx.copy(), inst.vals,
