@@ -16,6 +16,7 @@ HOST_LIB = os.path.join(LIBDIR, "libacdc_host.so")
 
 OK, EINVAL, ENOMEM, EUNSUPPORTED, ECUDA, ETIMEOUT, EDEVICE, EBUSY, ENOTFOUND, ENODEV = (
     0, -1, -2, -3, -4, -5, -6, -7, -8, -9)
+ECANCELED = -10
 LOSS_L1_SQUARE, LOSS_L2_SQUARE, LOSS_SVM_DUAL, LOSS_LOGISTIC = 0, 1, 2, 3
 NNZ_FIXED, NNZ_ZIPF, NNZ_UNIFORM = 0, 1, 2
 PREC_AUTO, PREC_FP32, PREC_FP64 = 0, 1, 2
@@ -178,6 +179,7 @@ def gpu_lib():
         L.acdc_test_accuracy.argtypes = [VP, I64, VP, VP, VP, VP, C.POINTER(D)]
         L.acdc_debug_sample_noalloc.argtypes = [VP, U64, U64, U64, I64, VP]
         L.acdc_server_get_stats.argtypes = [VP, C.c_void_p]
+        L.acdc_server_cancel.argtypes = [VP, I64]
         L.acdc_batch_solve_path.argtypes = [VP, I32, VP, VP, C.POINTER(BatchOptions), VP, VP]
         L.acdc_server_create.argtypes = [VP, C.POINTER(ServerOptions), C.POINTER(VP)]
         L.acdc_server_submit.argtypes = [VP, C.POINTER(Request), C.POINTER(I64)]
@@ -632,6 +634,9 @@ class Server:
 
     def release(self, ticket):
         self.ctx.check(self.L.acdc_server_release(self.h, ticket))
+
+    def cancel(self, ticket):
+        self.ctx.check(self.L.acdc_server_cancel(self.h, ticket))
 
     def close(self):
         if self.h:

@@ -37,6 +37,7 @@ extern "C" const char* acdc_status_string(int status) {
     case ACDC_EBUSY: return "admission refused";
     case ACDC_ENOTFOUND: return "unknown ticket";
     case ACDC_ENODEV: return "no CUDA device";
+    case ACDC_ECANCELED: return "request cancelled";
     default: return "unknown status";
   }
 }

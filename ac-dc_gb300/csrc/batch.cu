@@ -688,6 +688,37 @@ extern "C" int acdc_server_release(acdc_server* s, int64_t ticket) {
   return ACDC_OK;
 }
 
+extern "C" int acdc_server_cancel(acdc_server* s, int64_t ticket) {
+  if (!s) return ACDC_EINVAL;
+  auto it = s->all.find(ticket);
+  if (it == s->all.end()) return ACDC_ENOTFOUND;
+  Request* r = it->second.get();
+  if (r->res.state >= 2) return ACDC_OK;
+  if (r->res.state == 0) {
+    for (auto q = s->queue.begin(); q != s->queue.end(); ++q)
+      if (*q == r) {
+        s->queue.erase(q);
+        break;
+      }
+  } else {
+    // Running: no round is in flight between steps.  The engine's tables still
+    // point at the problem, so they are rebuilt before the next round.
+    for (auto q = s->resident.begin(); q != s->resident.end(); ++q)
+      if (*q == r) {
+        s->resident.erase(q);
+        break;
+      }
+    if (r->prob) acdc_problem_destroy(r->prob);
+    r->prob = nullptr;
+    s->used_bytes -= r->footprint;
+    s->dirty = true;
+  }
+  r->res.state = 3;
+  r->res.status = ACDC_ECANCELED;
+  r->res.finish_time = now_seconds();
+  return ACDC_OK;
+}
+
 extern "C" int acdc_server_destroy(acdc_server* s) {
   if (!s) return ACDC_EINVAL;
   for (Request* r : s->resident)

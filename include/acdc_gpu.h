@@ -49,6 +49,7 @@ extern "C" {
 #define ACDC_EBUSY (-7)       /* server admission refused (budget or slots)         */
 #define ACDC_ENOTFOUND (-8)   /* unknown ticket                                     */
 #define ACDC_ENODEV (-9)      /* no CUDA device                                     */
+#define ACDC_ECANCELED (-10)  /* a served request cancelled before it finished      */
 
 /* ---- loss codes (OptimizationSettings::lossFunction,
  *      cpp/src/solver/MulticoreEngineExecutor.h:32-58) ------------------- */
@@ -414,6 +415,11 @@ int acdc_server_step(acdc_server* s, int32_t* pending);
  * released by acdc_server_release. */
 int acdc_server_poll(acdc_server* s, int64_t ticket, acdc_request_result* res, double* x);
 int acdc_server_release(acdc_server* s, int64_t ticket);
+/* Cancels a queued or running request: it leaves the queue or the device (its
+ * memory is released and the slot tables are rebuilt at the next step) and
+ * ends in state 3 with status ACDC_ECANCELED.  A finished request is left as
+ * it is.  Call between steps, like every server call. */
+int acdc_server_cancel(acdc_server* s, int64_t ticket);
 int acdc_server_destroy(acdc_server* s);
 
 /* Where the server's host time went since its creation (seconds on the host

@@ -71,6 +71,35 @@ def test_each_result_is_the_same_alone_and_in_the_mix(ctx):
     server.close()
 
 
+def test_cancel_leaves_the_others_as_they_would_be(ctx):
+    """A running and a queued request cancelled between steps end failed with
+    ACDC_ECANCELED and give their memory back; the rest finish as they would
+    alone; cancelling a finished request changes nothing."""
+    insts = requests(300, 6)
+    server = acdc.Server(ctx, memory_budget_bytes=8 << 30, max_slots=3, quantum_rounds=2)
+    tickets = [server.submit(inst) for inst in insts]  # three run, three wait
+    server.step()
+    states = [server.poll(t)[0].state for t in tickets]
+    assert states[1] == 1 and states[4] == 0  # running (tables built), still queued
+    server.cancel(tickets[1])  # running
+    server.cancel(tickets[4])  # queued
+    results = drain(server, tickets)
+    for i, (inst, (res, x)) in enumerate(zip(insts, results)):
+        if i in (1, 4):
+            assert res.state == 3 and res.status == acdc.ECANCELED
+            continue
+        assert acdc.Server.STATES[res.state] == "done", res.status
+        r_alone, x_alone = alone(ctx, inst)
+        check_same(res, x, r_alone, x_alone, inst)
+    server.cancel(tickets[0])  # finished: no change
+    assert server.poll(tickets[0])[0].state == 2
+    st = server.stats()
+    assert st["admitted"] == 5 and st["retired"] == 4
+    for t in tickets:
+        server.release(t)
+    server.close()
+
+
 def test_memory_budget_queues_and_refuses(ctx):
     insts = requests(200, 4)
     lasso = [inst for inst in insts if inst.loss == acdc.LOSS_L1_SQUARE]
