@@ -94,6 +94,9 @@ int prepare(acdc_problem* p, const SolveOpts& o, int wpb_cap) {
   return acdc_problem_set_settings(p, &s);
 }
 
+// Rounds of a captured batch launched between two host synchronisations.
+constexpr int kRoundsPerSync = 4;
+
 // Device tables and per-slot state of one set of problems solved together.
 class BatchEngine {
  public:
@@ -255,8 +258,11 @@ class BatchEngine {
     ce = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
     if (ce != cudaSuccess) return acdc_cuda_error(ctx_, ce, "cudaGraphInstantiate");
-    for (int64_t r = 0; r < max_rounds && *h_live_ > 0; ++r) {
-      ce = cudaGraphLaunch(exec, st);
+    // A few rounds per host synchronisation: a round whose slots have all
+    // finished does no work, and the host reads the live count only to stop.
+    for (int64_t r = 0; r < max_rounds && *h_live_ > 0;) {
+      for (int k = 0; k < kRoundsPerSync && r < max_rounds && ce == cudaSuccess; ++k, ++r)
+        ce = cudaGraphLaunch(exec, st);
       if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
       if (ce != cudaSuccess) break;
     }
@@ -267,11 +273,13 @@ class BatchEngine {
 
   // Runs rounds without a graph (the slot set changes between calls).
   int run_rounds(int rounds, int64_t* count = nullptr) {
-    for (int r = 0; r < rounds && *h_live_ > 0; ++r) {
+    if (*h_live_ <= 0) return ACDC_OK;
+    // All of the step's rounds back to back, one synchronisation at the end.
+    for (int r = 0; r < rounds; ++r) {
       ACDC_CK(ctx_, enqueue_round());
-      ACDC_CK(ctx_, cudaStreamSynchronize(ctx_->stream));
       if (count) ++*count;
     }
+    ACDC_CK(ctx_, cudaStreamSynchronize(ctx_->stream));
     return ACDC_OK;
   }
 
