@@ -614,6 +614,12 @@ def run_ours(args, w):
                           "in %.2f s on %d threads; scaled to %.0f epochs, the epochs the GPU "
                           "solve needed (the reference samples uniformly: a lower bound)"
                           % (upd, secs, threads, ep))}
+        # the serial path (one thread, the reference's -t 1) on a smaller sample
+        upd1 = max(1, min(upd, 2_000_000))
+        per_epoch1, secs1 = cpu_time_per_epoch(inst, 1, upd1)
+        cpu["serial"] = {"value": per_epoch1 * ep, "unit": "s", "cores": 1,
+                         "sample": "%d updates on 1 thread in %.2f s, scaled the same way"
+                                   % (upd1, secs1)}
 
     p.close()
     batched = serving = None
@@ -644,6 +650,7 @@ def run_ours(args, w):
                        "tau": w["tau"], "refresh_every": w["refresh_every"],
                        "precision": "fp32 bulk; fp64 refresh, gap and hot-column polish",
                        "updates": int(updates), "update_launches": int(launches),
+                       "updates_per_s": updates / (upd_ms * 1e-3) if upd_ms > 0 else None,
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (no flush)", "omega": info.omega,
                        "beta": info.sigma, "epochs": epochs,
