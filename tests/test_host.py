@@ -28,6 +28,42 @@ def test_library_exports_every_declared_symbol(header, lib):
     assert not missing, missing
 
 
+STRUCTS = [("acdc_settings", "Settings"), ("acdc_eval", "Eval"), ("acdc_stats", "Stats"),
+           ("acdc_solve_result", "SolveResult"), ("acdc_trace_row", "TraceRow"),
+           ("acdc_problem_info", "ProblemInfo"), ("acdc_batch_options", "BatchOptions"),
+           ("acdc_batch_result", "BatchResult"), ("acdc_server_options", "ServerOptions"),
+           ("acdc_server_stats", "ServerStats"), ("acdc_request", "Request"),
+           ("acdc_request_result", "RequestResult"), ("acdc_lasso_gen", "LassoGen"),
+           ("acdc_svm_gen", "SvmGen")]
+
+
+def test_ctypes_structs_match_the_c_headers(tmp_path):
+    """Every struct of the C-ABI has the same size and field offsets in the
+    ctypes binding as the C compiler gives it from include/*.h."""
+    import subprocess
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "acdc_gpu.h"',
+             '#include "acdc_host.h"', 'int main(void) {']
+    for c_name, py_name in STRUCTS:
+        lines.append('  printf("%s size %%zu\\n", sizeof(%s));' % (c_name, c_name))
+        for field, _ in getattr(acdc, py_name)._fields_:
+            c_field = {"lambda_": "lambda"}.get(field, field)
+            lines.append('  printf("%s.%s %%zu\\n", offsetof(%s, %s));'
+                         % (c_name, field, c_name, c_field))
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = dict(line.rsplit(" ", 1) for line in out if line)
+    for c_name, py_name in STRUCTS:
+        cls = getattr(acdc, py_name)
+        assert int(got["%s size" % c_name]) == C.sizeof(cls), c_name
+        for field, _ in cls._fields_:
+            assert int(got["%s.%s" % (c_name, field)]) == getattr(cls, field).offset, (c_name, field)
+
+
 def test_gpu_library_loads_and_reports_no_device_cleanly():
     L = acdc.gpu_lib()
     s = acdc.default_settings()
