@@ -222,6 +222,7 @@ def host_lib():
                                              C.POINTER(I64)]
         H.acdc_load_libsvm.argtypes = [C.c_char_p, VP, VP, VP, VP]
         H.acdc_host_threads.argtypes = [I32]
+        H.acdc_save_csc_binary.argtypes = [C.c_char_p, C.c_char_p, C.c_int32, I64, VP, VP, VP]
         _host = H
     return _host
 
@@ -367,6 +368,18 @@ def load_csc_binary(prefix, suffix, rank, vector_file, local_n, lam, loss=LOSS_L
     _check_host(H.acdc_load_csc_binary(*args, _ptr(col_ptr), _ptr(row_idx), _ptr(vals), _ptr(b)),
                 "load_csc_binary")
     return Instance(loss, m.value, n.value, col_ptr, row_idx, vals, b, lam)
+
+
+def save_csc_binary(inst, prefix, suffix="", rank=0):
+    """acdc_save_csc_binary: the instance's matrix in the per-rank binary format
+    that load_csc_binary reads (the vector file is written separately)."""
+    cp = np.ascontiguousarray(inst.col_ptr, np.int64)
+    ri = np.ascontiguousarray(inst.row_idx, np.int32)
+    va = np.ascontiguousarray(inst.vals, np.float64)
+    _check_host(host_lib().acdc_save_csc_binary(prefix.encode(), suffix.encode(), int(rank),
+                                                inst.n, _ptr(cp), _ptr(ri) if ri.size else None,
+                                                _ptr(va) if va.size else None),
+                "save_csc_binary")
 
 
 def host_threads(threads):

@@ -359,6 +359,31 @@ extern "C" int acdc_host_threads(int32_t threads) {
   return g_threads.exchange(threads > 0 ? threads : 0);
 }
 
+extern "C" int acdc_save_csc_binary(const char* prefix, const char* suffix, int32_t rank,
+                                    int64_t n, const int64_t* col_ptr, const int32_t* row_idx,
+                                    const double* vals) {
+  if (!prefix || n < 0 || !col_ptr || col_ptr[0] != 0) return ACDC_EINVAL;
+  for (int64_t j = 0; j < n; ++j)
+    if (col_ptr[j + 1] < col_ptr[j]) return ACDC_EINVAL;
+  const int64_t nnz = col_ptr[n];
+  if (nnz > 0 && (!row_idx || !vals)) return ACDC_EINVAL;
+  const std::string pre(prefix), suf(suffix ? suffix : ""), rk = std::to_string(rank);
+  FILE* f = std::fopen((pre + "_colptr_" + rk + suf).c_str(), "wb");
+  if (!f) return ACDC_EINVAL;
+  bool ok = true;
+  for (int64_t j = 0; j <= n && ok; ++j) ok = std::fprintf(f, "%lld\n", (long long)col_ptr[j]) > 0;
+  ok = (std::fclose(f) == 0) && ok;
+  auto raw = [&](const std::string& path, const void* src, size_t bytes) {
+    FILE* g = std::fopen(path.c_str(), "wb");
+    if (!g) return false;
+    const bool w = bytes == 0 || std::fwrite(src, 1, bytes, g) == bytes;
+    return (std::fclose(g) == 0) && w;
+  };
+  ok = ok && raw(pre + "_rowid_" + rk + suf, row_idx, sizeof(int32_t) * (size_t)nnz);
+  ok = ok && raw(pre + "_values_" + rk + suf, vals, sizeof(double) * (size_t)nnz);
+  return ok ? ACDC_OK : ACDC_EINVAL;
+}
+
 extern "C" int acdc_load_libsvm_sizes(const char* path, int64_t* n_samples, int64_t* d,
                                       int64_t* nnz) {
   if (!path || !n_samples || !d || !nnz) return ACDC_EINVAL;

@@ -129,6 +129,13 @@ int acdc_load_csc_binary(const char* prefix, const char* suffix, int32_t rank,
                          const char* vector_file, int64_t local_n, int64_t* col_ptr,
                          int32_t* row_idx, double* vals, double* b);
 
+/* Writes a CSC matrix (n columns) in that per-rank format, the three files
+ * <prefix>_colptr_<rank><suffix> (text), _rowid_ (raw int32) and _values_
+ * (raw doubles), so that text or generated inputs can be converted once and
+ * then loaded without parsing.  The vector file stays text. */
+int acdc_save_csc_binary(const char* prefix, const char* suffix, int32_t rank, int64_t n,
+                         const int64_t* col_ptr, const int32_t* row_idx, const double* vals);
+
 /* Host threads of the text loaders (acdc_load_csc_text*, the offsets file of
  * acdc_load_csc_binary*, acdc_load_libsvm*): > 0 cuts every text into that
  * many pieces, each parsed on its own thread; 0 (the default) uses one piece

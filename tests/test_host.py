@@ -201,6 +201,23 @@ def test_csc_binary_loader_roundtrip(tmp_path):
     assert np.array_equal(part.vals, inst.vals[:inst.col_ptr[10]])
 
 
+def test_csc_binary_writer_roundtrip(tmp_path):
+    """acdc_save_csc_binary writes what acdc_load_csc_binary reads: a text
+    instance converted once loads back bit for bit."""
+    inst = acdc.gen_lasso(70, 120, nnz_per_col=5, n_star=6, seed=4)
+    pre, b_path = str(tmp_path / "A"), str(tmp_path / "b.txt")
+    acdc.save_csc_binary(inst, pre, ".bin", 2)
+    np.savetxt(b_path, inst.rhs, fmt="%.17g")
+    got = acdc.load_csc_binary(pre, ".bin", 2, b_path, inst.n, 0.5)
+    assert np.array_equal(got.col_ptr, inst.col_ptr) and np.array_equal(got.row_idx, inst.row_idx)
+    assert np.array_equal(got.vals, inst.vals) and np.array_equal(got.rhs, inst.rhs)
+    bad = acdc.Instance(inst.loss, inst.m, inst.n, inst.col_ptr.copy(), inst.row_idx, inst.vals,
+                        inst.rhs, inst.lam)
+    bad.col_ptr[3] = bad.col_ptr[4] + 1  # decreasing
+    with pytest.raises(acdc.AcdcError):
+        acdc.save_csc_binary(bad, pre, ".bin", 3)
+
+
 def test_csc_binary_loader_rejects_bad_input(tmp_path):
     inst = acdc.gen_lasso(30, 40, nnz_per_col=3, n_star=4, seed=3)
     pre, b_path = str(tmp_path / "A"), str(tmp_path / "b.txt")
