@@ -17,6 +17,9 @@
 //    per line, "label index:value ...", 1-based indices made 0-based, label 0
 //    mapped to -1.
 //
+// Every reader refuses a value that is not finite (nan, inf, or out of double
+// range), in the matrix as in the vector, with ACDC_EINVAL.
+//
 // The text formats are parsed by several host threads: the file is cut into
 // pieces just after a separator (whitespace for number lists, a newline for
 // LIBSVM), each piece is scanned on its own thread, and the pieces' counts are
@@ -25,6 +28,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cerrno>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -101,7 +105,7 @@ bool parse_range(const char* p, const char* end, std::vector<T>& out) {
     char* q = nullptr;
     errno = 0;
     double v = std::strtod(p, &q);
-    if (q == p || q > end || errno == ERANGE) return false;
+    if (q == p || q > end || errno == ERANGE || !std::isfinite(v)) return false;
     out.push_back((T)v);
     p = q;
   }
@@ -219,7 +223,7 @@ int walk_libsvm(const char* p, const char* end, LibsvmScan& sc, int64_t n0, int6
     if (q < eol && *q != '#') {
       char* r = nullptr;
       double label = std::strtod(q, &r);
-      if (r == q || r > eol) return ACDC_EINVAL;
+      if (r == q || r > eol || !std::isfinite(label)) return ACDC_EINVAL;
       q = r;
       if (row_ptr) {
         row_ptr[n0 + n] = nnz0 + nnz;
@@ -234,7 +238,7 @@ int walk_libsvm(const char* p, const char* end, LibsvmScan& sc, int64_t n0, int6
         // the value follows the colon directly (strtod would skip a line end)
         if (q >= eol || *q == ' ' || *q == '\t' || *q == '\r') return ACDC_EINVAL;
         double v = std::strtod(q, &r);
-        if (r == q || r > eol) return ACDC_EINVAL;
+        if (r == q || r > eol || !std::isfinite(v)) return ACDC_EINVAL;
         q = r;
         if (idx > d) d = idx;
         if (idx - 1 > INT32_MAX) return ACDC_EINVAL;
@@ -309,7 +313,7 @@ extern "C" int acdc_load_csc_binary(const char* prefix, const char* suffix, int3
     return ACDC_EINVAL;
   const int64_t m = (int64_t)t.b.size();
   for (int64_t e = 0; e < nnz; ++e)
-    if (row_idx[e] < 0 || row_idx[e] >= m) return ACDC_EINVAL;
+    if (row_idx[e] < 0 || row_idx[e] >= m || !std::isfinite(vals[e])) return ACDC_EINVAL;
   std::memcpy(col_ptr, t.col_ptr.data(), sizeof(int64_t) * t.col_ptr.size());
   std::memcpy(b, t.b.data(), sizeof(double) * t.b.size());
   return ACDC_OK;

@@ -311,6 +311,38 @@ def test_loaders_do_not_depend_on_threads(tmp_path, threads):
         acdc.host_threads(old)
 
 
+def test_loaders_refuse_non_finite_values(tmp_path):
+    inst = acdc.gen_lasso(30, 40, nnz_per_col=3, n_star=4, seed=5)
+    pre, b_path = str(tmp_path / "A"), str(tmp_path / "b.txt")
+    np.savetxt(pre + "_colPtr.txt", inst.col_ptr, fmt="%d")
+    np.savetxt(pre + "_rowIdx.txt", inst.row_idx, fmt="%d")
+    for bad in ("nan", "inf", "-inf", "1e999"):
+        v = [("%.17g" % x) for x in inst.vals]
+        v[7] = bad
+        open(pre + "_values.txt", "w").write(" ".join(v) + "\n")
+        np.savetxt(b_path, inst.rhs, fmt="%.17g")
+        with pytest.raises(acdc.AcdcError):
+            acdc.load_csc_text(pre, b_path, 0.5)
+    np.savetxt(pre + "_values.txt", inst.vals, fmt="%.17g")
+    open(b_path, "w").write(" ".join(["1"] * (inst.m - 1) + ["nan"]) + "\n")
+    with pytest.raises(acdc.AcdcError):
+        acdc.load_csc_text(pre, b_path, 0.5)
+    # binary values
+    np.savetxt(b_path, inst.rhs, fmt="%.17g")
+    vals = inst.vals.copy()
+    vals[3] = np.nan
+    acdc.save_csc_binary(acdc.Instance(inst.loss, inst.m, inst.n, inst.col_ptr, inst.row_idx,
+                                       vals, inst.rhs, inst.lam), pre, "", 0)
+    with pytest.raises(acdc.AcdcError):
+        acdc.load_csc_binary(pre, "", 0, b_path, inst.n, 0.5)
+    # LIBSVM value and label
+    p = tmp_path / "d.svm"
+    for text in ("+1 1:nan\n", "inf 1:0.5\n", "+1 2:1e400\n"):
+        p.write_text(text)
+        with pytest.raises(acdc.AcdcError):
+            acdc.load_libsvm(str(p), 0.1)
+
+
 def test_libsvm_value_must_follow_the_colon(tmp_path):
     p = tmp_path / "d.svm"
     p.write_text("+1 1:0.5 3:\n-1 2:2\n")  # a value may not come from the next line
