@@ -69,6 +69,8 @@ def test_gpu_library_loads_and_reports_no_device_cleanly():
     s = acdc.default_settings()
     assert s.tau == 4096 and s.refresh_every == 5 and s.gap_relative == 1
     assert L.acdc_status_string(acdc.EUNSUPPORTED) == b"unsupported loss"
+    assert L.acdc_status_string(acdc.ECANCELED) == b"request cancelled"
+    assert L.acdc_checkpoint_size(None) == 0
     h = acdc.VP()
     rc = L.acdc_ctx_create(0, C.byref(h))
     import torch
