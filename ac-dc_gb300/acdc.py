@@ -149,6 +149,7 @@ def gpu_lib():
         L.acdc_status_string.argtypes = [C.c_int]
         L.acdc_settings_default.argtypes = [C.POINTER(Settings)]
         L.acdc_settings_default.restype = None
+        L.acdc_settings_check.argtypes = [C.POINTER(Settings)]
         L.acdc_ctx_create.argtypes = [C.c_int, C.POINTER(VP)]
         L.acdc_ctx_destroy.argtypes = [VP]
         L.acdc_problem_create.argtypes = [VP, I32, I64, I64, VP, VP, VP, VP, D, C.POINTER(VP)]
@@ -467,6 +468,11 @@ def default_settings(loss=LOSS_L1_SQUARE, **kw):
     for k, v in kw.items():
         setattr(s, k, v)
     return s
+
+
+def settings_ok(s):
+    """acdc_settings_check: True when every field of s lies in its range."""
+    return gpu_lib().acdc_settings_check(C.byref(s)) == OK
 
 
 class Problem:

@@ -260,6 +260,10 @@ constexpr int kHostSlotDoubles = 16 + CNT_SLOTS;
 cudaError_t acdc_host_slot_take(acdc_ctx* ctx, double** slot);
 void acdc_host_slot_give(acdc_ctx* ctx, double* slot);
 int acdc_set_error(acdc_ctx* ctx, int code, const std::string& msg);
+// lambda and the like: false for zero, negatives, infinities and NaN.
+inline bool positive_finite(double v) { return v > 0 && v <= 1.7976931348623157e308; }
+// Name of the first field of s outside its range, or nullptr when every one is valid.
+const char* settings_fault(const acdc_settings* s);
 int acdc_cuda_error(acdc_ctx* ctx, cudaError_t e, const char* what);
 
 #define ACDC_CK(ctx, call)                                             \

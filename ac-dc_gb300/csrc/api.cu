@@ -66,6 +66,33 @@ extern "C" void acdc_settings_default(acdc_settings* s) {
   s->polish_active_passes = 2;
 }
 
+const char* settings_fault(const acdc_settings* s) {
+  if (s->loss < ACDC_LOSS_L1_SQUARE || s->loss > ACDC_LOSS_LOGISTIC) return "loss";
+  if (s->tau < 1) return "tau";
+  if (s->tau_active < 0) return "tau_active";
+  if (s->warps_per_block < 1 || s->warps_per_block > 8) return "warps_per_block";
+  if (s->refresh_every < 1) return "refresh_every";
+  if (s->max_epochs < 0) return "max_epochs";
+  // sigma <= 0 asks for the computed beta; NaN and infinities are no beta.
+  if (!(std::fabs(s->sigma) <= 1.7976931348623157e308)) return "sigma";
+  if (!(s->gap_target >= 0)) return "gap_target";
+  if (!(s->shrinking_probability >= 0 && s->shrinking_probability <= 1))
+    return "shrinking_probability";
+  if (!(s->shrink_eps >= 0 && s->shrink_eps < 1)) return "shrink_eps";
+  if (s->precision < ACDC_PREC_AUTO || s->precision > ACDC_PREC_FP64) return "precision";
+  if (!(s->polish_rel_gap >= 0)) return "polish_rel_gap";
+  if (!(s->hot_threshold >= 0)) return "hot_threshold";
+  if (s->polish_stall_epochs < 0) return "polish_stall_epochs";
+  if (s->hot_polish_sweeps < 0) return "hot_polish_sweeps";
+  if (s->polish_active_passes < 0) return "polish_active_passes";
+  return nullptr;
+}
+
+extern "C" int acdc_settings_check(const acdc_settings* s) {
+  if (!s) return ACDC_EINVAL;
+  return settings_fault(s) ? ACDC_EINVAL : ACDC_OK;
+}
+
 // ---- context ----
 
 extern "C" int acdc_ctx_create(int device, acdc_ctx** out) {
@@ -95,9 +122,12 @@ extern "C" int acdc_ctx_create(int device, acdc_ctx** out) {
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
   if (e == cudaSuccess) e = update_kernels_init();
   if (e != cudaSuccess) {
+    for (int i = 0; i < 6; ++i)
+      if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     delete ctx;
-    return ACDC_ECUDA;
+    return e == cudaErrorMemoryAllocation ? ACDC_ENOMEM : ACDC_ECUDA;
   }
   *out = ctx;
   return ACDC_OK;
@@ -298,14 +328,8 @@ bool shrink_now(const acdc_problem* p) {
 int apply_settings(acdc_problem* p, const acdc_settings* s) {
   acdc_ctx* ctx = p->ctx;
   if (s->loss != p->loss) return acdc_set_error(ctx, ACDC_EINVAL, "settings.loss differs from the problem's loss");
-  if (s->tau < 1 || s->tau_active < 0 || s->warps_per_block < 1 || s->warps_per_block > 8 ||
-      s->refresh_every < 1 ||
-      s->max_epochs < 0 || !(s->gap_target >= 0) || s->shrinking_probability < 0 ||
-      s->shrinking_probability > 1 || s->shrink_eps < 0 || s->shrink_eps >= 1 ||
-      s->precision < ACDC_PREC_AUTO || s->precision > ACDC_PREC_FP64 || !(s->polish_rel_gap >= 0) ||
-      !(s->hot_threshold >= 0) || s->polish_stall_epochs < 0 || s->hot_polish_sweeps < 0 ||
-      s->polish_active_passes < 0)
-    return acdc_set_error(ctx, ACDC_EINVAL, "invalid settings value");
+  if (const char* bad = settings_fault(s))
+    return acdc_set_error(ctx, ACDC_EINVAL, std::string("invalid settings value: ") + bad);
   p->s = *s;
   // q-shrinking and its screened evaluations cover losses 0 and 2 only.
   if (p->loss == ACDC_LOSS_L2_SQUARE || p->loss == ACDC_LOSS_LOGISTIC) p->s.use_shrinking = 0;
@@ -335,7 +359,7 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
   *out = nullptr;
   if (loss < ACDC_LOSS_L1_SQUARE || loss > ACDC_LOSS_LOGISTIC)
     return acdc_set_error(ctx, ACDC_EINVAL, "unknown loss code");
-  if (m <= 0 || n <= 0 || m > INT32_MAX || n > INT32_MAX || !(lambda > 0) || !rhs ||
+  if (m <= 0 || n <= 0 || m > INT32_MAX || n > INT32_MAX || !positive_finite(lambda) || !rhs ||
       (!by_rows && !col_ptr64 && !col_ptr32) || (by_rows && !by_rows->row_ptr))
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid sizes, lambda or null pointer");
   int64_t nnz = 0;
@@ -632,7 +656,8 @@ int leave_fp64(acdc_problem* p) {
 
 extern "C" int acdc_problem_set_lambda(acdc_problem* p, double lambda) {
   if (!p) return ACDC_EINVAL;
-  if (!(lambda > 0)) return acdc_set_error(p->ctx, ACDC_EINVAL, "lambda must be positive");
+  if (!positive_finite(lambda))
+    return acdc_set_error(p->ctx, ACDC_EINVAL, "lambda must be positive and finite");
   p->lambda = lambda;
   p->active_valid = false;
   p->screen_valid = false;
@@ -975,7 +1000,7 @@ extern "C" int acdc_checkpoint_load(acdc_problem* p, const void* buf, int64_t si
   CheckpointHeader h;
   std::memcpy(&h, buf, sizeof(h));
   if (std::memcmp(h.magic, kCheckpointMagic, sizeof(h.magic)) != 0 || h.loss != p->loss ||
-      h.m != p->d.m || h.n != p->d.n || !(h.lambda > 0))
+      h.m != p->d.m || h.n != p->d.n || !positive_finite(h.lambda))
     return acdc_set_error(p->ctx, ACDC_EINVAL, "checkpoint of another problem");
   int rc = ACDC_OK;
   if (h.lambda != p->lambda) rc = acdc_problem_set_lambda(p, h.lambda);

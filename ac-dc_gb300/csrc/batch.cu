@@ -440,7 +440,8 @@ extern "C" int acdc_batch_solve_path(acdc_ctx* ctx, int32_t count, acdc_problem*
       return acdc_set_error(ctx, ACDC_EUNSUPPORTED, "batched paths cover losses 0 and 2");
   }
   for (int64_t i = 0; i < (int64_t)count * opt->path_len; ++i)
-    if (!(lambdas[i] > 0)) return acdc_set_error(ctx, ACDC_EINVAL, "lambdas must be positive");
+    if (!positive_finite(lambdas[i]))
+      return acdc_set_error(ctx, ACDC_EINVAL, "lambdas must be positive and finite");
   if (count == 0) return ACDC_OK;
   ACDC_CK(ctx, cudaSetDevice(ctx->device));
   if (opt->plain) return plain_path(ctx, count, problems, lambdas, opt, results, x_out);
@@ -509,7 +510,8 @@ extern "C" int acdc_server_submit(acdc_server* s, const acdc_request* req, int64
   if (!s || !req || !ticket) return ACDC_EINVAL;
   acdc_ctx* ctx = s->ctx;
   if ((req->loss != ACDC_LOSS_L1_SQUARE && req->loss != ACDC_LOSS_SVM_DUAL) || req->m <= 0 ||
-      req->n <= 0 || !req->col_ptr || !req->rhs || !(req->lambda > 0) || !(req->gap_target >= 0))
+      req->n <= 0 || !req->col_ptr || !req->rhs || !positive_finite(req->lambda) ||
+      !(req->gap_target >= 0))
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid request");
   const int64_t nnz = req->col_ptr[req->n];
   if (req->col_ptr[0] != 0 || nnz < 0 || (nnz > 0 && (!req->row_idx || !req->vals)))

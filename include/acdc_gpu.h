@@ -196,6 +196,11 @@ typedef struct acdc_problem_info {
 
 /* ---- context ---------------------------------------------------------- */
 void acdc_settings_default(acdc_settings* s);
+/* ACDC_OK when every field of s lies in its range, else ACDC_EINVAL: the check
+ * acdc_problem_set_settings makes (which also names the field in
+ * acdc_last_error).  Needs no device, so a caller can refuse bad settings
+ * before uploading a matrix. */
+int acdc_settings_check(const acdc_settings* s);
 int acdc_ctx_create(int device, acdc_ctx** out);
 int acdc_ctx_destroy(acdc_ctx* ctx);
 const char* acdc_last_error(const acdc_ctx* ctx);
