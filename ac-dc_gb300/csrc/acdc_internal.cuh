@@ -27,6 +27,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/acdc_gpu.h"
 #include "acdc_philox.h"
 
@@ -265,6 +267,16 @@ inline bool positive_finite(double v) { return v > 0 && v <= 1.7976931348623157e
 // Name of the first field of s outside its range, or nullptr when every one is valid.
 const char* settings_fault(const acdc_settings* s);
 int acdc_cuda_error(acdc_ctx* ctx, cudaError_t e, const char* what);
+
+// A named range on a profiler's timeline for the scope it lives in (NVTX 3,
+// header-only: a no-op unless a tool is attached).  ncu can select the kernels
+// of one range, e.g. --nvtx --nvtx-include "acdc_evaluate/".
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 #define ACDC_CK(ctx, call)                                             \
   do {                                                                 \

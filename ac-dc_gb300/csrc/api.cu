@@ -357,6 +357,7 @@ int create_impl(acdc_ctx* ctx, int32_t loss, int64_t m, int64_t n, const int64_t
                 const RowsInput* by_rows = nullptr) {
   if (!ctx || !out) return ACDC_EINVAL;
   *out = nullptr;
+  NvtxRange range("acdc_problem_create");
   if (loss < ACDC_LOSS_L1_SQUARE || loss > ACDC_LOSS_LOGISTIC)
     return acdc_set_error(ctx, ACDC_EINVAL, "unknown loss code");
   if (m <= 0 || n <= 0 || m > INT32_MAX || n > INT32_MAX || !positive_finite(lambda) || !rhs ||
@@ -695,6 +696,7 @@ namespace {
 int evaluate_impl(acdc_problem* p, acdc_eval* out, float* ms, bool screened = false) {
   acdc_ctx* ctx = p->ctx;
   screened = screened && p->screen_valid;
+  NvtxRange range(screened ? "acdc_evaluate_screened" : "acdc_evaluate");
   const bool build_active = p->s.use_shrinking != 0 && !screened;
   EvalParams e = eval_params(p, p->s.use_shrinking != 0);
   e.screened = screened ? 1 : 0;
@@ -778,6 +780,7 @@ int run_counted(acdc_problem* p, const UpdateParams& u, int warps_per_block, uin
 // continue.  The new evaluation's time is added to *ms.
 int polish_for_certificate(acdc_problem* p, acdc_eval* ev, bool screen, uint64_t* done,
                            uint64_t* done_fp64, float* ms) {
+  NvtxRange range("acdc_polish");
   int rc = enter_fp64(p);
   if (rc != ACDC_OK) return rc;
   if (p->s.polish_active_passes > 0 && ev->active > 0) {
@@ -845,6 +848,7 @@ extern "C" int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_t
     if (n_rows) *n_rows = n_trace;
   };
   if (n_rows) *n_rows = 0;
+  NvtxRange range("acdc_solve");
   auto t0 = std::chrono::steady_clock::now();
   ACDC_CK(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
   int rc = ACDC_OK;
@@ -886,9 +890,12 @@ extern "C" int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_t
     count = std::min(count, budget - done);
     const bool screen = shrink && p->s.screened_eval != 0 && p->screen_valid;
     UpdateParams u = update_params(p, count, shrink);
-    ACDC_CK(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
-    ACDC_CK(ctx, launch_update(u, p->k_next, p->s.warps_per_block, ctx->stream));
-    ACDC_CK(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+    {
+      NvtxRange bulk(shrink ? "acdc_bulk_active" : "acdc_bulk");
+      ACDC_CK(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+      ACDC_CK(ctx, launch_update(u, p->k_next, p->s.warps_per_block, ctx->stream));
+      ACDC_CK(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+    }
     p->k_next += count;
     p->stats.update_launches++;
     done += count;

@@ -444,6 +444,7 @@ extern "C" int acdc_batch_solve_path(acdc_ctx* ctx, int32_t count, acdc_problem*
       return acdc_set_error(ctx, ACDC_EINVAL, "lambdas must be positive and finite");
   if (count == 0) return ACDC_OK;
   ACDC_CK(ctx, cudaSetDevice(ctx->device));
+  NvtxRange range(opt->plain ? "acdc_batch_plain" : "acdc_batch_solve_path");
   if (opt->plain) return plain_path(ctx, count, problems, lambdas, opt, results, x_out);
   return batched_path(ctx, count, problems, lambdas, opt, results, x_out);
 }
@@ -638,6 +639,7 @@ extern "C" int acdc_server_step(acdc_server* s, int32_t* pending) {
   if (!s) return ACDC_EINVAL;
   acdc_ctx* ctx = s->ctx;
   ACDC_CK(ctx, cudaSetDevice(ctx->device));
+  NvtxRange range("acdc_server_step");
   admit(s);
   if (!s->resident.empty()) {
     if (s->dirty) {
