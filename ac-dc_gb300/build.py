@@ -77,7 +77,7 @@ def build_gpu(verbose=False):
             if verbose and out:
                 print(out)
     if _stale(GPU_LIB, objs):
-        _run([nvcc()] + ARCH + ["-shared", "-o", GPU_LIB] + objs + ["-Xcompiler", "-fopenmp"])
+        _run([nvcc()] + ARCH + ["-shared", "-o", GPU_LIB] + objs + ["-ldl", "-Xcompiler", "-fopenmp"])
     return GPU_LIB
 
 
