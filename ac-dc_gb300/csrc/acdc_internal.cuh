@@ -313,8 +313,6 @@ cudaError_t launch_list_long(const DevProblem& d, int32_t* list, unsigned long l
 // omega over the active list (counters[CNT_OMEGA_ACTIVE]); rowcnt holds m ints.
 cudaError_t launch_active_omega(const EvalParams& p, int32_t* rowcnt, cudaStream_t st);
 cudaError_t launch_gap(const EvalParams& p, cudaStream_t st);
-// Active-set violations (Lasso, after a full gap pass that built the list).
-cudaError_t launch_active_viol(const EvalParams& p, cudaStream_t st);
 // Test-set 0-1 accuracy (count of positive margins into *good).
 cudaError_t launch_test_accuracy(int64_t n_test, const int64_t* row_ptr, const int32_t* col_idx,
                                  const double* vals, const double* labels, const double* w64,
