@@ -105,6 +105,9 @@ def parse_args():
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--serve-quantum", type=int, default=4,
                     help="rounds per server step (acdc_server_options.quantum_epochs)")
+    ap.add_argument("--active-passes", type=int, default=0,
+                    help="passes over the active set per bulk while q-shrinking (Lasso; "
+                         "0 = the workload's own, 100 for the 1e6 x 1e7 Lasso)")
     ap.add_argument("--probe-launches", action="store_true",
                     help="profiling aid: run one uniform-draw update launch (refresh_every "
                          "epochs) and one active-set launch (active_passes |A|/q updates) on "
@@ -680,6 +683,8 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     w = dict(WORKLOADS[args.workload], name=args.workload)
+    if args.active_passes > 0 and "active_passes" in w:
+        w["active_passes"] = args.active_passes
     if args.probe_launches:
         return probe_launches(w)
     if args.max_epochs > 0:
