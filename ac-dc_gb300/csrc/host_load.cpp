@@ -56,6 +56,63 @@ int pieces_for(size_t len) {
 bool is_space(char c) { return c == ' ' || c == '\n' || c == '\r' || c == '\t'; }
 bool is_newline(char c) { return c == '\n'; }
 
+// Decimal number at p with strtod's result and end pointer.  Plain decimals
+// ([+-]digits[.digits][(e|E)[+-]digits]) of at most 19 significant digits whose
+// digits fit a 53-bit integer w and whose decimal exponent e lies in [-22, 22]
+// are converted as w * 10^e or w / 10^-e: w and 10^|e| are exact doubles, so the
+// one rounded operation gives the correctly rounded value (Clinger, "How to
+// read floating point numbers accurately", PLDI 1990), which is what strtod
+// returns.  Every other token (more digits, larger exponents, hex, inf, nan, a
+// letter right after the number) goes to strtod itself.  end bounds the fast
+// path only; strtod, like before, reads the NUL-terminated text.
+const char* parse_double(const char* p, const char* end, double* out) {
+  static const double kPow10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,
+                                    1e8,  1e9,  1e10, 1e11, 1e12, 1e13, 1e14, 1e15,
+                                    1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+  const char* q = p;
+  bool neg = false;
+  if (q < end && (*q == '+' || *q == '-')) neg = *q++ == '-';
+  uint64_t w = 0;
+  int sig = 0, digits = 0, frac = 0;
+  for (; q < end && *q >= '0' && *q <= '9'; ++q, ++digits)
+    if (sig || *q != '0') {
+      if (++sig > 19) goto slow;
+      w = w * 10 + (uint64_t)(*q - '0');
+    }
+  if (q < end && *q == '.') {
+    for (++q; q < end && *q >= '0' && *q <= '9'; ++q, ++digits, ++frac)
+      if (sig || *q != '0') {
+        if (++sig > 19) goto slow;
+        w = w * 10 + (uint64_t)(*q - '0');
+      }
+  }
+  if (digits == 0) goto slow;
+  {
+    int e = 0;
+    if (q < end && (*q == 'e' || *q == 'E')) {
+      const char* t = q + 1;
+      bool eneg = false;
+      if (t < end && (*t == '+' || *t == '-')) eneg = *t++ == '-';
+      if (!(t < end && *t >= '0' && *t <= '9')) goto slow;
+      for (; t < end && *t >= '0' && *t <= '9'; ++t)
+        if ((e = e * 10 + (*t - '0')) > 1000) goto slow;
+      if (eneg) e = -e;
+      q = t;
+    }
+    if (q < end && (*q == '.' || ((*q | 0x20) >= 'a' && (*q | 0x20) <= 'z'))) goto slow;
+    e -= frac;
+    if (w > ((uint64_t)1 << 53) || e < -22 || e > 22) goto slow;
+    double v = (double)w;
+    v = e >= 0 ? v * kPow10[e] : v / kPow10[-e];
+    *out = neg ? -v : v;
+    return q;
+  }
+slow:
+  char* r = nullptr;
+  *out = std::strtod(p, &r);
+  return r;
+}
+
 // Cuts [0, len) into k ranges whose inner boundaries sit just after a
 // separator, so that no token (or line) is split; ranges may be empty.
 std::vector<size_t> cut_after(const std::string& text, int k, bool (*sep)(char)) {
@@ -102,9 +159,9 @@ bool parse_range(const char* p, const char* end, std::vector<T>& out) {
   while (p < end) {
     while (p < end && is_space(*p)) ++p;
     if (p >= end) break;
-    char* q = nullptr;
     errno = 0;
-    double v = std::strtod(p, &q);
+    double v = 0;
+    const char* q = parse_double(p, end, &v);
     if (q == p || q > end || errno == ERANGE || !std::isfinite(v)) return false;
     out.push_back((T)v);
     p = q;
@@ -222,8 +279,10 @@ int walk_libsvm(const char* p, const char* end, LibsvmScan& sc, int64_t n0, int6
     while (q < eol && (*q == ' ' || *q == '\t' || *q == '\r')) ++q;
     if (q < eol && *q != '#') {
       char* r = nullptr;
-      double label = std::strtod(q, &r);
-      if (r == q || r > eol || !std::isfinite(label)) return ACDC_EINVAL;
+      double label = 0;
+      const char* lq = parse_double(q, eol, &label);
+      if (lq == q || lq > eol || !std::isfinite(label)) return ACDC_EINVAL;
+      r = const_cast<char*>(lq);
       q = r;
       if (row_ptr) {
         row_ptr[n0 + n] = nnz0 + nnz;
@@ -237,9 +296,10 @@ int walk_libsvm(const char* p, const char* end, LibsvmScan& sc, int64_t n0, int6
         q = r + 1;
         // the value follows the colon directly (strtod would skip a line end)
         if (q >= eol || *q == ' ' || *q == '\t' || *q == '\r') return ACDC_EINVAL;
-        double v = std::strtod(q, &r);
-        if (r == q || r > eol || !std::isfinite(v)) return ACDC_EINVAL;
-        q = r;
+        double v = 0;
+        const char* vq = parse_double(q, eol, &v);
+        if (vq == q || vq > eol || !std::isfinite(v)) return ACDC_EINVAL;
+        q = vq;
         if (idx > d) d = idx;
         if (idx - 1 > INT32_MAX) return ACDC_EINVAL;
         if (col_idx) {

@@ -195,6 +195,53 @@ def test_csc_text_loader_roundtrip(tmp_path):
     assert np.array_equal(acdc.load_csc_text(pre, str(tmp_path / "b.txt"), 0.5).vals, inst.vals)
 
 
+def decimal_tokens(count, seed):
+    """Decimal strings of many shapes: signs, leading and trailing zeros, points at
+    either end, exponents with and without signs, 1 to 24 significant digits."""
+    rng = np.random.default_rng(seed)
+    out = ["0", "-0", "+0.0", "0.1", "0.2", "0.3", "1e22", "1e23", "-1E-22", "9007199254740992",
+           "9007199254740993", "123456789012345678", "1.7976931348623157e308", "2.2250738585072014e-308",
+           "5.", ".5", "-.5e+3", "00012.5000", "1234567890123456789", "12345678901234567890", "7e0",
+           "3.14159265358979323846264338327950288", "1e-0022", "0.000000000000000000000001"]
+    for _ in range(count):
+        nd = int(rng.integers(1, 25))
+        digits = "".join(str(d) for d in rng.integers(0, 10, nd))
+        if rng.random() < 0.3:
+            digits = "0" * int(rng.integers(1, 4)) + digits
+        point = int(rng.integers(0, len(digits) + 1))
+        t = digits[:point] + ("." if rng.random() < 0.8 else "") + digits[point:]
+        if rng.random() < 0.5:
+            t += rng.choice(["e", "E"]) + rng.choice(["", "+", "-"]) + str(int(rng.integers(0, 40)))
+        t = rng.choice(["", "-", "+"]) + t
+        out.append(t)
+    return out
+
+
+def test_text_numbers_are_read_as_correctly_rounded_doubles(tmp_path):
+    """The loaders' decimal conversion (a fast path for short decimals, strtod for
+    the rest) gives the correctly rounded double of every token, as Python's
+    float() does: bit for bit, signed zeros included."""
+    toks = decimal_tokens(20000, 7)
+    want = np.array([float(t) for t in toks])
+    pre = str(tmp_path / "A")
+    with open(pre + "_values.txt", "w") as f:
+        f.write("\n".join(toks) + "\n")
+    np.savetxt(pre + "_colPtr.txt", np.arange(len(toks) + 1), fmt="%d")
+    np.savetxt(pre + "_rowIdx.txt", np.zeros(len(toks), np.int64), fmt="%d")
+    np.savetxt(str(tmp_path / "b.txt"), [1.0])
+    got = acdc.load_csc_text(pre, str(tmp_path / "b.txt"), 0.5).vals
+    assert np.array_equal(got.view(np.int64), want.view(np.int64))
+    path = str(tmp_path / "s.svm")
+    with open(path, "w") as f:
+        for i, t in enumerate(toks):
+            f.write("%s %d:%s\n" % (t if i % 2 else "+1", i % 97 + 1, t))
+    sv = acdc.load_libsvm(path, 1e-3)
+    assert np.array_equal(np.asarray(sv.vals).view(np.int64), want.view(np.int64))
+    labels = np.array([float(t) if i % 2 else 1.0 for i, t in enumerate(toks)])
+    labels[labels == 0] = -1.0
+    assert np.array_equal(np.asarray(sv.rhs), labels)
+
+
 def test_csc_text_loader_rejects_bad_input(tmp_path):
     pre = str(tmp_path / "A")
     open(pre + "_values.txt", "w").write("1 2 3\n")
