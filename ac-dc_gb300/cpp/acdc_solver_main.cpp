@@ -137,7 +137,8 @@ int main(int argc, char* argv[]) {
       if (++rows[(size_t)r] > omega) omega = rows[(size_t)r];
   }
   instance.omega = omega;
-  instance.sigma = 1 + (omega - 1) * (settings.totalThreads - 1) / (instance.n - 1.0);
+  // (one column: the reference's formula divides by zero; beta is then 1)
+  instance.sigma = instance.n > 1 ? 1 + (omega - 1) * (settings.totalThreads - 1) / (instance.n - 1.0) : 1.0;
   std::cout << "Omega: " << omega << std::endl;
   if (q > 0) {
     settings.use_shrinking = true;

@@ -61,34 +61,7 @@ class CudaEngineExecutor : public AbstractEngineExecutor<L, D> {
     loss_ = s->lossFunction;
     if (loss_ < ACDC_LOSS_L1_SQUARE || loss_ > ACDC_LOSS_LOGISTIC)
       throw std::runtime_error("unknown lossFunction " + std::to_string(loss_));
-    check(acdc_ctx_create(opt.device, &ctx_), "acdc_ctx_create");
-    // Losses 0, 1 and 3 read the CSC arrays (for 3 after MultiCoreSolver.cpp:80-105
-    // turned the samples into rows), the SVM dual the CSR by sample
-    // (MulticoreEngineExecutor.h:32-58).  For loss 3 without the CSC arrays the
-    // sample rows (A_csr_*, m = samples) are transposed on the device.
-    const int64_t n = (int64_t)inst.n;
-    const bool rows = loss_ == ACDC_LOSS_LOGISTIC && inst.A_csc_col_ptr.empty();
-    const bool csc = loss_ != ACDC_LOSS_SVM_DUAL && !rows;
-    const std::vector<L>& ptr = csc ? inst.A_csc_col_ptr : inst.A_csr_row_ptr;
-    const std::vector<L>& idx = csc ? inst.A_csc_row_idx : inst.A_csr_col_idx;
-    const std::vector<D>& val = csc ? inst.A_csc_values : inst.A_csr_values;
-    const int64_t ptr_len = rows ? (int64_t)inst.m + 1 : n + 1;
-    if ((int64_t)ptr.size() != ptr_len) throw std::runtime_error("pointer array does not match the sizes");
-    std::vector<int64_t> cp(ptr.begin(), ptr.end());
-    std::vector<int32_t> ri(idx.begin(), idx.end());
-    std::vector<double> va(val.begin(), val.end());
-    std::vector<double> rhs(inst.b.begin(), inst.b.end());
-    if (rows)
-      check(acdc_problem_create_rows(ctx_, loss_, (int64_t)inst.m, n, cp.data(),
-                                     ri.empty() ? nullptr : ri.data(),
-                                     va.empty() ? nullptr : va.data(), rhs.data(),
-                                     (double)inst.lambda, &prob_),
-            "acdc_problem_create_rows");
-    else
-      check(acdc_problem_create(ctx_, loss_, (int64_t)inst.m, n, cp.data(),
-                                ri.empty() ? nullptr : ri.data(), va.empty() ? nullptr : va.data(),
-                                rhs.data(), (double)inst.lambda, &prob_),
-            "acdc_problem_create");
+    // Settings first: a bad value is refused before any device work.
     acdc_settings st;
     acdc_settings_default(&st);
     st.loss = loss_;
@@ -111,8 +84,47 @@ class CudaEngineExecutor : public AbstractEngineExecutor<L, D> {
     st.precision = opt.precision;
     st.tau_active = opt.tau_active;
     st.active_passes = opt.active_passes;
-    check(acdc_problem_set_settings(prob_, &st), "acdc_problem_set_settings");
-    inst.x.assign((size_t)n, (D)0);
+    if (acdc_settings_check(&st) != ACDC_OK)
+      throw std::runtime_error("OptimizationSettings out of range for the GPU engine");
+    check(acdc_ctx_create(opt.device, &ctx_), "acdc_ctx_create");
+    // A constructor that throws runs no destructor: release what exists here.
+    try {
+      // Losses 0, 1 and 3 read the CSC arrays (for 3 after MultiCoreSolver.cpp:80-105
+      // turned the samples into rows), the SVM dual the CSR by sample
+      // (MulticoreEngineExecutor.h:32-58).  For loss 3 without the CSC arrays the
+      // sample rows (A_csr_*, m = samples) are transposed on the device.
+      const int64_t n = (int64_t)inst.n;
+      const bool rows = loss_ == ACDC_LOSS_LOGISTIC && inst.A_csc_col_ptr.empty();
+      const bool csc = loss_ != ACDC_LOSS_SVM_DUAL && !rows;
+      const std::vector<L>& ptr = csc ? inst.A_csc_col_ptr : inst.A_csr_row_ptr;
+      const std::vector<L>& idx = csc ? inst.A_csc_row_idx : inst.A_csr_col_idx;
+      const std::vector<D>& val = csc ? inst.A_csc_values : inst.A_csr_values;
+      const int64_t ptr_len = rows ? (int64_t)inst.m + 1 : n + 1;
+      if ((int64_t)ptr.size() != ptr_len) throw std::runtime_error("pointer array does not match the sizes");
+      std::vector<int64_t> cp(ptr.begin(), ptr.end());
+      std::vector<int32_t> ri(idx.begin(), idx.end());
+      std::vector<double> va(val.begin(), val.end());
+      std::vector<double> rhs(inst.b.begin(), inst.b.end());
+      if (rows)
+        check(acdc_problem_create_rows(ctx_, loss_, (int64_t)inst.m, n, cp.data(),
+                                       ri.empty() ? nullptr : ri.data(),
+                                       va.empty() ? nullptr : va.data(), rhs.data(),
+                                       (double)inst.lambda, &prob_),
+              "acdc_problem_create_rows");
+      else
+        check(acdc_problem_create(ctx_, loss_, (int64_t)inst.m, n, cp.data(),
+                                  ri.empty() ? nullptr : ri.data(), va.empty() ? nullptr : va.data(),
+                                  rhs.data(), (double)inst.lambda, &prob_),
+              "acdc_problem_create");
+      check(acdc_problem_set_settings(prob_, &st), "acdc_problem_set_settings");
+    } catch (...) {
+      if (prob_) acdc_problem_destroy(prob_);
+      prob_ = nullptr;
+      acdc_ctx_destroy(ctx_);
+      ctx_ = nullptr;
+      throw;
+    }
+    inst.x.assign((size_t)inst.n, (D)0);
   }
 
   ~CudaEngineExecutor() {

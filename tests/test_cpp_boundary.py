@@ -60,6 +60,16 @@ def write_csc(tmp_path, inst):
     return pre, str(tmp_path / "b.txt")
 
 
+def test_console_solver_refuses_bad_settings_before_device_work(tmp_path):
+    """A shrinking probability above 1 is refused by the engine's settings check,
+    which runs before a context is made (so this needs no GPU)."""
+    inst = acdc.gen_lasso(60, 90, nnz_per_col=4, n_star=5, seed=3)
+    pre, bfile = write_csc(tmp_path, inst)
+    out = subprocess.run([SOLVER, "-A", pre, "-b", bfile, "-l", "0.1", "-f", "0", "-S", "1.5"],
+                         capture_output=True, text=True, timeout=60)
+    assert out.returncode == 1 and "out of range" in out.stderr, out.stderr
+
+
 @pytest.mark.gpu
 def test_console_solver_reaches_the_oracle_optimum(tmp_path):
     inst = acdc.gen_lasso(800, 3000, nnz_per_col=10, n_star=40, lambda_frac=0.1, seed=91)
