@@ -10,8 +10,10 @@
 //
 // Behaviour per reference member:
 //  * constructor: loss switch on settings->lossFunction (0: L1-regularised
-//    square loss on A_csc_*, 2: SVM dual on A_csr_* with labels in b; 1 and 3
-//    throw std::runtime_error), x = 0, residual refreshed, reciprocal
+//    square loss on A_csc_*; 1: L2-regularised square loss on A_csc_*; 2: SVM
+//    dual on A_csr_* with labels in b; 3: L2-regularised logistic loss on
+//    A_csc_* after the samples were made rows; any other code throws
+//    std::runtime_error), x = 0, residual refreshed, reciprocal
 //    Lipschitz constants Li = 1/(sigma ||a_j||^2) with sigma = forcedSigma when
 //    positive, instance.sigma for the SVM, else the ESO value for
 //    tau = totalThreads;

@@ -11,9 +11,11 @@
 // the pool is a driver call).
 //
 // Scratch: ACDC_NOALLOC_MAX_SAMPLES int64 draws (512 KiB) and one status word,
-// both file-scope __device__ arrays of this module.  Their device addresses
-// are looked up once per device with cudaGetSymbolAddress, with that device
-// current, by the first call on the device; the lookup may load the module, so
+// both file-scope __device__ arrays of this module.  Every call makes the
+// context's device current and restores the caller's device before it
+// returns.  The device addresses of the arrays are looked up once per device
+// with cudaGetSymbolAddress, with that device current, by the first call on
+// the device; the lookup may load the module, so
 // the first call on a device should come before any stream capture.  The status
 // word must start at zero and is cleared by every call.  There is one scratch
 // array per device, so calls that overlap on one device (two host threads, or
@@ -39,6 +41,22 @@ struct ScratchAddr {
 std::mutex g_setup_mu;
 ScratchAddr g_addr[kMaxDevices];
 
+// Makes dev current for the scope and gives the caller's thread its previous
+// device back on every return path.
+struct CurrentDevice {
+  int prev = -1;
+  cudaError_t err = cudaSuccess;
+  explicit CurrentDevice(int dev) {
+    err = cudaGetDevice(&prev);
+    if (err == cudaSuccess) err = cudaSetDevice(dev);
+  }
+  ~CurrentDevice() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+  CurrentDevice(const CurrentDevice&) = delete;
+  CurrentDevice& operator=(const CurrentDevice&) = delete;
+};
+
 // The same draw as k_debug_sample; a draw outside [0, n) (impossible for the
 // 64x64 high product, checked all the same) sets bit 0 of the status word.
 __global__ void k_debug_sample_fixed(uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
@@ -55,14 +73,12 @@ __global__ void k_debug_sample_fixed(uint64_t seed, uint64_t k0, uint64_t count,
   }
 }
 
-// Device addresses of the scratch for ctx's device (looked up on first use).
+// Device addresses of the scratch for ctx's device (looked up on first use);
+// the caller has made ctx's device current.
 int scratch_for(acdc_ctx* ctx, ScratchAddr* out) {
-  if (ctx->device < 0 || ctx->device >= kMaxDevices)
-    return acdc_set_error(ctx, ACDC_EINVAL, "device index out of range for the fixed scratch");
   std::lock_guard<std::mutex> lock(g_setup_mu);
   ScratchAddr& a = g_addr[ctx->device];
   if (!a.draws) {
-    ACDC_CK(ctx, cudaSetDevice(ctx->device));
     void* draws = nullptr;
     void* status = nullptr;
     ACDC_CK(ctx, cudaGetSymbolAddress(&draws, g_sample_scratch));
@@ -81,6 +97,12 @@ extern "C" int acdc_debug_sample_noalloc(acdc_ctx* ctx, uint64_t seed, uint64_t 
   if (!ctx || (count > 0 && !out) || n <= 0) return ACDC_EINVAL;
   if (count > (uint64_t)ACDC_NOALLOC_MAX_SAMPLES)
     return acdc_set_error(ctx, ACDC_EINVAL, "count exceeds ACDC_NOALLOC_MAX_SAMPLES");
+  if (ctx->device < 0 || ctx->device >= kMaxDevices)
+    return acdc_set_error(ctx, ACDC_EINVAL, "device index out of range for the fixed scratch");
+  // Every call runs on the context's device, whatever the calling thread has
+  // current, and leaves the thread's current device as it found it.
+  CurrentDevice on(ctx->device);
+  if (on.err != cudaSuccess) return acdc_cuda_error(ctx, on.err, "cudaSetDevice");
   ScratchAddr a;
   int rc = scratch_for(ctx, &a);
   if (rc != ACDC_OK) return rc;

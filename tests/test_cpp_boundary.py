@@ -13,7 +13,8 @@ import acdc
 import oracle
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference/cpp/src"
+# the reference checkout's sources (ACDC_REFERENCE_ROOT); the check is skipped without it
+REF = os.path.join(os.environ.get("ACDC_REFERENCE_ROOT", ""), "cpp", "src")
 CPP = os.path.join(ROOT, "ac-dc_gb300", "cpp")
 SOLVER = os.path.join(ROOT, "ac-dc_gb300", "lib", "acdc_solver")
 
@@ -33,7 +34,8 @@ int probe(ProblemData<int, double>& inst, OptimizationSettings* s) {
 """
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources not present")
+@pytest.mark.skipif(not os.environ.get("ACDC_REFERENCE_ROOT") or not os.path.isdir(REF),
+                    reason="reference sources not present (set ACDC_REFERENCE_ROOT)")
 def test_engine_header_compiles_against_reference_headers(tmp_path):
     src = tmp_path / "probe.cpp"
     src.write_text(PROBE)

@@ -81,14 +81,15 @@ def test_gpu_library_loads_and_reports_no_device_cleanly():
 def test_settings_check_refuses_every_out_of_range_field():
     """acdc_settings_check (the check acdc_problem_set_settings makes) needs no
     device: defaults of every loss pass, and each field outside its range,
-    NaN included, is refused on its own."""
+    NaN and infinities included, is refused on its own (an infinite gap target
+    would end a solve at its first evaluation)."""
     nan, inf = float("nan"), float("inf")
     for loss in range(4):
         assert acdc.settings_ok(acdc.default_settings(loss))
     assert acdc.gpu_lib().acdc_settings_check(None) == acdc.EINVAL
     good = [("sigma", -1.0), ("sigma", 0.0), ("sigma", 1.7), ("shrinking_probability", 0.0),
             ("shrinking_probability", 1.0), ("shrink_eps", 0.0), ("gap_target", 0.0),
-            ("gap_target", inf), ("tau_active", 0), ("max_epochs", 0), ("warps_per_block", 8),
+            ("gap_target", 1e300), ("tau_active", 0), ("max_epochs", 0), ("warps_per_block", 8),
             ("precision", acdc.PREC_FP64), ("hot_threshold", 0.0), ("polish_stall_epochs", 0),
             ("hot_polish_sweeps", 0), ("polish_active_passes", 0), ("active_passes", -3),
             ("shrinking_starting_iter", -1)]
@@ -99,6 +100,7 @@ def test_settings_check_refuses_every_out_of_range_field():
            ("shrinking_probability", nan), ("shrink_eps", -0.1), ("shrink_eps", 1.0),
            ("shrink_eps", nan), ("precision", -1), ("precision", 3), ("polish_rel_gap", -1.0),
            ("polish_rel_gap", nan), ("hot_threshold", -0.5), ("hot_threshold", nan),
+           ("gap_target", inf), ("polish_rel_gap", inf), ("hot_threshold", inf),
            ("polish_stall_epochs", -1), ("hot_polish_sweeps", -1), ("polish_active_passes", -1)]
     for field, value in good:
         assert acdc.settings_ok(acdc.default_settings(**{field: value})), (field, value)

@@ -23,6 +23,15 @@ def test_two_calls_in_a_row_match_the_allocating_entry_point(ctx):
         assert got.min() >= 0 and got.max() < n
 
 
+def test_calls_leave_the_memory_pool_unchanged(ctx):
+    # a warm call first: the first call on a device looks up the scratch address
+    acdc.debug_sample_noalloc(ctx, 3, 0, 1024, 5000)
+    before = ctx.memory()
+    for k0 in (0, 10**6):
+        acdc.debug_sample_noalloc(ctx, 3, k0, acdc.NOALLOC_MAX_SAMPLES, 5000)
+    assert ctx.memory() == before
+
+
 def test_sizes_beyond_the_scratch_are_refused(ctx):
     with pytest.raises(acdc.AcdcError) as e:
         acdc.debug_sample_noalloc(ctx, 1, 0, acdc.NOALLOC_MAX_SAMPLES + 1, 100)
