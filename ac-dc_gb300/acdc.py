@@ -32,7 +32,7 @@ class Settings(C.Structure):
                 ("shrinking_probability", D), ("shrink_eps", D), ("precision", I32),
                 ("tau_active", I32), ("polish_rel_gap", D), ("active_passes", I32),
                 ("screened_eval", I32), ("polish_stall_epochs", I32), ("hot_polish_sweeps", I32),
-                ("hot_threshold", D), ("polish_active_passes", I32), ("reserved2", I32)]
+                ("hot_threshold", D), ("polish_active_passes", I32), ("lanes_per_update", I32)]
 
 
 class Eval(C.Structure):
@@ -152,6 +152,7 @@ def gpu_lib():
         L.acdc_settings_check.argtypes = [C.POINTER(Settings)]
         L.acdc_ctx_create.argtypes = [C.c_int, C.POINTER(VP)]
         L.acdc_ctx_destroy.argtypes = [VP]
+        L.acdc_ctx_memory.argtypes = [VP, C.POINTER(I64), C.POINTER(I64)]
         L.acdc_problem_create.argtypes = [VP, I32, I64, I64, VP, VP, VP, VP, D, C.POINTER(VP)]
         L.acdc_problem_create_i32.argtypes = [VP, I32, I64, I64, VP, VP, VP, VP, D, C.POINTER(VP)]
         L.acdc_problem_create_rows.argtypes = [VP, I32, I64, I64, VP, VP, VP, VP, D,
@@ -423,6 +424,12 @@ class Context:
         """Destroys the context once no problem created on it is alive."""
         if self.h and self.L.acdc_ctx_destroy(self.h) == OK:
             self.h = None
+
+    def memory(self):
+        """(reserved, used) bytes of the context's device memory pool."""
+        r, u = I64(0), I64(0)
+        self.check(self.L.acdc_ctx_memory(self.h, C.byref(r), C.byref(u)))
+        return int(r.value), int(u.value)
 
     def __del__(self):
         try:

@@ -90,6 +90,10 @@ struct UpdateParams {
   int32_t loss;
   int32_t fp64;         // 1: x and r in FP64 (x64, r64)
   uint64_t k_base;      // sampler counter of the launch's first update (batched launches)
+  // Lanes per update: 8 or 32 select the grouped kernel (32 / lanes updates
+  // per warp, register prefetch); anything else the one-warp ring kernel.
+  int32_t lanes = 0;
+  int32_t sm_count = 0;  // SMs of the device (the grouped kernel spreads its warps over them)
 };
 
 // Parameters of the evaluation kernels.

@@ -75,16 +75,20 @@ const char* settings_fault(const acdc_settings* s) {
   if (s->max_epochs < 0) return "max_epochs";
   // sigma <= 0 asks for the computed beta; NaN and infinities are no beta.
   if (!(std::fabs(s->sigma) <= 1.7976931348623157e308)) return "sigma";
-  if (!(s->gap_target >= 0)) return "gap_target";
+  // finite and non-negative: +inf would end every solve at its first evaluation
+  if (!(std::isfinite(s->gap_target) && s->gap_target >= 0)) return "gap_target";
   if (!(s->shrinking_probability >= 0 && s->shrinking_probability <= 1))
     return "shrinking_probability";
   if (!(s->shrink_eps >= 0 && s->shrink_eps < 1)) return "shrink_eps";
   if (s->precision < ACDC_PREC_AUTO || s->precision > ACDC_PREC_FP64) return "precision";
-  if (!(s->polish_rel_gap >= 0)) return "polish_rel_gap";
-  if (!(s->hot_threshold >= 0)) return "hot_threshold";
+  if (!(std::isfinite(s->polish_rel_gap) && s->polish_rel_gap >= 0)) return "polish_rel_gap";
+  if (!(std::isfinite(s->hot_threshold) && s->hot_threshold >= 0)) return "hot_threshold";
   if (s->polish_stall_epochs < 0) return "polish_stall_epochs";
   if (s->hot_polish_sweeps < 0) return "hot_polish_sweeps";
   if (s->polish_active_passes < 0) return "polish_active_passes";
+  if (s->lanes_per_update != 0 && s->lanes_per_update != -1 && s->lanes_per_update != 8 &&
+      s->lanes_per_update != 16 && s->lanes_per_update != 32)
+    return "lanes_per_update";
   return nullptr;
 }
 
@@ -145,6 +149,16 @@ extern "C" int acdc_ctx_destroy(acdc_ctx* ctx) {
   if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
   for (void* b : ctx->host_blocks) cudaFreeHost(b);
   delete ctx;
+  return ACDC_OK;
+}
+
+extern "C" int acdc_ctx_memory(acdc_ctx* ctx, int64_t* reserved, int64_t* used) {
+  if (!ctx || !reserved || !used) return ACDC_EINVAL;
+  uint64_t r = 0, u = 0;
+  ACDC_CK(ctx, cudaMemPoolGetAttribute(ctx->pool, cudaMemPoolAttrReservedMemCurrent, &r));
+  ACDC_CK(ctx, cudaMemPoolGetAttribute(ctx->pool, cudaMemPoolAttrUsedMemCurrent, &u));
+  *reserved = (int64_t)r;
+  *used = (int64_t)u;
   return ACDC_OK;
 }
 
@@ -267,6 +281,15 @@ EvalParams eval_params(acdc_problem* p, bool build_active) {
   return e;
 }
 
+// Lanes per update of the problem's update launches (settings.lanes_per_update;
+// 0 = the one-warp ring kernel, the fastest per update in the measurements of
+// both the uniform and the active-set launches at the default tau).
+int32_t lanes_for(const acdc_problem* p) {
+  const int32_t l = p->s.lanes_per_update;
+  if (l == 8 || l == 16 || l == 32) return l;
+  return -1;
+}
+
 UpdateParams update_params(acdc_problem* p, uint64_t count, bool shrink) {
   UpdateParams u;
   u.meta = p->d.meta;
@@ -299,6 +322,8 @@ UpdateParams update_params(acdc_problem* p, uint64_t count, bool shrink) {
     u.shrink_q32 = (uint32_t)(q * 4294967296.0);
   u.n_warps = (shrink && p->s.tau_active > 0) ? p->s.tau_active : p->s.tau;
   u.loss = p->loss;
+  u.lanes = lanes_for(p);
+  u.sm_count = p->ctx->sm_count;
   if (shrink && u.shrink_q32 && p->hot_count > 0 && p->hot_q > 0) {
     u.hot = p->d.hot;
     u.hot_q32 = (uint32_t)std::min(4294967295.0, p->hot_q * 4294967296.0);

@@ -66,19 +66,22 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// Sum over the lanes that hold entries of a column of len entries, returned
-// in every lane.  Only the lowest ceil(len/4) lanes carry nonzero partials, so
-// log2 of that many butterfly steps suffice before a broadcast from lane 0.
+// Sum over the lanes that hold entries of a column of len entries.  Lane l
+// holds entries 4l..4l+3, so a column of at most 16 entries lives in lanes
+// 0..3: two butterfly steps give its sum in those lanes, which are the only
+// ones that scatter (lane 0 also writes x_j); other lanes get partial sums
+// that they do not use.  Longer columns take all five steps (sum in every
+// lane).  No broadcast and no loop: the short case is two dependent shuffles.
 template <typename T>
 __device__ __forceinline__ T column_sum(T v, uint32_t len) {
-  if (len > 64u) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(ACDC_FULL_MASK, v, o);
-    return v;  // every butterfly step adds the same pair in both lanes
+  v += __shfl_xor_sync(ACDC_FULL_MASK, v, 1);
+  v += __shfl_xor_sync(ACDC_FULL_MASK, v, 2);
+  if (len > 16u) {
+    v += __shfl_xor_sync(ACDC_FULL_MASK, v, 4);
+    v += __shfl_xor_sync(ACDC_FULL_MASK, v, 8);
+    v += __shfl_xor_sync(ACDC_FULL_MASK, v, 16);
   }
-  const uint32_t lanes = (len + 3u) >> 2;  // 1..16
-  for (uint32_t o = 1; o < lanes; o <<= 1) v += __shfl_xor_sync(ACDC_FULL_MASK, v, (int)o);
-  return __shfl_sync(ACDC_FULL_MASK, v, 0);
+  return v;
 }
 
 // Coordinate of update k.  With shrinking, word 2 picks the tier (hot set below
@@ -278,8 +281,9 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
       cp_async_commit();
 
       // g = a_j^T r.  (Issuing these gathers before the refill above, or
-      // prefetching x_j into L2 with the record, shortens uniform-draw launches
-      // but lengthens active-set ones, which dominate the solve.)
+      // prefetching x_j into L2 with the record, did not shorten the launches
+      // in the measurements: active-set launches, which dominate the solve,
+      // got longer.)
       T acc = gather_dot_head<LOSS, T>(r, c0, e0, len);
       if (len > 128u) {
         Chunk a = load_chunk(p, start, len, 128u, lane);
@@ -320,7 +324,9 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
         coef = delta * y * inv_ln;
       }
       chunk_read += len;
-      if (delta != T(0)) {
+      // lanes with entries (and lane 0, which writes x_j) hold the column's sum
+      const bool holds = e0 < len || lane == 0 || len > 16u;
+      if (holds && delta != T(0)) {
         chunk_nz++;
         chunk_scat += len;
         scatter_head<T>(r, c0, coef, e0, len);
@@ -355,6 +361,228 @@ template <int LOSS, typename T>
 __global__ void __launch_bounds__(256, 4) k_pcdm_update(UpdateParams p, uint64_t k_base) {
   __shared__ WarpRing rings[kMaxWarps];
   pcdm_update_body<LOSS, T>(p, k_base, blockIdx.x, rings);
+}
+
+// ---- grouped update kernel: G lanes per update, 32/G updates per warp ----
+//
+// A group of G lanes (G = 8, 16 or 32) performs one update at a time; a warp runs
+// 32/G groups side by side on independent update numbers, so p.n_warps (tau,
+// the updates in flight) needs tau G / 32 warps.  Lane l of a group holds
+// entries 4l..4l+3 of a column's first 4G entries (one 128-bit load of values
+// and one of row indices, the layout's 16-byte column starts); longer columns
+// stream further chunks of 4G entries.  Nothing is staged in shared memory but
+// the warp's drawn coordinates: the record of the group's update i+3 and the
+// first entry chunk of update i+2 are loaded into registers while update i
+// runs (ld.global.nc: the matrix and the records do not change during a
+// launch), so one update costs the gathers of r, the group reduction (log2 G
+// shuffles) and the scatter, with no copy bookkeeping.  x_j and r are read
+// through L2 (ld.cg) when the update runs, as in the ring kernel.
+struct GroupChunk {
+  float4 v;
+  int4 i;
+};
+
+template <int G>
+__device__ __forceinline__ GroupChunk group_chunk(const UpdateParams& p, int4 mt, int gl,
+                                                  bool stream) {
+  GroupChunk c;
+  const uint32_t len = (uint32_t)mt.y;
+  const uint32_t e = 4u * (uint32_t)gl;
+  if (e < len) {
+    const uint64_t src = ((uint64_t)(uint32_t)mt.x << 2) + e;
+    if (stream) {
+      c.v = __ldcs(reinterpret_cast<const float4*>(p.vals + src));
+      c.i = __ldcs(reinterpret_cast<const int4*>(p.idx + src));
+    } else {
+      c.v = __ldg(reinterpret_cast<const float4*>(p.vals + src));
+      c.i = __ldg(reinterpret_cast<const int4*>(p.idx + src));
+    }
+  } else {
+    c.v = make_float4(0.f, 0.f, 0.f, 0.f);
+    c.i = make_int4(0, 0, 0, 0);
+  }
+  return c;
+}
+
+template <int G, typename T>
+__device__ __forceinline__ T group_sum(T v, unsigned gmask) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(gmask, v, o);
+  return v;
+}
+
+template <int LOSS, typename T, int G>
+__device__ __forceinline__ void pcdm_update_grouped_body(const UpdateParams& p, uint64_t k_base,
+                                                         int64_t rank, int32_t* coords) {
+  constexpr int kGroups = 32 / G;
+  constexpr uint32_t kSpan = 4u * G;  // entries per chunk
+  const int lane = threadIdx.x & 31;
+  const int gl = lane & (G - 1);
+  const int grp = lane / G;
+  const int64_t gwarp = (rank * blockDim.x + threadIdx.x) >> 5;
+  const int64_t warps = ((int64_t)p.n_warps + kGroups - 1) / kGroups;
+  if (gwarp >= warps) return;
+  // groups of this warp that run (tau need not fill the last warp: tau = 1
+  // keeps a single update in flight)
+  const int ng = (int)min((int64_t)kGroups, (int64_t)p.n_warps - gwarp * kGroups);
+  T* r = reinterpret_cast<T*>(sizeof(T) == 8 ? (void*)p.r64 : (void*)p.r);
+  unsigned long long* work = p.counters + CNT_WORK;
+  const int32_t active_cnt =
+      p.shrink_q32 ? (int32_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n) : 0;
+  const int32_t hot_cnt =
+      p.hot_q32 ? (int32_t)min(p.counters[CNT_HOT], (unsigned long long)p.n) : 0;
+  // uniform-draw launches read each column about once: stream its entries
+  // past L2 instead of evicting the residual and the active columns
+  const bool stream = p.shrink_q32 == 0;
+  const T lam = (T)p.lambda_d;
+  const T inv_ln = (T)p.inv_lambda_n_d;
+  const T li_scale = (T)p.li_scale;
+  const T li_scale_hot = (T)p.li_scale_hot;
+  const uint32_t e0 = 4u * (uint32_t)gl;
+  unsigned long long n_upd = 0, n_nz = 0, n_read = 0, n_scat = 0;
+
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(work, (unsigned long long)kChunk);
+    base = __shfl_sync(ACDC_FULL_MASK, base, 0);
+    if (base >= p.count) break;
+    const int cnt = (int)min((unsigned long long)kChunk, p.count - base);
+#pragma unroll
+    for (int q = 0; q < kChunk / 32; ++q) {
+      const int s = 32 * q + lane;
+      coords[s] = s < cnt ? draw_coord(p, k_base + base + (uint64_t)s, active_cnt, hot_cnt) : 0;
+    }
+    __syncwarp();
+    // this group's updates of the chunk: s = i * ng + grp.  Every lane of the
+    // warp runs the same my_all iterations (a group past its last update, or
+    // beyond ng, runs them with a zero-length record), so the group reductions
+    // are full-warp shuffles of a converged warp.
+    const int my = grp < ng && cnt > grp ? (cnt - grp + ng - 1) / ng : 0;
+    const int my_all = (cnt + ng - 1) / ng;
+    const int4 none = make_int4(0, 0, 0, 0);
+    auto coord_of = [&](int i) { return coords[i * ng + grp]; };
+    auto meta_of = [&](int i) {
+      return i < my ? __ldg(p.meta + (coord_of(i) & kCoordMask)) : none;
+    };
+    // Pipeline: at update i the group holds the records of updates i..i+3 and
+    // the first entry chunks of updates i and i+1; it issues the record of
+    // update i+4 and the chunk of update i+2 (whose record came in two updates
+    // ago) after the gathers of update i, so neither waits on the other.
+    int4 m0 = meta_of(0), m1 = meta_of(1), m2 = meta_of(2), m3 = meta_of(3);
+    GroupChunk c0 = group_chunk<G>(p, m0, gl, stream);
+    GroupChunk c1 = group_chunk<G>(p, m1, gl, stream);
+    for (int i = 0; i < my_all; ++i) {
+      const bool live = i < my;
+      const int32_t cj = live ? coord_of(i) : 0;
+      const int32_t j = cj & kCoordMask;
+      const int4 mt = m0;
+      const uint64_t start = (uint64_t)(uint32_t)mt.x << 2;
+      const uint32_t len = (uint32_t)mt.y;
+      T xj = T(0);
+      if (live) {
+        if constexpr (sizeof(T) == 8)
+          xj = __ldcg(p.x64 + j);
+        else
+          xj = __ldcg(p.x32 + j);
+      }
+      T r0 = T(0), r1 = T(0), r2 = T(0), r3 = T(0);
+      if (e0 < len) r0 = rval<LOSS>(r, c0.i.x);
+      if (e0 + 1u < len) r1 = rval<LOSS>(r, c0.i.y);
+      if (e0 + 2u < len) r2 = rval<LOSS>(r, c0.i.z);
+      if (e0 + 3u < len) r3 = rval<LOSS>(r, c0.i.w);
+      // refill while the gathers are in flight
+      const GroupChunk c2 = group_chunk<G>(p, m2, gl, stream);  // zero past the group's end
+      const int4 m4 = meta_of(i + 4);
+      T acc = (T)c0.v.x * r0;
+      acc += (T)c0.v.y * r1;
+      acc += (T)c0.v.z * r2;
+      acc += (T)c0.v.w * r3;
+      for (uint32_t off = kSpan; off < len; off += kSpan) {
+        const uint32_t e = off + e0;
+        if (e < len) {
+          const float4 v = __ldcs(reinterpret_cast<const float4*>(p.vals + start + e));
+          const int4 ix = __ldcs(reinterpret_cast<const int4*>(p.idx + start + e));
+          acc += (T)v.x * rval<LOSS>(r, ix.x);
+          if (e + 1u < len) acc += (T)v.y * rval<LOSS>(r, ix.y);
+          if (e + 2u < len) acc += (T)v.z * rval<LOSS>(r, ix.z);
+          if (e + 3u < len) acc += (T)v.w * rval<LOSS>(r, ix.w);
+        }
+      }
+      const T g = group_sum<G, T>(acc, ACDC_FULL_MASK);
+      if (live) {
+        const T li = (T)__int_as_float(mt.z) * (cj < 0 ? li_scale_hot : li_scale);
+        T delta, coef;
+        if (LOSS == ACDC_LOSS_L1_SQUARE) {
+          const T z = xj - li * g;
+          T a = fabs(z) - lam * li;
+          a = a < T(0) ? T(0) : a;
+          const T xn = z > T(0) ? a : (z < T(0) ? -a : T(0));
+          delta = xn - xj;
+          coef = delta;
+        } else if (LOSS == ACDC_LOSS_L2_SQUARE) {
+          delta = -li * (g + lam * xj);
+          coef = delta;
+        } else if (LOSS == ACDC_LOSS_LOGISTIC) {
+          delta = -li * (lam * xj - g) / T(2);
+          coef = -delta;
+        } else {
+          const T y = li < T(0) ? T(-1) : T(1);
+          delta = (T(1) - g * y) * lam * fabs(li);
+          if (delta < -xj)
+            delta = -xj;
+          else if (delta > T(1) - xj)
+            delta = T(1) - xj;
+          coef = delta * y * inv_ln;
+        }
+        n_read += len;
+        if (delta != T(0)) {
+          n_nz++;
+          n_scat += len;
+          if (e0 < len) atomicAdd(r + c0.i.x, coef * (T)c0.v.x);
+          if (e0 + 1u < len) atomicAdd(r + c0.i.y, coef * (T)c0.v.y);
+          if (e0 + 2u < len) atomicAdd(r + c0.i.z, coef * (T)c0.v.z);
+          if (e0 + 3u < len) atomicAdd(r + c0.i.w, coef * (T)c0.v.w);
+          for (uint32_t off = kSpan; off < len; off += kSpan) {
+            const uint32_t e = off + e0;
+            if (e < len) {
+              const float4 v = __ldcs(reinterpret_cast<const float4*>(p.vals + start + e));
+              const int4 ix = __ldcs(reinterpret_cast<const int4*>(p.idx + start + e));
+              atomicAdd(r + ix.x, coef * (T)v.x);
+              if (e + 1u < len) atomicAdd(r + ix.y, coef * (T)v.y);
+              if (e + 2u < len) atomicAdd(r + ix.z, coef * (T)v.z);
+              if (e + 3u < len) atomicAdd(r + ix.w, coef * (T)v.w);
+            }
+          }
+          if (gl == 0) {
+            if constexpr (sizeof(T) == 8)
+              atomicAdd(p.x64 + j, delta);
+            else
+              atomicAdd(p.x32 + j, delta);
+          }
+        }
+      }  // live
+      m0 = m1;
+      m1 = m2;
+      m2 = m3;
+      m3 = m4;
+      c0 = c1;
+      c1 = c2;
+    }
+    n_upd += (unsigned)my;
+    __syncwarp();  // every group is done with the chunk's coordinates
+  }
+  if (gl == 0) {
+    atomicAdd(p.counters + CNT_UPDATES, n_upd);
+    atomicAdd(p.counters + CNT_NONZERO, n_nz);
+    atomicAdd(p.counters + CNT_NNZ_READ, n_read);
+    atomicAdd(p.counters + CNT_NNZ_SCATTERED, n_scat);
+  }
+}
+
+template <int LOSS, typename T, int G>
+__global__ void __launch_bounds__(256) k_pcdm_update_grouped(UpdateParams p, uint64_t k_base) {
+  __shared__ int32_t coords[kMaxWarps][kChunk];
+  pcdm_update_grouped_body<LOSS, T, G>(p, k_base, blockIdx.x, coords[threadIdx.x >> 5]);
 }
 
 // Batched launch: each block serves one slot at rank blockIdx.x - first block
@@ -396,6 +624,28 @@ cudaError_t launch_debug_sample(uint64_t seed, uint64_t k0, uint64_t count, int6
   return cudaGetLastError();
 }
 
+template <int G>
+void launch_grouped(const UpdateParams& p, uint64_t k_base, dim3 grid, dim3 block,
+                    cudaStream_t st) {
+#define ACDC_LAUNCH(L, T) k_pcdm_update_grouped<L, T, G><<<grid, block, 0, st>>>(p, k_base)
+  if (p.fp64) {
+    switch (p.loss) {
+      case ACDC_LOSS_L1_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L1_SQUARE, double); break;
+      case ACDC_LOSS_L2_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L2_SQUARE, double); break;
+      case ACDC_LOSS_SVM_DUAL: ACDC_LAUNCH(ACDC_LOSS_SVM_DUAL, double); break;
+      default: ACDC_LAUNCH(ACDC_LOSS_LOGISTIC, double); break;
+    }
+  } else {
+    switch (p.loss) {
+      case ACDC_LOSS_L1_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L1_SQUARE, float); break;
+      case ACDC_LOSS_L2_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L2_SQUARE, float); break;
+      case ACDC_LOSS_SVM_DUAL: ACDC_LAUNCH(ACDC_LOSS_SVM_DUAL, float); break;
+      default: ACDC_LAUNCH(ACDC_LOSS_LOGISTIC, float); break;
+    }
+  }
+#undef ACDC_LAUNCH
+}
+
 cudaError_t launch_update(const UpdateParams& p, uint64_t k_base, int warps_per_block,
                           cudaStream_t st) {
   if (p.count == 0 || p.n_warps <= 0) return cudaSuccess;
@@ -403,6 +653,25 @@ cudaError_t launch_update(const UpdateParams& p, uint64_t k_base, int warps_per_
   if (warps_per_block > kMaxWarps) warps_per_block = kMaxWarps;
   cudaError_t e = cudaMemsetAsync(p.counters + CNT_WORK, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
+  if (p.lanes == 8 || p.lanes == 16 || p.lanes == 32) {
+    // tau updates in flight, 32 / lanes of them per warp; the warps are spread
+    // over every SM (blocks of fewer warps when there are few of them) so that
+    // the SMs' load/store units and L1 miss queues all take part
+    const int64_t warps = ((int64_t)p.n_warps * p.lanes + 31) / 32;
+    if (p.sm_count > 0) {
+      const int64_t spread = (warps + p.sm_count - 1) / p.sm_count;
+      if (spread < warps_per_block) warps_per_block = (int)(spread > 0 ? spread : 1);
+    }
+    const int64_t blocks = (warps + warps_per_block - 1) / warps_per_block;
+    const dim3 grid((unsigned)blocks), block(warps_per_block * 32);
+    if (p.lanes == 8)
+      launch_grouped<8>(p, k_base, grid, block, st);
+    else if (p.lanes == 16)
+      launch_grouped<16>(p, k_base, grid, block, st);
+    else
+      launch_grouped<32>(p, k_base, grid, block, st);
+    return cudaGetLastError();
+  }
   const int blocks = (p.n_warps + warps_per_block - 1) / warps_per_block;
   dim3 grid(blocks), block(warps_per_block * 32);
 #define ACDC_LAUNCH(L, T) k_pcdm_update<L, T><<<grid, block, 0, st>>>(p, k_base)
@@ -439,14 +708,18 @@ cudaError_t launch_batch_update(const BatchDev& b, int update_blocks, cudaStream
 cudaError_t update_kernels_init() {
   const int carve = cudaSharedmemCarveoutMaxShared;
   const cudaFuncAttribute a = cudaFuncAttributePreferredSharedMemoryCarveout;
-  cudaError_t e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L1_SQUARE, float>, a, carve);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L1_SQUARE, double>, a, carve);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_SVM_DUAL, float>, a, carve);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_SVM_DUAL, double>, a, carve);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L2_SQUARE, float>, a, carve);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_L2_SQUARE, double>, a, carve);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_LOGISTIC, float>, a, carve);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<ACDC_LOSS_LOGISTIC, double>, a, carve);
+  cudaError_t e = cudaSuccess;
+#define ACDC_CARVE(L, T) \
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update<L, T>, a, carve)
+  ACDC_CARVE(ACDC_LOSS_L1_SQUARE, float);
+  ACDC_CARVE(ACDC_LOSS_L1_SQUARE, double);
+  ACDC_CARVE(ACDC_LOSS_SVM_DUAL, float);
+  ACDC_CARVE(ACDC_LOSS_SVM_DUAL, double);
+  ACDC_CARVE(ACDC_LOSS_L2_SQUARE, float);
+  ACDC_CARVE(ACDC_LOSS_L2_SQUARE, double);
+  ACDC_CARVE(ACDC_LOSS_LOGISTIC, float);
+  ACDC_CARVE(ACDC_LOSS_LOGISTIC, double);
+#undef ACDC_CARVE
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_L1_SQUARE, float>, a, carve);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_L1_SQUARE, double>, a, carve);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_SVM_DUAL, float>, a, carve);

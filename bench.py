@@ -91,7 +91,11 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="lasso_m1e6_n1e7_zipf", choices=sorted(WORKLOADS))
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=3,
+                    help="end-to-end solves through the C-ABI from host buffers (mean reported)")
+    ap.add_argument("--lanes", type=int, default=0, choices=[-1, 0, 8, 16, 32],
+                    help="lanes per update of the update kernel (settings.lanes_per_update: "
+                         "8 or 32 grouped, -1 the one-warp ring kernel, 0 by column length)")
     ap.add_argument("--cpu-sample-updates", type=float, default=0,
                     help="updates timed for the CPU baseline (default: one epoch)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -403,6 +407,123 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+OPTIMA = {"lasso_m1e6_n1e7_zipf": os.path.join(GOLDEN, "lasso_m1e6_n1e7_optimum.npz"),
+          "svm_n2e4_d1355191": os.path.join(GOLDEN, "svm_n2e4_d1355191_optimum.npz")}
+
+
+def instance_digest(inst):
+    """SHA-256 of the generated arrays and lambda (the fixtures record it)."""
+    import hashlib
+    import numpy as np
+    h = hashlib.sha256()
+    for a in (inst.col_ptr, inst.row_idx, inst.vals, inst.rhs):
+        h.update(np.ascontiguousarray(a).tobytes())
+    h.update(np.float64(inst.lam).tobytes())
+    return h.hexdigest()
+
+
+def duplicate_classes(inst):
+    """Class id per coordinate: one-entry columns at the same row are the same
+    column up to sign (the generator scales them to +-1), so any split of
+    their mass is optimal; they share one class, keyed by the row.  Every other
+    column is its own class.  Returns (class ids, sign of the one entry or 1)."""
+    import numpy as np
+    lens = np.diff(inst.col_ptr)
+    one = lens == 1
+    cls = np.arange(inst.n, dtype=np.int64) + inst.m
+    first = inst.col_ptr[:-1][one]
+    cls[one] = inst.row_idx[first]
+    sign = np.ones(inst.n)
+    sign[one] = np.sign(inst.vals[first])
+    return cls, sign
+
+
+def class_support(cls, sign, x, idx=None):
+    """Classes whose signed mass is nonzero."""
+    import numpy as np
+    idx = np.nonzero(x)[0] if idx is None else idx
+    vals = x[idx] if len(x) == len(cls) else x
+    mass = {}
+    for c, v in zip(cls[idx].tolist(), (sign[idx] * vals).tolist()):
+        mass[c] = mass.get(c, 0.0) + v
+    return {c for c, v in mass.items() if v != 0.0}
+
+
+def host_objective(inst, x):
+    """FP64 primal objective of x on the generated (FP64) data, on the host:
+    0.5||Ax - b||^2 + lambda||x||_1 for the Lasso; for the SVM dual (x = alpha)
+    lambda/2 ||w||^2 + mean hinge with w = sum_i alpha_i y_i x_i / (lambda n)."""
+    import numpy as np
+    lens = np.diff(inst.col_ptr)
+    if is_svm_inst(inst):
+        coef = x * inst.rhs / (inst.lam * inst.n)
+        w = np.bincount(inst.row_idx, weights=inst.vals * np.repeat(coef, lens), minlength=inst.m)
+        prod = inst.vals * w[inst.row_idx]
+        cs = np.concatenate([[0.0], np.cumsum(prod)])
+        margin = cs[inst.col_ptr[1:]] - cs[inst.col_ptr[:-1]]
+        hinge = np.maximum(0.0, 1.0 - inst.rhs * margin)
+        return float(0.5 * inst.lam * w.dot(w) + hinge.mean())
+    sup = np.nonzero(x)[0]
+    sl = lens[sup]
+    first = np.repeat(inst.col_ptr[sup] - np.concatenate([[0], np.cumsum(sl)[:-1]]), sl)
+    ent = first + np.arange(int(sl.sum()))
+    r = np.bincount(inst.row_idx[ent], weights=inst.vals[ent] * np.repeat(x[sup], sl),
+                    minlength=inst.m) - inst.rhs
+    return float(0.5 * r.dot(r) + inst.lam * np.abs(x).sum())
+
+
+def is_svm_inst(inst):
+    return inst.loss == 2
+
+
+def oracle_error(workload, inst, x, primal):
+    """The solve's error against the committed FP64 optimum of the workload
+    (tests/golden/make_config_optima.py: oracle run to a gap <= 1e-9): relative
+    objective error, support match raw and up to duplicate columns."""
+    import numpy as np
+    path = OPTIMA.get(workload)
+    if not path or not os.path.exists(path):
+        return None
+    f = np.load(path)
+    digest = instance_digest(inst)
+    out = {"fixture": os.path.relpath(path, ROOT), "same_input": digest == str(f["sha256"]),
+           "oracle_objective": float(f["primal"]), "oracle_gap": float(f["gap"]),
+           "oracle_rel_gap": float(f["rel_gap"])}
+    p_o = float(f["primal"])
+    p_h = host_objective(inst, x)
+    out["objective_fp64_host"] = p_h
+    out["objective_device"] = primal
+    out["oracle_rel_err"] = abs(p_h - p_o) / abs(p_o)
+    out["oracle_rel_err_device"] = abs(primal - p_o) / abs(p_o)
+    sup_o = np.asarray(f["support"], np.int64)
+    sup = np.nonzero(x)[0]
+    sym = np.setxor1d(sup, sup_o)
+    out["support"] = int(len(sup))
+    out["oracle_support"] = int(len(sup_o))
+    out["support_symmetric_difference"] = int(len(sym))
+    if "x_support" in f.files:
+        xo = np.zeros(inst.n)
+        xo[sup_o] = f["x_support"]
+        out["max_abs_x_in_difference"] = float(np.abs(np.concatenate([x[sym], xo[sym]])).max()) \
+            if len(sym) else 0.0
+        cls, sign = duplicate_classes(inst)
+        cs = class_support(cls, sign, x, sup)
+        co = class_support(cls, sign, xo, sup_o)
+        out["class_support"] = len(cs)
+        out["oracle_class_support"] = len(co)
+        out["class_symmetric_difference"] = len(cs ^ co)
+        out["support_match"] = cs == co
+        out["support_rule"] = ("same nonzero classes; one-entry columns at one row form one class "
+                               "(the same column up to sign, so the split of their mass is not unique)")
+    else:
+        out["support_match"] = bool(len(sym) == 0)
+        out["support_rule"] = "same nonzero coordinates"
+    if "alpha" in f.files:
+        out["max_abs_alpha_err"] = float(np.abs(x - f["alpha"]).max())
+    return out
+
+
 def load_json(path, default=None):
     try:
         with open(path) as f:
@@ -437,13 +558,13 @@ def settings_for(w):
         return acdc.default_settings(acdc.LOSS_SVM_DUAL, tau=w["tau"], warps_per_block=8,
                                      refresh_every=w["refresh_every"], gap_target=w["gap"],
                                      gap_relative=0, max_epochs=w["max_epochs"], seed=1,
-                                     precision=acdc.PREC_FP32)
+                                     precision=acdc.PREC_FP32, lanes_per_update=w.get("lanes", 0))
     return acdc.default_settings(acdc.LOSS_L1_SQUARE, tau=w["tau"], warps_per_block=8,
                                  refresh_every=w["refresh_every"], gap_target=w["gap"],
                                  gap_relative=1, max_epochs=w["max_epochs"], use_shrinking=1,
                                  shrinking_probability=0.9, shrinking_starting_iter=5, seed=1,
                                  precision=acdc.PREC_FP32, tau_active=w["tau_active"],
-                                 active_passes=w["active_passes"])
+                                 active_passes=w["active_passes"], lanes_per_update=w.get("lanes", 0))
 
 
 def cpu_time_per_epoch(inst, threads, updates):
@@ -544,6 +665,10 @@ def run_ours(args, w):
         dist.barrier()
     clk = clocks.stop()
 
+    # the last timed solve's error against the committed FP64 optimum
+    # (outside the timed region)
+    oracle_cmp = oracle_error(args.workload, inst, p.get_x(), results[-1].eval.primal)
+
     dev_ms = [r.device_ms for r in results]
     ms_per_step = max_over_ranks(dist, statistics.mean(dev_ms), dev)
     value = ms_per_step / 1e3
@@ -592,18 +717,26 @@ def run_ours(args, w):
     # e2e: the same metric through the C-ABI from pinned host buffers.
     h2d = inst.col_ptr.nbytes + inst.row_idx.nbytes + inst.vals.nbytes + inst.rhs.nbytes
     d2h = inst.n * 8
-    e2e_times = []
+    # One untimed pass first (pool growth, module load), then e2e_steps timed
+    # passes, each split into create (upload + device layout), solve and
+    # readback (x to host) on the host clock.
+    e2e_times, e2e_parts = [], []
     x_last = None
     for i in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         torch.cuda.synchronize()
         t = time.perf_counter()
         q = acdc.Problem(ctx, inst, s)
+        q.synchronize()
+        t_create = time.perf_counter()
         rq = q.solve()
+        t_solve = time.perf_counter()
         x_last = q.get_x()
         q.close()
         torch.cuda.synchronize()
+        t_end = time.perf_counter()
         if i > 0:
-            e2e_times.append(time.perf_counter() - t)
+            e2e_times.append(t_end - t)
+            e2e_parts.append((t_create - t, t_solve - t_create, t_end - t_solve, rq.epochs))
     e2e_value = max_over_ranks(dist, statistics.mean(e2e_times), dev) if e2e_times else None
 
     cpu = None
@@ -651,6 +784,7 @@ def run_ours(args, w):
             "config": dict(solver_keys, **{
                        "workload": args.workload, "m": w["m"], "n": w["n"], "nnz": inst.nnz,
                        "tau": w["tau"], "refresh_every": w["refresh_every"],
+                       "lanes_per_update": s.lanes_per_update,
                        "precision": "fp32 bulk; fp64 refresh, gap and hot-column polish",
                        "updates": int(updates), "update_launches": int(launches),
                        "updates_per_s": updates / (upd_ms * 1e-3) if upd_ms > 0 else None,
@@ -660,11 +794,18 @@ def run_ours(args, w):
                        "fp64_epochs": [r.fp64_epochs for r in results],
                        "converged": converged, "final_rel_gap": [r.eval.rel_gap for r in results],
                        "objective": results[-1].eval.primal, "support": results[-1].eval.support,
+                       "oracle_rel_err": oracle_cmp["oracle_rel_err"] if oracle_cmp else None,
+                       "support_match": oracle_cmp["support_match"] if oracle_cmp else None,
+                       "oracle": oracle_cmp,
                        "host_wall_s": wall / args.steps, "generate_s": t_gen}),
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h)},
+                    "d2h_bytes_per_step": int(d2h), "solves": len(e2e_times),
+                    "create_s": [round(x[0], 4) for x in e2e_parts],
+                    "solve_s": [round(x[1], 4) for x in e2e_parts],
+                    "readback_s": [round(x[2], 4) for x in e2e_parts],
+                    "epochs": [x[3] for x in e2e_parts]},
             "gpu_launches": int(gpu_launches),
             "clocks": clk,
             "batched": batched,
@@ -685,6 +826,7 @@ def main():
     w = dict(WORKLOADS[args.workload], name=args.workload)
     if args.active_passes > 0 and "active_passes" in w:
         w["active_passes"] = args.active_passes
+    w["lanes"] = args.lanes
     if args.probe_launches:
         return probe_launches(w)
     if args.max_epochs > 0:

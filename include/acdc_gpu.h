@@ -121,7 +121,13 @@ typedef struct acdc_settings {
                                      this many passes (|A|/q updates each) of the
                                      q-shrinking draws in FP64, tau_active in
                                      flight; 0 = none, default 2                  */
-  int32_t reserved2;
+  int32_t lanes_per_update;       /* update kernel: 0 (default) or -1 = one warp
+                                     per update with a shared-memory copy ring;
+                                     8, 16 or 32 = the grouped kernel, in which
+                                     that many lanes perform one update (32/lanes
+                                     updates per warp) with records and entries
+                                     prefetched into registers.  tau counts the
+                                     updates in flight either way.                */
 } acdc_settings;
 
 /* precision: FP32 x and residual with FP64 refresh and gap (FP32), the same
@@ -203,6 +209,11 @@ void acdc_settings_default(acdc_settings* s);
 int acdc_settings_check(const acdc_settings* s);
 int acdc_ctx_create(int device, acdc_ctx** out);
 int acdc_ctx_destroy(acdc_ctx* ctx);
+/* Device memory of the context's pool (every problem, staging buffer and
+ * table of the context comes from it): bytes the pool holds from the driver,
+ * and bytes handed out now.  No reference counterpart: the reference engine
+ * has no device memory. */
+int acdc_ctx_memory(acdc_ctx* ctx, int64_t* reserved, int64_t* used);
 const char* acdc_last_error(const acdc_ctx* ctx);
 const char* acdc_status_string(int status);
 

@@ -235,6 +235,213 @@ int64_t orc_lasso_solve_shrink(int64_t m, int64_t n, const int64_t* col_ptr,
   return epochs;
 }
 
+/* Working-set solve for the fixtures of the large configurations: it finds the
+ * optimum to a certified gap; it does not follow a sampler trajectory.  The
+ * coordinate step is the reference's serial update with the exact Lipschitz
+ * constant (MulticoreL1RegSquareLoss.h:41-63, MulticoreSquareLoss.h:27-40 with
+ * beta = 1), applied in cyclic sweeps over the working set
+ * W = {j : x_j != 0 or |a_j^T r| > (1 - eps) lambda}.  Each check recomputes
+ * r = A x - b exactly (MulticoreSquareLoss.h:42-53), takes a_j^T r over every
+ * column (OpenMP over `threads`, read-only), evaluates the gap as
+ * orc_lasso_eval does and rebuilds W in column order.  `sweeps` sweeps run
+ * between checks; the solve stops when the (relative if rel) gap is <= target
+ * or after max_checks checks.  With anderson = K > 1 (at most 16), every K + 1
+ * sweeps are followed by an Anderson extrapolation step.  Returns the sweeps
+ * made; *checks_out gets the checks. */
+int64_t orc_lasso_solve_ws(int64_t m, int64_t n, const int64_t* col_ptr, const int32_t* row_idx,
+                           const double* vals, const double* b, double lambda, double target,
+                           int rel, int64_t max_checks, int64_t sweeps, double eps, int threads,
+                           int anderson, double* x, double* r, double* out, int64_t* checks_out) {
+  double* g = (double*)malloc(sizeof(double) * (size_t)n);
+  const int K = anderson > 1 ? (anderson < 16 ? anderson : 16) : 0;
+  double* snap = NULL;     /* K + 1 snapshots of x over the working set */
+  double* xe = NULL;       /* extrapolated x over the working set */
+  double* re = K ? (double*)malloc(sizeof(double) * (size_t)m) : NULL;
+  int64_t snap_cap = 0;
+  int32_t* ws = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+  int64_t* wptr = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n + 1));
+  int32_t* wrow = NULL;
+  double* wval = NULL;
+  double* wli = (double*)malloc(sizeof(double) * (size_t)n);
+  int64_t wcap = 0, total_sweeps = 0, checks = 0;
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#else
+  (void)threads;
+#endif
+  for (;;) {
+    orc_lasso_residuals(m, n, col_ptr, row_idx, vals, b, x, r);
+    double rr = 0, br = 0, l1 = 0, gmax = 0;
+    int64_t support = 0;
+#pragma omp parallel for schedule(static) reduction(+ : rr, br)
+    for (int64_t i = 0; i < m; ++i) {
+      rr += r[i] * r[i];
+      br += b[i] * r[i];
+    }
+#pragma omp parallel for schedule(dynamic, 4096) reduction(+ : l1, support) reduction(max : gmax)
+    for (int64_t j = 0; j < n; ++j) {
+      double s = 0;
+      for (int64_t e = col_ptr[j]; e < col_ptr[j + 1]; ++e) s += vals[e] * r[row_idx[e]];
+      g[j] = s;
+      s = fabs(s);
+      if (s > gmax) gmax = s;
+      l1 += fabs(x[j]);
+      support += x[j] != 0;
+    }
+    const double P = 0.5 * rr + lambda * l1;
+    const double sc = (gmax > lambda) ? lambda / gmax : 1.0;
+    const double D = -sc * br - 0.5 * sc * sc * rr;
+    out[0] = P;
+    out[1] = D;
+    out[2] = P - D;
+    out[3] = (P - D) / (fabs(P) > 1 ? fabs(P) : 1);
+    out[4] = 0;
+    out[5] = l1;
+    out[6] = rr;
+    out[7] = gmax;
+    out[8] = (double)support;
+    checks++;
+    if ((rel ? out[3] : out[2]) <= target || checks >= max_checks) break;
+    /* working set in column order, packed for the sweeps */
+    int64_t nw = 0, entries = 0;
+    for (int64_t j = 0; j < n; ++j)
+      if (x[j] != 0 || fabs(g[j]) > (1 - eps) * lambda) {
+        ws[nw++] = (int32_t)j;
+        entries += col_ptr[j + 1] - col_ptr[j];
+      }
+    if (entries > wcap) {
+      free(wrow);
+      free(wval);
+      wcap = entries;
+      wrow = (int32_t*)malloc(sizeof(int32_t) * (size_t)(wcap > 0 ? wcap : 1));
+      wval = (double*)malloc(sizeof(double) * (size_t)(wcap > 0 ? wcap : 1));
+    }
+    wptr[0] = 0;
+    for (int64_t t = 0; t < nw; ++t) {
+      const int64_t j = ws[t];
+      int64_t o = wptr[t];
+      double s = 0;
+      for (int64_t e = col_ptr[j]; e < col_ptr[j + 1]; ++e, ++o) {
+        wrow[o] = row_idx[e];
+        wval[o] = vals[e];
+        s += vals[e] * vals[e];
+      }
+      wptr[t + 1] = o;
+      wli[t] = s > 0 ? 1 / s : 0;
+    }
+    if (K && nw * (K + 1) > snap_cap) {
+      free(snap);
+      free(xe);
+      snap_cap = nw * (K + 1);
+      snap = (double*)malloc(sizeof(double) * (size_t)snap_cap);
+      xe = (double*)malloc(sizeof(double) * (size_t)(nw > 0 ? nw : 1));
+    }
+    for (int64_t sw = 0; sw < sweeps; ++sw) {
+      for (int64_t t = 0; t < nw; ++t) {
+        const int64_t j = ws[t];
+        double tmp = 0;
+        for (int64_t e = wptr[t]; e < wptr[t + 1]; ++e) tmp += wval[e] * r[wrow[e]];
+        tmp = soft_threshold(wli[t] * lambda, x[j] - wli[t] * tmp) - x[j];
+        if (tmp == 0) continue;
+        x[j] = x[j] + tmp;
+        for (int64_t e = wptr[t]; e < wptr[t + 1]; ++e) r[wrow[e]] = r[wrow[e]] + tmp * wval[e];
+      }
+      if (!K || nw == 0) continue;
+      /* Anderson extrapolation of the sweeps (Bertrand and Massias, "Anderson
+       * acceleration of coordinate descent", AISTATS 2021): after K + 1
+       * snapshots, the combination of the last K iterates whose weights
+       * (summing to 1) minimise the norm of the combined differences, kept
+       * only if it lowers the objective. */
+      const int slot = (int)(sw % (K + 1));
+      for (int64_t t = 0; t < nw; ++t) snap[(size_t)slot * nw + t] = x[ws[t]];
+      if (slot != K) continue;
+      double G[16 * 16], z[16];
+      for (int a = 0; a < K; ++a)
+        for (int c = 0; c <= a; ++c) {
+          double acc = 0;
+          const double* ua1 = snap + (size_t)(a + 1) * nw;
+          const double* ua0 = snap + (size_t)a * nw;
+          const double* uc1 = snap + (size_t)(c + 1) * nw;
+          const double* uc0 = snap + (size_t)c * nw;
+          for (int64_t t = 0; t < nw; ++t) acc += (ua1[t] - ua0[t]) * (uc1[t] - uc0[t]);
+          G[a * K + c] = G[c * K + a] = acc;
+        }
+      double tr = 0;
+      for (int a = 0; a < K; ++a) tr += G[a * K + a];
+      if (!(tr > 0)) continue;
+      for (int a = 0; a < K; ++a) {
+        G[a * K + a] += 1e-12 * tr;
+        z[a] = 1;
+      }
+      /* Cholesky solve of G z = 1 */
+      int ok = 1;
+      for (int a = 0; a < K && ok; ++a) {
+        double d = G[a * K + a];
+        for (int c = 0; c < a; ++c) d -= G[a * K + c] * G[a * K + c];
+        if (!(d > 0)) {
+          ok = 0;
+          break;
+        }
+        G[a * K + a] = sqrt(d);
+        for (int e = a + 1; e < K; ++e) {
+          double v = G[e * K + a];
+          for (int c = 0; c < a; ++c) v -= G[e * K + c] * G[a * K + c];
+          G[e * K + a] = v / G[a * K + a];
+        }
+      }
+      if (!ok) continue;
+      for (int a = 0; a < K; ++a) {
+        double v = z[a];
+        for (int c = 0; c < a; ++c) v -= G[a * K + c] * z[c];
+        z[a] = v / G[a * K + a];
+      }
+      for (int a = K - 1; a >= 0; --a) {
+        double v = z[a];
+        for (int c = a + 1; c < K; ++c) v -= G[c * K + a] * z[c];
+        z[a] = v / G[a * K + a];
+      }
+      double zs = 0;
+      for (int a = 0; a < K; ++a) zs += z[a];
+      if (!(fabs(zs) > 0)) continue;
+      double l1_cur = 0, l1_e = 0;
+      for (int64_t t = 0; t < nw; ++t) {
+        double v = 0;
+        for (int a = 0; a < K; ++a) v += z[a] / zs * snap[(size_t)(a + 1) * nw + t];
+        xe[t] = v;
+        l1_cur += fabs(x[ws[t]]);
+        l1_e += fabs(v);
+      }
+      memcpy(re, r, sizeof(double) * (size_t)m);
+      for (int64_t t = 0; t < nw; ++t) {
+        const double dlt = xe[t] - x[ws[t]];
+        if (dlt == 0) continue;
+        for (int64_t e = wptr[t]; e < wptr[t + 1]; ++e) re[wrow[e]] += dlt * wval[e];
+      }
+      double rr_cur = 0, rr_e = 0;
+      for (int64_t i = 0; i < m; ++i) {
+        rr_cur += r[i] * r[i];
+        rr_e += re[i] * re[i];
+      }
+      if (0.5 * rr_e + lambda * l1_e < 0.5 * rr_cur + lambda * l1_cur) {
+        for (int64_t t = 0; t < nw; ++t) x[ws[t]] = xe[t];
+        memcpy(r, re, sizeof(double) * (size_t)m);
+      }
+    }
+    total_sweeps += sweeps;
+  }
+  free(g);
+  free(ws);
+  free(wptr);
+  free(wrow);
+  free(wval);
+  free(wli);
+  free(snap);
+  free(xe);
+  free(re);
+  if (checks_out) *checks_out = checks;
+  return total_sweeps;
+}
+
 /* ---- L2-regularised square loss (lossFunction 1) and L2-regularised
  *      logistic loss (lossFunction 3): the "smooth" losses ---- */
 

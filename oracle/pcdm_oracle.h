@@ -66,6 +66,17 @@ int64_t orc_lasso_solve_shrink(int64_t m, int64_t n, const int64_t* col_ptr,
                                int64_t start_epoch, double step_scale, double* x, double* r,
                                double* out, double* gap_trace);
 
+/* Working-set solve for fixtures of large instances (the optimum, not a
+ * sampler trajectory): cyclic sweeps of the reference's exact-step update over
+ * W = {j : x_j != 0 or |a_j^T r| > (1 - eps) lambda}, `sweeps` of them between
+ * checks; every check refreshes r exactly, evaluates the gap over all columns
+ * (OpenMP, threads) and rebuilds W; anderson = K > 1 adds an Anderson
+ * extrapolation after every K + 1 sweeps.  Returns the sweeps made. */
+int64_t orc_lasso_solve_ws(int64_t m, int64_t n, const int64_t* col_ptr, const int32_t* row_idx,
+                           const double* vals, const double* b, double lambda, double target,
+                           int rel, int64_t max_checks, int64_t sweeps, double eps, int threads,
+                           int anderson, double* x, double* r, double* out, int64_t* checks_out);
+
 /* ---- losses 1 (L2-regularised square) and 3 (L2-regularised logistic); the
  *      matrix is CSC over coordinates, m = residual entries (samples for 3) ---- */
 #define ORC_LOSS_RIDGE 1
