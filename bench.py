@@ -79,11 +79,6 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "k_pcdm_update_traffic.json")
 
 
-def epochs_file(workload):
-    """Epochs-to-gap measured by the GPU solver on a workload (written from bench runs)."""
-    return os.path.join(ROOT, "profiles", workload + "_epochs.json")
-
-
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -96,8 +91,10 @@ def parse_args():
     ap.add_argument("--lanes", type=int, default=0, choices=[-1, 0, 8, 16, 32],
                     help="lanes per update of the update kernel (settings.lanes_per_update: "
                          "8 or 32 grouped, -1 the one-warp ring kernel, 0 by column length)")
-    ap.add_argument("--cpu-sample-updates", type=float, default=0,
-                    help="updates timed for the CPU baseline (default: one epoch)")
+    ap.add_argument("--cpu-budget", type=float, default=20.0,
+                    help="seconds of computation for the CPU baseline run of the workload")
+    ap.add_argument("--ref-step-seconds", type=float, default=0,
+                    help="--impl reference: computation seconds per step (0 = 120 / steps, at least 2)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--max-epochs", type=int, default=0,
                     help="cap each solve (profiling runs; the line then reports converged=false)")
@@ -567,55 +564,124 @@ def settings_for(w):
                                  active_passes=w["active_passes"], lanes_per_update=w.get("lanes", 0))
 
 
-def cpu_time_per_epoch(inst, threads, updates):
-    """The reference's asynchronous multicore engine, restated (oracle port), timed
-    on the host cores for a bounded number of updates from x = 0."""
+def cpu_engine(inst):
+    """The reference's multicore engine restated (oracle port) on an instance:
+    the Lasso (MulticoreL1RegSquareLoss) or the SVM dual (MulticoreSVMDualLoss)
+    with the reference's own Lipschitz constants, from x = 0."""
     sys.path.insert(0, ORACLE)
     import oracle
     import acdc
     if inst.loss == acdc.LOSS_SVM_DUAL:
-        L = oracle.SVM(inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals, inst.rhs, inst.lam)
-    else:
-        L = oracle.Lasso(inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals, inst.rhs, inst.lam)
-    secs = L.hogwild(updates, 1, threads)
-    return secs * inst.n / updates, secs
+        return oracle.SVM(inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals, inst.rhs, inst.lam)
+    return oracle.Lasso(inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals, inst.rhs, inst.lam)
+
+
+def cpu_time_to_gap(inst, threads, target, rel, budget_s, bulk_epochs=1, engine=None, eval_every=1):
+    """Measured time-to-gap of the reference's algorithm on the host cores: the
+    asynchronous multicore engine (OpenMP over updates, CAS-loop atomics,
+    uniform sampling; the serial engine when threads = 1) runs bulks of
+    bulk_epochs epochs; after a bulk the residual is recomputed and the FP64
+    duality gap evaluated, outside the timed computation, as the reference's
+    Solver loop times only its bulks (cpp/src/solver/Solver.h:43-65).
+    Evaluations follow every eval_every bulks while they cost at most a
+    quarter of the computation (every bulk on small instances), and always at
+    the end of the budget.  Stops at the gap target or once the computation
+    time reaches budget_s.  Returns the computation seconds, epochs, the last
+    gap and whether the target was reached (if not, the seconds are a lower
+    bound on the time-to-gap)."""
+    L = engine if engine is not None else cpu_engine(inst)
+    secs, epochs, bulks, eval_s = 0.0, 0, 0, 0.0
+    gap = None
+    trace = []
+    while True:
+        count = int(bulk_epochs * inst.n)
+        if threads == 1:
+            t = time.perf_counter()
+            L.updates(count, 1)
+            secs += time.perf_counter() - t
+        else:
+            secs += L.hogwild(count, 1, threads)
+        epochs += bulk_epochs
+        bulks += 1
+        if (bulks % eval_every == 0 and eval_s <= 0.25 * secs) or secs >= budget_s:
+            t = time.perf_counter()
+            L.refresh()
+            ev = L.evaluate(threads)
+            eval_s += time.perf_counter() - t
+            gap = ev["rel_gap"] if rel else ev["gap"]
+            trace.append((round(secs, 3), epochs, gap))
+            if gap <= target or secs >= budget_s:
+                break
+    return {"seconds": secs, "epochs": epochs, "gap": gap, "reached": bool(gap <= target),
+            "updates_per_s": epochs * inst.n / secs if secs > 0 else None, "threads": threads,
+            "trace": trace[-8:]}
+
+
+def cpu_config0(threads):
+    """The reference's CPU case (2,000 x 10,000, 20 per column, FP64, absolute
+    gap 1e-6), run to the gap by the serial engine and by the OpenMP engine."""
+    w0 = dict(WORKLOADS["lasso_m2e3_n1e4"])
+    inst0 = generate(w0, pinned=False)
+    out = {"workload": "lasso_m2e3_n1e4", "gap_target_absolute": 1e-6}
+    out["serial"] = cpu_time_to_gap(inst0, 1, 1e-6, False, 60.0)
+    out["openmp"] = cpu_time_to_gap(inst0, threads, 1e-6, False, 60.0)
+    for k in ("serial", "openmp"):
+        out[k].pop("trace", None)
+    return out
 
 
 def run_reference(args, w):
-    """--impl reference: the reference's CPU algorithm on all host cores."""
+    """--impl reference: the reference's algorithm (its asynchronous multicore
+    engine restated in the oracle; the x86 build of the reference itself does
+    not run on an Arm host) on all host cores, on the same workload.  The solve
+    starts from x = 0 and each timed step continues it for a bounded time;
+    value is the computation time to the gap target, or, when the target is not
+    reached within the steps, the total computation time with reached = false
+    (a measured lower bound, never an extrapolation)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
     inst = generate(w, pinned=False)
-    upd = int(args.cpu_sample_updates) if args.cpu_sample_updates > 0 else inst.n
-    rec = load_json(epochs_file(args.workload), {})
-    epochs = rec.get("epochs_to_gap")
-    samples = []
-    for i in range(args.warmup + args.steps):
-        per_epoch, secs = cpu_time_per_epoch(inst, threads, upd)
-        if i >= args.warmup:
-            samples.append(per_epoch)
-    per_epoch = statistics.mean(samples)
-    if not epochs:
-        print(json.dumps({"impl": "reference", "unavailable":
-                          "epochs-to-gap record missing (profiles/%s)"
-                          % os.path.basename(epochs_file(args.workload))}))
-        return 0
-    value = per_epoch * epochs
-    sample = ("%d updates (%.2f epochs) of the asynchronous multicore engine from x=0 per step, "
-              "%d threads; time-to-gap = s/epoch x %d epochs (the epochs the GPU solver needs "
-              "with q-shrinking; the reference samples uniformly, so this is a lower bound)"
-              % (upd, upd / inst.n, threads, epochs))
+    rel = not is_svm(w)
+    step_s = args.ref_step_seconds if args.ref_step_seconds > 0 else max(2.0, 120.0 / args.steps)
+    # warm-up: short solves from x = 0 (page-in, thread pool), discarded
+    for _ in range(args.warmup):
+        cpu_time_to_gap(inst, threads, w["gap"], rel, 0.2)
+    engine = cpu_engine(inst)
+    total, epochs, gap, steps_run, trace = 0.0, 0, None, 0, []
+    reached = False
+    for _ in range(args.steps):
+        r = cpu_time_to_gap(inst, threads, w["gap"], rel, step_s, engine=engine)
+        total += r["seconds"]
+        epochs += r["epochs"]
+        gap = r["gap"]
+        steps_run += 1
+        trace.append((round(total, 2), epochs, gap))
+        if r["reached"]:
+            reached = True
+            break
+    c0 = cpu_config0(threads)
+    value = total
+    sample = ("the reference's asynchronous multicore engine (oracle port, uniform sampling, "
+              "CAS atomics) on %d threads from x = 0, continued over %d steps of up to %.1f s of "
+              "computation each, FP64 gap evaluated outside the timing; %s"
+              % (threads, steps_run, step_s,
+                 "target reached" if reached else
+                 "target not reached: value is a measured lower bound (gap %.3g after %.0f s)"
+                 % (gap, total)))
     line = {"metric": METRICS[w.get("loss", "lasso")], "value": value, "unit": "s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3 / max(1, steps_run),
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded %s generator)" % ("SVM" if is_svm(w) else "Zipf Lasso"),
             "impl": "reference",
             "config": {"workload": args.workload, "m": w["m"], "n": w["n"], "nnz": inst.nnz,
-                       "threads": threads, "seconds_per_epoch": per_epoch},
+                       "threads": threads, "gap_target": w["gap"], "gap_relative": rel,
+                       "reached": reached, "gap_reached": gap, "epochs": epochs,
+                       "updates_per_s": epochs * inst.n / total if total > 0 else None,
+                       "trace": trace, "config0_time_to_gap": c0},
             "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
-                             "sample": sample},
+                             "lower_bound": not reached, "sample": sample},
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -741,21 +807,22 @@ def run_ours(args, w):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
+        # measured, bounded: the reference's algorithm on the same workload
+        # from x = 0 for at most cpu_budget seconds of computation
         threads = os.cpu_count() or 1
-        upd = int(args.cpu_sample_updates) if args.cpu_sample_updates > 0 else inst.n
-        per_epoch, secs = cpu_time_per_epoch(inst, threads, upd)
-        ep = statistics.mean(epochs)
-        cpu = {"value": per_epoch * ep, "unit": "s", "cores": threads, "kind": "port",
-               "sample": ("%d updates of the asynchronous multicore engine (oracle port) from x=0 "
-                          "in %.2f s on %d threads; scaled to %.0f epochs, the epochs the GPU "
-                          "solve needed (the reference samples uniformly: a lower bound)"
-                          % (upd, secs, threads, ep))}
-        # the serial path (one thread, the reference's -t 1) on a smaller sample
-        upd1 = max(1, min(upd, 2_000_000))
-        per_epoch1, secs1 = cpu_time_per_epoch(inst, 1, upd1)
-        cpu["serial"] = {"value": per_epoch1 * ep, "unit": "s", "cores": 1,
-                         "sample": "%d updates on 1 thread in %.2f s, scaled the same way"
-                                   % (upd1, secs1)}
+        rel = not is_svm(w)
+        run = cpu_time_to_gap(inst, threads, w["gap"], rel, args.cpu_budget)
+        cpu = {"value": run["seconds"], "unit": "s", "cores": threads, "kind": "port",
+               "lower_bound": not run["reached"], "gap_reached": run["gap"],
+               "epochs": run["epochs"], "updates_per_s": run["updates_per_s"],
+               "sample": ("the reference's asynchronous multicore engine (oracle port, uniform "
+                          "sampling) on %d threads from x = 0 for up to %.0f s of computation: "
+                          "%s" % (threads, args.cpu_budget,
+                                  "reached the target" if run["reached"] else
+                                  "gap %.3g after %d epochs, so its time-to-gap exceeds %.1f s "
+                                  "(measured lower bound)" % (run["gap"], run["epochs"],
+                                                              run["seconds"])))}
+        cpu["config0_time_to_gap"] = cpu_config0(threads)
 
     p.close()
     batched = serving = None

@@ -1,7 +1,7 @@
 """Writes the FP64 optima of the two large benchmark workloads (TEST
 INFRASTRUCTURE: the oracle, run on the CPU; nothing here runs on a GPU).
 
-    python tests/golden/make_config_optima.py [lasso] [svm]
+    python tests/golden/make_config_optima.py [lasso] [svm] [--resume x.npy]
 
 lasso_m1e6_n1e7_optimum.npz
     The 1,000,000 x 10,000,000 Zipf Lasso (about 2.0e8 nonzeros), generated by
@@ -54,13 +54,19 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
-def lasso(target=1e-9, sweeps=400, eps=0.02, anderson=5):
+def lasso(target=1e-9, sweeps=500, eps=0.05, anderson=5, resume=None):
+    """resume: a .npy file where x is saved after every block of checks; an
+    existing one (for the same input) is the start point, so an interrupted
+    run continues instead of starting over."""
     w = dict(bench.WORKLOADS[LASSO_WORKLOAD])
     t0 = time.time()
     inst = bench.generate(w, pinned=False)
     digest = instance_hash(inst)
     log("generated", inst.m, inst.n, inst.nnz, "lambda", inst.lam, digest, "%.1fs" % (time.time() - t0))
     x = None
+    if resume and os.path.exists(resume):
+        x = np.load(resume)
+        log("resuming from", resume)
     total_sweeps = checks = 0
     t1 = time.time()
     while True:
@@ -72,6 +78,9 @@ def lasso(target=1e-9, sweeps=400, eps=0.02, anderson=5):
         checks += ch
         log("sweeps %d checks %d rel_gap %.3e support %d  %.0fs" %
             (total_sweeps, checks, ev["rel_gap"], ev["support"], time.time() - t1))
+        if resume:
+            np.save(resume + ".tmp.npy", x)
+            os.replace(resume + ".tmp.npy", resume)
         if ev["rel_gap"] <= target:
             break
     sup = np.nonzero(x)[0].astype(np.int64)
@@ -102,12 +111,17 @@ def svm(target=1e-9):
 
 
 def main(argv):
+    resume = None
+    if "--resume" in argv:
+        i = argv.index("--resume")
+        resume = argv[i + 1]
+        argv = argv[:i] + argv[i + 2:]
     which = argv or ["lasso", "svm"]
     oracle.build()
     if "svm" in which:
         svm()
     if "lasso" in which:
-        lasso()
+        lasso(resume=resume)
 
 
 if __name__ == "__main__":
