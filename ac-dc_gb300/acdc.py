@@ -32,7 +32,8 @@ class Settings(C.Structure):
                 ("shrinking_probability", D), ("shrink_eps", D), ("precision", I32),
                 ("tau_active", I32), ("polish_rel_gap", D), ("active_passes", I32),
                 ("screened_eval", I32), ("polish_stall_epochs", I32), ("hot_polish_sweeps", I32),
-                ("hot_threshold", D), ("polish_active_passes", I32), ("lanes_per_update", I32)]
+                ("hot_threshold", D), ("polish_active_passes", I32), ("lanes_per_update", I32),
+                ("minibatch", I32), ("reserved3", I32)]
 
 
 class Eval(C.Structure):
@@ -180,6 +181,7 @@ def gpu_lib():
         L.acdc_debug_sample.argtypes = [VP, U64, U64, U64, I64, VP]
         L.acdc_test_accuracy.argtypes = [VP, I64, VP, VP, VP, VP, C.POINTER(D)]
         L.acdc_debug_sample_noalloc.argtypes = [VP, U64, U64, U64, I64, VP]
+        L.acdc_debug_tau_nice.argtypes = [VP, U64, U64, I64, I32, I32, VP, C.POINTER(U64)]
         L.acdc_server_get_stats.argtypes = [VP, C.c_void_p]
         L.acdc_server_cancel.argtypes = [VP, I64]
         L.acdc_batch_solve_path.argtypes = [VP, I32, VP, VP, C.POINTER(BatchOptions), VP, VP]
@@ -454,6 +456,14 @@ def debug_sample(ctx, seed, k0, count, n):
     out = np.zeros(count, np.int64)
     ctx.check(ctx.L.acdc_debug_sample(ctx.h, seed, k0, count, n, _ptr(out)))
     return out
+
+
+def debug_tau_nice(ctx, seed, k0, n, tau, steps):
+    """acdc_debug_tau_nice: the mini-batch draws (steps x tau) and the next counter."""
+    out = np.zeros((max(steps, 1), tau), np.int32)[:steps]
+    k = U64(0)
+    ctx.check(ctx.L.acdc_debug_tau_nice(ctx.h, seed, k0, n, tau, steps, _ptr(out), C.byref(k)))
+    return out, int(k.value)
 
 
 NOALLOC_MAX_SAMPLES = 65536  # ACDC_NOALLOC_MAX_SAMPLES

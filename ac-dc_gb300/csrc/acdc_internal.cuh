@@ -50,6 +50,7 @@ enum {
   CNT_COLSQ_BITS = 11, // max ||a_j||^2 as FP64 bits
   CNT_HOT = 12,        // hot-set length
   CNT_OMEGA_HOT = 13,  // max entries per residual row over the hot columns
+  CNT_MB_COUNTER = 14, // sampler counter of the synchronous mini-batch draws
   CNT_SLOTS = 16
 };
 
@@ -201,6 +202,11 @@ struct DevProblem {
   float* viol = nullptr;    // n floats: KKT violation of active[t] (Lasso)
   int32_t* hot = nullptr;   // n ints: hot list (Lasso)
   uint8_t* row_flag = nullptr;  // m bytes: rows of the hot columns (Lasso)
+  // synchronous mini-batch (SVM dual): one epoch of draws, the step's deltas,
+  // the n-bit draw marks (allocated on first use)
+  int32_t* mb_draws = nullptr;
+  double* mb_delta = nullptr;
+  uint32_t* mb_mark = nullptr;
   double* part = nullptr;
   double* eval_out = nullptr;
   unsigned long long* counters = nullptr;
@@ -232,6 +238,16 @@ struct acdc_problem {
   double beta = 1;
   int64_t omega = 1;
   uint64_t k_next = 0;      // sampler counter of the next update
+  // synchronous mini-batch: updates made in that mode and the tau its buffers
+  // were sized for (the sampler counter itself lives in counters[CNT_MB_COUNTER])
+  uint64_t mb_updates = 0;
+  int32_t mb_tau = 0;
+  // one mini-batch epoch as a CUDA graph, with the precision, lambda and seed
+  // it was captured for
+  cudaGraphExec_t mb_graph = nullptr;
+  bool mb_graph_fp64 = false;
+  double mb_graph_lambda = 0;
+  uint64_t mb_graph_seed = 0;
   int64_t epochs_done = 0;  // epochs since the start (shrinking starts after a few)
   uint64_t updates_done = 0;
   bool active_valid = false;
@@ -333,6 +349,15 @@ cudaError_t launch_rows_to_columns(const int64_t* row_ptr, int32_t* col, double*
                                    int64_t n, int64_t nnz, char* scratch, int64_t* col_ptr,
                                    int32_t* rows_out, double* vals_out,
                                    unsigned long long* status, cudaStream_t st);
+// Synchronous mini-batch SDCA (hinge dual): `steps` steps of tau distinct
+// draws from the sampler stream at *counter into S (steps x tau), with the n-bit
+// scratch `mark` clear on entry and exit; and one step: deltas from the same w
+// into delta (tau values of the update precision), then applied.
+cudaError_t launch_tau_nice(uint64_t seed, int64_t n, int32_t tau, int32_t steps,
+                            unsigned long long* counter, int32_t* S, uint32_t* mark,
+                            cudaStream_t st);
+cudaError_t launch_minibatch_step(const UpdateParams& p, const int32_t* S, int32_t tau, void* delta,
+                                  cudaStream_t st);
 cudaError_t launch_debug_sample(uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
                                 int64_t* out, cudaStream_t st);
 // Batched round: update, refresh, gap and control kernels over every live slot.

@@ -89,6 +89,7 @@ const char* settings_fault(const acdc_settings* s) {
   if (s->lanes_per_update != 0 && s->lanes_per_update != -1 && s->lanes_per_update != 8 &&
       s->lanes_per_update != 16 && s->lanes_per_update != 32)
     return "lanes_per_update";
+  if (s->minibatch != 0 && (s->minibatch != 1 || s->loss != ACDC_LOSS_SVM_DUAL)) return "minibatch";
   return nullptr;
 }
 
@@ -218,6 +219,9 @@ void free_problem_buffers(acdc_ctx* ctx, DevProblem& d) {
   acdc_dev_free(ctx, d.viol);
   acdc_dev_free(ctx, d.hot);
   acdc_dev_free(ctx, d.row_flag);
+  acdc_dev_free(ctx, d.mb_draws);
+  acdc_dev_free(ctx, d.mb_delta);
+  acdc_dev_free(ctx, d.mb_mark);
   acdc_dev_free(ctx, d.part);
   acdc_dev_free(ctx, d.eval_out);
   acdc_dev_free(ctx, d.counters);
@@ -356,8 +360,10 @@ int apply_settings(acdc_problem* p, const acdc_settings* s) {
   if (const char* bad = settings_fault(s))
     return acdc_set_error(ctx, ACDC_EINVAL, std::string("invalid settings value: ") + bad);
   p->s = *s;
-  // q-shrinking and its screened evaluations cover losses 0 and 2 only.
-  if (p->loss == ACDC_LOSS_L2_SQUARE || p->loss == ACDC_LOSS_LOGISTIC) p->s.use_shrinking = 0;
+  // q-shrinking and its screened evaluations cover losses 0 and 2 only, and
+  // the asynchronous draws only.
+  if (p->loss == ACDC_LOSS_L2_SQUARE || p->loss == ACDC_LOSS_LOGISTIC || p->s.minibatch)
+    p->s.use_shrinking = 0;
   p->screen_valid = false;
   const double n = (double)p->d.n;
   if (s->sigma > 0)
@@ -608,6 +614,7 @@ extern "C" int acdc_problem_destroy(acdc_problem* p) {
   cudaSetDevice(ctx->device);
   // copies into the problem's pinned slot must land before the slot is reused
   cudaStreamSynchronize(ctx->stream);
+  if (p->mb_graph) cudaGraphExecDestroy(p->mb_graph);
   free_problem_buffers(ctx, p->d);
   acdc_host_slot_give(ctx, p->h_eval);
   ctx->live_problems--;
@@ -642,6 +649,9 @@ extern "C" int acdc_problem_reset(acdc_problem* p) {
   p->k_next = 0;
   p->epochs_done = 0;
   p->updates_done = 0;
+  p->mb_updates = 0;
+  ACDC_CK(ctx, cudaMemsetAsync(p->d.counters + CNT_MB_COUNTER, 0, sizeof(unsigned long long),
+                               ctx->stream));
   p->active_valid = false;
   p->screen_valid = false;
   p->li_scale_shrink = 1.0;
@@ -695,9 +705,95 @@ extern "C" int acdc_problem_set_lambda(acdc_problem* p, double lambda) {
   return ACDC_OK;
 }
 
+namespace {
+bool minibatch_mode(const acdc_problem* p) {
+  return p->s.minibatch != 0 && p->loss == ACDC_LOSS_SVM_DUAL;
+}
+
+// Updates of one mini-batch epoch: ceil(n / tau) steps of tau (tau <= n).
+uint64_t minibatch_epoch(const acdc_problem* p) {
+  const uint64_t n = (uint64_t)p->d.n;
+  const uint64_t tau = (uint64_t)std::min<int64_t>(std::max(1, p->s.tau), p->d.n);
+  return (n + tau - 1) / tau * tau;
+}
+
+// Synchronous mini-batch steps (settings.minibatch, SVM dual): enough steps of
+// tau distinct draws for n_updates updates (at least one), drawn an epoch's
+// worth at a time.  *done gets the updates made.
+int run_minibatch(acdc_problem* p, uint64_t n_updates, uint64_t* done) {
+  acdc_ctx* ctx = p->ctx;
+  DevProblem& d = p->d;
+  const int32_t tau = (int32_t)std::min<int64_t>(std::max(1, p->s.tau), d.n);
+  const int64_t per_epoch = (d.n + tau - 1) / tau;
+  if (!d.mb_draws) {
+    const size_t words = (size_t)((d.n + 31) / 32);
+    ACDC_CK(ctx, acdc_dev_alloc(ctx, (void**)&d.mb_draws, sizeof(int32_t) * (size_t)(per_epoch * tau)));
+    ACDC_CK(ctx, acdc_dev_alloc(ctx, (void**)&d.mb_delta, sizeof(double) * (size_t)tau));
+    ACDC_CK(ctx, acdc_dev_alloc(ctx, (void**)&d.mb_mark, sizeof(uint32_t) * words));
+    ACDC_CK(ctx, cudaMemsetAsync(d.mb_mark, 0, sizeof(uint32_t) * words, ctx->stream));
+    d.bytes += (int64_t)(sizeof(int32_t) * per_epoch * tau + sizeof(double) * tau +
+                         sizeof(uint32_t) * words);
+    p->mb_tau = tau;
+  }
+  if (tau != p->mb_tau)
+    return acdc_set_error(ctx, ACDC_EINVAL, "minibatch: tau changed after the first mini-batch step");
+  int64_t steps = (int64_t)((n_updates + (uint64_t)tau - 1) / (uint64_t)tau);
+  if (steps < 1) steps = 1;
+  UpdateParams u = update_params(p, (uint64_t)tau, false);
+  auto enqueue = [&](int32_t batch) -> cudaError_t {
+    cudaError_t e = launch_tau_nice(p->s.seed, d.n, tau, batch, d.counters + CNT_MB_COUNTER,
+                                    d.mb_draws, d.mb_mark, ctx->stream);
+    for (int32_t t = 0; t < batch && e == cudaSuccess; ++t)
+      e = launch_minibatch_step(u, d.mb_draws + (int64_t)t * tau, tau, d.mb_delta, ctx->stream);
+    return e;
+  };
+  // A whole epoch (the sampler and 2 ceil(n / tau) kernels) replays from a
+  // CUDA graph captured once for the current precision, lambda and seed; the
+  // draw counter lives on the device, so every replay continues the stream.
+  const bool key_ok = p->mb_graph && p->mb_graph_fp64 == p->fp64_mode &&
+                      p->mb_graph_lambda == p->lambda && p->mb_graph_seed == p->s.seed;
+  if (!key_ok && p->mb_graph) {
+    cudaGraphExecDestroy(p->mb_graph);
+    p->mb_graph = nullptr;
+  }
+  if (!p->mb_graph && steps >= per_epoch) {
+    cudaGraph_t g = nullptr;
+    ACDC_CK(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = enqueue((int32_t)per_epoch);
+    cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&p->mb_graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      p->mb_graph = nullptr;
+      return acdc_cuda_error(ctx, e, "mini-batch epoch graph");
+    }
+    p->mb_graph_fp64 = p->fp64_mode;
+    p->mb_graph_lambda = p->lambda;
+    p->mb_graph_seed = p->s.seed;
+  }
+  int64_t s0 = 0;
+  for (; p->mb_graph && s0 + per_epoch <= steps; s0 += per_epoch)
+    ACDC_CK(ctx, cudaGraphLaunch(p->mb_graph, ctx->stream));
+  for (; s0 < steps; s0 += per_epoch)
+    ACDC_CK(ctx, enqueue((int32_t)std::min<int64_t>(per_epoch, steps - s0)));
+  const uint64_t made = (uint64_t)steps * (uint64_t)tau;
+  p->mb_updates += made;
+  p->updates_done += made;
+  p->epochs_done = (int64_t)(p->updates_done / (uint64_t)d.n);
+  p->stats.update_launches += 2 * steps;
+  *done = made;
+  return ACDC_OK;
+}
+}  // namespace
+
 extern "C" int acdc_run_updates(acdc_problem* p, uint64_t n_updates) {
   if (!p) return ACDC_EINVAL;
   acdc_ctx* ctx = p->ctx;
+  if (minibatch_mode(p)) {
+    uint64_t done = 0;
+    return run_minibatch(p, n_updates, &done);
+  }
   UpdateParams u = update_params(p, n_updates, shrink_now(p));
   ACDC_CK(ctx, launch_update(u, p->k_next, p->s.warps_per_block, ctx->stream));
   p->k_next += n_updates;
@@ -885,8 +981,10 @@ extern "C" int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_t
   rc = evaluate_impl(p, &ev, &ev_ms);
   if (rc != ACDC_OK) return rc;
   trace(0, ev, 0.f, ev_ms, false, p->fp64_mode, false);
-  // Work is counted in updates; an epoch is n of them.
-  const uint64_t n = (uint64_t)p->d.n;
+  // Work is counted in updates; an epoch is n of them (in mini-batch mode,
+  // ceil(n / tau) steps of tau, so that bulks and the epoch budget are whole
+  // steps).
+  const uint64_t n = minibatch_mode(p) ? minibatch_epoch(p) : (uint64_t)p->d.n;
   const uint64_t budget = (uint64_t)p->s.max_epochs * n;
   uint64_t done = 0, done_fp64 = 0;
   double best = ev.rel_gap;
@@ -915,18 +1013,30 @@ extern "C" int acdc_solve_traced(acdc_problem* p, acdc_solve_result* out, acdc_t
     count = std::min(count, budget - done);
     const bool screen = shrink && p->s.screened_eval != 0 && p->screen_valid;
     UpdateParams u = update_params(p, count, shrink);
-    {
-      NvtxRange bulk(shrink ? "acdc_bulk_active" : "acdc_bulk");
+    if (minibatch_mode(p)) {
+      NvtxRange bulk("acdc_bulk_minibatch");
+      uint64_t made = 0;
       ACDC_CK(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
-      ACDC_CK(ctx, launch_update(u, p->k_next, p->s.warps_per_block, ctx->stream));
+      rc = run_minibatch(p, count, &made);
+      if (rc != ACDC_OK) return rc;
       ACDC_CK(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+      count = made;
+      done += count;
+      if (p->fp64_mode) done_fp64 += count;
+    } else {
+      {
+        NvtxRange bulk(shrink ? "acdc_bulk_active" : "acdc_bulk");
+        ACDC_CK(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+        ACDC_CK(ctx, launch_update(u, p->k_next, p->s.warps_per_block, ctx->stream));
+        ACDC_CK(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+      }
+      p->k_next += count;
+      p->stats.update_launches++;
+      done += count;
+      if (p->fp64_mode) done_fp64 += count;
+      p->updates_done += count;
+      p->epochs_done = (int64_t)(p->updates_done / n);
     }
-    p->k_next += count;
-    p->stats.update_launches++;
-    done += count;
-    if (p->fp64_mode) done_fp64 += count;
-    p->updates_done += count;
-    p->epochs_done = (int64_t)(p->updates_done / n);
     const bool screened_now = screen && p->screen_valid;
     rc = evaluate_impl(p, &ev, &ev_ms, screen);
     if (rc != ACDC_OK) return rc;
@@ -995,14 +1105,16 @@ extern "C" int acdc_set_x(acdc_problem* p, const double* x) {
 namespace {
 // Checkpoint layout: this header, then x as n doubles.
 struct CheckpointHeader {
-  char magic[8];            // "ACDCCKP1"
+  char magic[8];            // "ACDCCKP2"
   int32_t loss, fp64;
   int64_t m, n;
   uint64_t k_next, updates_done;
   int64_t epochs_done;
   double lambda;
+  uint64_t mb_counter;      // sampler counter of the synchronous mini-batch draws
+  uint64_t mb_updates;
 };
-constexpr char kCheckpointMagic[8] = {'A', 'C', 'D', 'C', 'C', 'K', 'P', '1'};
+constexpr char kCheckpointMagic[8] = {'A', 'C', 'D', 'C', 'C', 'K', 'P', '2'};
 }  // namespace
 
 extern "C" int64_t acdc_checkpoint_size(const acdc_problem* p) {
@@ -1023,6 +1135,10 @@ extern "C" int acdc_checkpoint_save(acdc_problem* p, void* buf, int64_t size) {
   h.updates_done = p->updates_done;
   h.epochs_done = p->epochs_done;
   h.lambda = p->lambda;
+  h.mb_updates = p->mb_updates;
+  ACDC_CK(p->ctx, cudaMemcpyAsync(&h.mb_counter, p->d.counters + CNT_MB_COUNTER, sizeof(uint64_t),
+                                  cudaMemcpyDeviceToHost, p->ctx->stream));
+  ACDC_CK(p->ctx, cudaStreamSynchronize(p->ctx->stream));
   std::memcpy(buf, &h, sizeof(h));
   return acdc_get_x(p, reinterpret_cast<double*>(static_cast<char*>(buf) + sizeof(h)));
 }
@@ -1043,6 +1159,10 @@ extern "C" int acdc_checkpoint_load(acdc_problem* p, const void* buf, int64_t si
   p->k_next = h.k_next;
   p->updates_done = h.updates_done;
   p->epochs_done = h.epochs_done;
+  p->mb_updates = h.mb_updates;
+  ACDC_CK(p->ctx, cudaMemcpyAsync(p->d.counters + CNT_MB_COUNTER, &h.mb_counter, sizeof(uint64_t),
+                                  cudaMemcpyHostToDevice, p->ctx->stream));
+  ACDC_CK(p->ctx, cudaStreamSynchronize(p->ctx->stream));
   p->hot_count = 0;
   return ACDC_OK;
 }
@@ -1095,6 +1215,37 @@ extern "C" int acdc_debug_sample(acdc_ctx* ctx, uint64_t seed, uint64_t k0, uint
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   acdc_dev_free(ctx, d);
   if (e != cudaSuccess) return acdc_cuda_error(ctx, e, "acdc_debug_sample");
+  return ACDC_OK;
+}
+
+extern "C" int acdc_debug_tau_nice(acdc_ctx* ctx, uint64_t seed, uint64_t k0, int64_t n,
+                                   int32_t tau, int32_t steps, int32_t* out, uint64_t* k_out) {
+  if (!ctx || n <= 0 || n > INT32_MAX || tau < 1 || tau > n || steps < 0 ||
+      (steps > 0 && !out) || !k_out)
+    return ACDC_EINVAL;
+  ACDC_CK(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  const size_t words = (size_t)((n + 31) / 32);
+  const size_t draws = (size_t)steps * (size_t)tau;
+  unsigned long long* d_k = nullptr;
+  int32_t* d_s = nullptr;
+  uint32_t* d_mark = nullptr;
+  cudaError_t e = acdc_dev_alloc(ctx, (void**)&d_k, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = acdc_dev_alloc(ctx, (void**)&d_s, sizeof(int32_t) * (draws > 0 ? draws : 1));
+  if (e == cudaSuccess) e = acdc_dev_alloc(ctx, (void**)&d_mark, sizeof(uint32_t) * words);
+  unsigned long long k = k0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_k, &k, sizeof(k), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_mark, 0, sizeof(uint32_t) * words, st);
+  if (e == cudaSuccess) e = launch_tau_nice(seed, n, tau, steps, d_k, d_s, d_mark, st);
+  if (e == cudaSuccess && draws > 0)
+    e = cudaMemcpyAsync(out, d_s, sizeof(int32_t) * draws, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&k, d_k, sizeof(k), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  acdc_dev_free(ctx, d_k);
+  acdc_dev_free(ctx, d_s);
+  acdc_dev_free(ctx, d_mark);
+  if (e != cudaSuccess) return acdc_cuda_error(ctx, e, "acdc_debug_tau_nice");
+  *k_out = k;
   return ACDC_OK;
 }
 

@@ -600,6 +600,176 @@ __global__ void __launch_bounds__(256, 4) k_pcdm_update_batch(BatchDev b) {
   pcdm_update_body<LOSS, T>(p, p.k_base, (int64_t)blockIdx.x - b.ublk_first[s], rings);
 }
 
+// ---- synchronous mini-batch SDCA (hinge dual), tau-nice steps ----
+//
+// The structure of the reference's mini-batch loop
+// (cpp/src/experiments/mSDCA.cpp:60-105): a step draws tau distinct
+// coordinates, computes every delta from the same w, then applies them all.
+//
+// k_tau_nice: one warp draws `steps` steps.  Each step takes the first tau
+// distinct values of the uniform sampler stream (counter *counter, the draw of
+// acdc_debug_sample), exactly the values the reference's rejection loop
+// (draw again while the value repeats an earlier one of the step) accepts:
+// the warp looks at 32 consecutive stream values at a time, keeps the first
+// lane of each value (match_any) if its mark bit is clear, and accepts the
+// fresh lanes in lane order until the step is full; the counter advances past
+// the last accepted candidate only.  The n mark bits live in shared memory
+// when they fit (cleared here), else in gmark (clear on entry); a step clears
+// the bits it set.
+template <bool kShared>
+__global__ void k_tau_nice(uint64_t seed, int64_t n, int32_t tau, int32_t steps,
+                           unsigned long long* counter, int32_t* S, uint32_t* gmark) {
+  extern __shared__ uint32_t smark[];
+  uint32_t* mark = kShared ? smark : gmark;
+  const int lane = threadIdx.x & 31;
+  if (kShared) {
+    for (int64_t i = lane; i < (n + 31) / 32; i += 32) smark[i] = 0u;
+    __syncwarp();
+  }
+  uint64_t k = *counter;
+  for (int st = 0; st < steps; ++st) {
+    int32_t* out = S + (int64_t)st * tau;
+    int count = 0;
+    while (count < tau) {
+      const uint64_t kk = k + (uint64_t)lane;
+      acdc_u32x4 o = acdc_philox4x32_10((uint32_t)kk, (uint32_t)(kk >> 32), ACDC_STREAM_SAMPLER, 0u,
+                                        (uint32_t)seed, (uint32_t)(seed >> 32));
+      const uint64_t u = ((uint64_t)o.v[0] << 32) | (uint64_t)o.v[1];
+      const int32_t c = (int32_t)__umul64hi(u, (uint64_t)n);
+      const unsigned same = __match_any_sync(ACDC_FULL_MASK, c);
+      const bool first = (int)(__ffs(same) - 1) == lane;
+      const uint32_t word = kShared ? mark[c >> 5] : __ldcg(mark + (c >> 5));
+      const bool fresh = first && ((word >> (c & 31)) & 1u) == 0u;
+      const unsigned fm = __ballot_sync(ACDC_FULL_MASK, fresh);
+      const int need = tau - count;
+      const int rank = __popc(fm & ((1u << lane) - 1u));
+      if (fresh && rank < need) {
+        out[count + rank] = c;
+        atomicOr(mark + (c >> 5), 1u << (c & 31));
+      }
+      if (__popc(fm) >= need) {
+        // the step fills at the need-th fresh lane: later candidates stay unused
+        const unsigned lastm = __ballot_sync(ACDC_FULL_MASK, fresh && rank == need - 1);
+        k += (uint64_t)(__ffs(lastm));
+        count = tau;
+      } else {
+        k += 32;
+        count += __popc(fm);
+      }
+      __syncwarp();  // marks and draws visible to every lane
+    }
+    for (int i = lane; i < tau; i += 32) {
+      const int32_t c = out[i];
+      atomicAnd(mark + (c >> 5), ~(1u << (c & 31)));
+    }
+    __syncwarp();
+  }
+  if (lane == 0) *counter = k;
+}
+
+// Sum of a full warp, in every lane.
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(ACDC_FULL_MASK, v, o);
+  return v;
+}
+
+// Adds lane 0's count of every warp of the block to *dst with one atomic.
+// Every thread of the block calls it.
+__device__ __forceinline__ void block_count(unsigned long long v, unsigned long long* dst) {
+  __shared__ unsigned long long part[kMaxWarps];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) part[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += part[i];
+    if (t) atomicAdd(dst, t);
+  }
+  __syncthreads();
+}
+
+// Phase 1: warp i computes delta_i = clip((1 - y g) lambda n Li, -a, 1 - a),
+// g = x_i^T w, for the i-th coordinate of the step, from w as the step found
+// it (MulticoreSVMDualLoss.h:119-141).  Entries stream in chunks of 128 with
+// the update kernel's loads and gathers.
+template <typename T>
+__global__ void __launch_bounds__(256) k_sdca_phase1(UpdateParams p, const int32_t* S, int32_t tau,
+                                                     T* dout) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wi = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const T* r = reinterpret_cast<const T*>(sizeof(T) == 8 ? (const void*)p.r64 : (const void*)p.r);
+  unsigned long long nread = 0;
+  if (wi < tau) {
+    const int32_t j = S[wi];
+    const int4 mt = __ldg(p.meta + j);
+    const uint64_t start = (uint64_t)(uint32_t)mt.x << 2;
+    const uint32_t len = (uint32_t)mt.y;
+    T acc = T(0);
+    for (uint32_t off = 0; off < len; off += 128u) {
+      const Chunk c = load_chunk(p, start, len, off, lane);
+      acc += gather_dot_head<ACDC_LOSS_SVM_DUAL, T>(r, c, off + 4u * (uint32_t)lane, len);
+    }
+    const T g = warp_sum(acc);
+    if (lane == 0) {
+      T xj;
+      if constexpr (sizeof(T) == 8)
+        xj = __ldcg(p.x64 + j);
+      else
+        xj = __ldcg(p.x32 + j);
+      const T li = (T)__int_as_float(mt.z) * (T)p.li_scale;
+      const T y = li < T(0) ? T(-1) : T(1);
+      T delta = (T(1) - g * y) * (T)p.lambda_d * fabs(li);
+      if (delta < -xj)
+        delta = -xj;
+      else if (delta > T(1) - xj)
+        delta = T(1) - xj;
+      dout[wi] = delta;
+      nread = len;
+    }
+  }
+  block_count(nread, p.counters + CNT_NNZ_READ);
+}
+
+// Phase 2: warp i applies delta_i: alpha_i += delta_i (the coordinates of a
+// step are distinct, so no other warp writes it) and w += delta_i y_i/(lambda n)
+// x_i with red.global.
+template <typename T>
+__global__ void __launch_bounds__(256) k_sdca_phase2(UpdateParams p, const int32_t* S, int32_t tau,
+                                                     const T* din) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wi = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  T* r = reinterpret_cast<T*>(sizeof(T) == 8 ? (void*)p.r64 : (void*)p.r);
+  unsigned long long nz = 0, nscat = 0;
+  if (wi < tau) {
+    const T d = din[wi];
+    if (d != T(0)) {
+      const int32_t j = S[wi];
+      const int4 mt = __ldg(p.meta + j);
+      const uint64_t start = (uint64_t)(uint32_t)mt.x << 2;
+      const uint32_t len = (uint32_t)mt.y;
+      const T y = __int_as_float(mt.z) < 0.f ? T(-1) : T(1);
+      const T coef = d * y * (T)p.inv_lambda_n_d;
+      for (uint32_t off = 0; off < len; off += 128u) {
+        const Chunk c = load_chunk(p, start, len, off, lane);
+        scatter<T>(r, c, coef, off + 4u * (uint32_t)lane < len);
+      }
+      if (lane == 0) {
+        if constexpr (sizeof(T) == 8)
+          p.x64[j] = p.x64[j] + d;
+        else
+          p.x32[j] = p.x32[j] + d;
+        nz = 1;
+        nscat = len;
+      }
+    }
+  }
+  block_count(nz, p.counters + CNT_NONZERO);
+  block_count(nscat, p.counters + CNT_NNZ_SCATTERED);
+  block_count(wi < tau && lane == 0 ? 1ull : 0ull, p.counters + CNT_UPDATES);
+}
+
 // The sampler's uniform draw with a 64-bit result, so the stream can be checked
 // for any n (problems themselves hold fewer than 2^31 coordinates).
 __global__ void k_debug_sample(uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
@@ -691,6 +861,38 @@ cudaError_t launch_update(const UpdateParams& p, uint64_t k_base, int warps_per_
     }
   }
 #undef ACDC_LAUNCH
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tau_nice(uint64_t seed, int64_t n, int32_t tau, int32_t steps,
+                            unsigned long long* counter, int32_t* S, uint32_t* mark,
+                            cudaStream_t st) {
+  if (steps <= 0 || tau <= 0) return cudaSuccess;
+  const int64_t words = (n + 31) / 32;
+  if (words * 4 <= 48 * 1024)
+    k_tau_nice<true><<<1, 32, (size_t)words * 4, st>>>(seed, n, tau, steps, counter, S, mark);
+  else
+    k_tau_nice<false><<<1, 32, 0, st>>>(seed, n, tau, steps, counter, S, mark);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_minibatch_step(const UpdateParams& p, const int32_t* S, int32_t tau, void* delta,
+                                  cudaStream_t st) {
+  if (tau <= 0) return cudaSuccess;
+  // tau warps, spread over the SMs
+  int wpb = kMaxWarps;
+  if (p.sm_count > 0) {
+    const int spread = (tau + p.sm_count - 1) / p.sm_count;
+    if (spread < wpb) wpb = spread > 0 ? spread : 1;
+  }
+  const dim3 grid((unsigned)((tau + wpb - 1) / wpb)), block(wpb * 32);
+  if (p.fp64) {
+    k_sdca_phase1<double><<<grid, block, 0, st>>>(p, S, tau, static_cast<double*>(delta));
+    k_sdca_phase2<double><<<grid, block, 0, st>>>(p, S, tau, static_cast<const double*>(delta));
+  } else {
+    k_sdca_phase1<float><<<grid, block, 0, st>>>(p, S, tau, static_cast<float*>(delta));
+    k_sdca_phase2<float><<<grid, block, 0, st>>>(p, S, tau, static_cast<const float*>(delta));
+  }
   return cudaGetLastError();
 }
 

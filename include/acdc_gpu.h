@@ -128,6 +128,17 @@ typedef struct acdc_settings {
                                      updates per warp) with records and entries
                                      prefetched into registers.  tau counts the
                                      updates in flight either way.                */
+  int32_t minibatch;              /* SVM dual (loss 2) only, 1: synchronous
+                                     mini-batch SDCA as the reference's mini-batch
+                                     loop runs it (cpp/src/experiments/mSDCA.cpp:
+                                     60-105): each step draws tau distinct samples
+                                     (the first tau distinct values of the sampler
+                                     stream), computes every delta from the same w,
+                                     then applies them all; beta is the ESO value
+                                     for tau and an epoch is ceil(n / tau) steps.
+                                     q-shrinking is off in this mode.  0 (default):
+                                     asynchronous, tau updates in flight.         */
+  int32_t reserved3;
 } acdc_settings;
 
 /* precision: FP32 x and residual with FP64 refresh and gap (FP32), the same
@@ -302,7 +313,8 @@ int acdc_get_x(acdc_problem* p, double* x);        /* n entries (alpha for loss 
 int acdc_set_x(acdc_problem* p, const double* x);  /* warm start; refreshes r      */
 
 /* Checkpoint and resume of a problem's solver state: x (FP64), the sampler's
- * update counter, the updates and epochs done, lambda and the precision stage
+ * update counter (and the mini-batch draw counter), the updates and epochs
+ * done, lambda and the precision stage
  * (FP32 or FP64 x).  acdc_checkpoint_size gives the bytes (0 for a null
  * problem); acdc_checkpoint_save writes them to host memory; acdc_checkpoint_load
  * restores them into a problem of the same loss and sizes, recomputing the
@@ -333,6 +345,15 @@ int acdc_synchronize(acdc_problem* p);
  * against acdc_sample_coordinate (acdc_host.h). */
 int acdc_debug_sample(acdc_ctx* ctx, uint64_t seed, uint64_t k0, uint64_t count, int64_t n,
                       int64_t* out);
+
+/* The tau-nice draws of the synchronous mini-batch (settings.minibatch):
+ * `steps` steps of tau distinct coordinates in [0, n), each the first tau
+ * distinct values of the sampler stream from counter k0 on, into out
+ * (steps x tau, in the order drawn); *k_out gets the counter after the last
+ * step.  Replaces the draw loop of cpp/src/experiments/mSDCA.cpp:60-74
+ * (gsl_rng_uniform_int drawn again while it repeats a value of the step). */
+int acdc_debug_tau_nice(acdc_ctx* ctx, uint64_t seed, uint64_t k0, int64_t n, int32_t tau,
+                        int32_t steps, int32_t* out, uint64_t* k_out);
 
 /* acdc_debug_sample without any allocation (no counterpart in the reference,
  * whose sampler is a host GSL call), for callers that must not allocate device

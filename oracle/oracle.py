@@ -70,6 +70,12 @@ def lib():
         L.orc_svm_solve.argtypes = [I64, I64, i64p, i32p, f64p, f64p, D, D, U64, D, I64, I64, f64p,
                                     f64p, f64p]
         L.orc_svm_solve.restype = I64
+        L.orc_tau_nice.argtypes = [U64, C.POINTER(U64), I64, I64, i32p]
+        L.orc_svm_minibatch.argtypes = [I64, i64p, i32p, f64p, f64p, D, f64p, f64p, f64p, U64,
+                                        C.POINTER(U64), I64, I64]
+        L.orc_svm_minibatch_solve.argtypes = [I64, I64, i64p, i32p, f64p, f64p, D, D, U64, I64, D,
+                                              I64, I64, f64p, f64p, f64p]
+        L.orc_svm_minibatch_solve.restype = I64
         L.orc_lasso_hogwild.argtypes = [I64, i64p, i32p, f64p, D, f64p, f64p, f64p, U64, U64, U64,
                                         I]
         L.orc_lasso_hogwild.restype = D
@@ -308,6 +314,13 @@ class SVM:
                               self.Li, self.x, self.r, seed, self.k, int(count))
         self.k += int(count)
 
+    def minibatch(self, steps, seed, tau):
+        """Synchronous tau-nice mini-batch steps (counter self.k continues)."""
+        k = U64(self.k)
+        lib().orc_svm_minibatch(self.n, self.row_ptr, self.col_idx, self.vals, self.y, self.lam,
+                                self.Li, self.x, self.r, seed, C.byref(k), int(tau), int(steps))
+        self.k = int(k.value)
+
     def hogwild(self, count, seed, threads):
         t = lib().orc_svm_hogwild(self.n, self.row_ptr, self.col_idx, self.vals, self.y, self.lam,
                                   self.Li, self.x, self.r, seed, self.k, int(count), threads)
@@ -331,6 +344,31 @@ def svm_solve(d, n, row_ptr, col_idx, vals, y, lam, sigma=1.0, seed=1, target=1e
                              np.ascontiguousarray(vals, np.float64),
                              np.ascontiguousarray(y, np.float64), lam, sigma, seed, target,
                              max_epochs, check_every, a, w, out)
+    return a, w, _eval_dict(out), int(ep)
+
+
+def tau_nice(seed, k, n, tau, steps=1):
+    """The tau-nice draws of `steps` steps from counter k: (array steps x tau, new k)."""
+    kk = U64(k)
+    out = np.zeros((steps, tau), np.int32)
+    for st in range(steps):
+        row = np.zeros(tau, np.int32)
+        lib().orc_tau_nice(seed, C.byref(kk), n, tau, row)
+        out[st] = row
+    return out, int(kk.value)
+
+
+def svm_minibatch_solve(d, n, row_ptr, col_idx, vals, y, lam, tau, sigma=1.0, seed=1,
+                        target=1e-9, max_epochs=100000, check_every=1):
+    """Synchronous mini-batch SDCA solve (hinge dual, tau-nice steps)."""
+    a = np.zeros(n)
+    w = np.zeros(d)
+    out = np.zeros(9)
+    ep = lib().orc_svm_minibatch_solve(d, n, np.ascontiguousarray(row_ptr, np.int64),
+                                       np.ascontiguousarray(col_idx, np.int32),
+                                       np.ascontiguousarray(vals, np.float64),
+                                       np.ascontiguousarray(y, np.float64), lam, sigma, seed,
+                                       int(tau), target, max_epochs, check_every, a, w, out)
     return a, w, _eval_dict(out), int(ep)
 
 

@@ -675,6 +675,96 @@ void orc_svm_updates(int64_t n, const int64_t* row_ptr, const int32_t* col_idx,
   }
 }
 
+/* tau-nice sampling as the reference's mini-batch loop draws it
+ * (cpp/src/experiments/mSDCA.cpp:60-74): each of the tau entries is drawn
+ * from the uniform stream (gsl_rng_uniform_int, here orc_sample with a running
+ * counter *k) and drawn again while it repeats an earlier entry of the same
+ * step, so a step holds the first tau distinct values of the stream.  tau must
+ * not exceed n.  Writes S[0..tau) in acceptance order; *k advances by the
+ * candidates consumed. */
+void orc_tau_nice(uint64_t seed, uint64_t* k, int64_t n, int64_t tau, int32_t* S) {
+  for (int64_t i = 0; i < tau; ++i) {
+    for (;;) {
+      const int32_t c = (int32_t)orc_sample(seed, (*k)++, (uint64_t)n);
+      int64_t j = 0;
+      while (j < i && S[j] != c) ++j;
+      if (j == i) {
+        S[i] = c;
+        break;
+      }
+    }
+  }
+}
+
+/* Synchronous mini-batch SDCA for the hinge-loss dual: the structure of the
+ * reference's mini-batch loop (cpp/src/experiments/mSDCA.cpp:79-105: every
+ * delta of the step computed from the same w, then all applied) with the
+ * hinge-dual coordinate step of MulticoreSVMDualLoss.h:119-141
+ * (delta_i = clip((1 - y_i x_i^T w) lambda n Li_i, -alpha_i, 1 - alpha_i),
+ * Li_i = 1/(sigma ||x_i||^2)).  Runs `steps` steps of tau-nice draws from the
+ * counter *k; deltas are applied in the order of S. */
+void orc_svm_minibatch(int64_t n, const int64_t* row_ptr, const int32_t* col_idx,
+                       const double* vals, const double* y, double lambda, const double* Li,
+                       double* alpha, double* w, uint64_t seed, uint64_t* k, int64_t tau,
+                       int64_t steps) {
+  if (tau > n) tau = n;
+  int32_t* S = (int32_t*)malloc(sizeof(int32_t) * (size_t)(tau > 0 ? tau : 1));
+  double* d = (double*)malloc(sizeof(double) * (size_t)(tau > 0 ? tau : 1));
+  const double scaling = 1 / (lambda * (double)n);
+  for (int64_t st = 0; st < steps; ++st) {
+    orc_tau_nice(seed, k, n, tau, S);
+    for (int64_t i = 0; i < tau; ++i) {
+      const int64_t idx = S[i];
+      double tmp = 0;
+      for (int64_t t = row_ptr[idx]; t < row_ptr[idx + 1]; ++t) tmp += vals[t] * w[col_idx[t]];
+      tmp = (1 - tmp * y[idx]) * lambda * (double)n * Li[idx];
+      if (tmp < -alpha[idx])
+        tmp = -alpha[idx];
+      else if (tmp > 1 - alpha[idx])
+        tmp = 1 - alpha[idx];
+      d[i] = tmp;
+    }
+    for (int64_t i = 0; i < tau; ++i) {
+      const int64_t idx = S[i];
+      alpha[idx] = alpha[idx] + d[i];
+      for (int64_t t = row_ptr[idx]; t < row_ptr[idx + 1]; ++t)
+        w[col_idx[t]] = w[col_idx[t]] + d[i] * vals[t] * y[idx] * scaling;
+    }
+  }
+  free(S);
+  free(d);
+}
+
+/* Solve with the synchronous mini-batch: epochs of ceil(n / tau) steps, the
+ * FP64 refresh and gap after every check_every epochs (the reference checks
+ * once per n / tau steps, mSDCA.cpp:109-125), until the gap <= target or
+ * max_epochs.  Returns the epochs run. */
+int64_t orc_svm_minibatch_solve(int64_t m, int64_t n, const int64_t* row_ptr,
+                                const int32_t* col_idx, const double* vals, const double* y,
+                                double lambda, double sigma, uint64_t seed, int64_t tau,
+                                double target, int64_t max_epochs, int64_t check_every,
+                                double* alpha, double* w, double* out) {
+  double* Li = (double*)malloc(sizeof(double) * (size_t)n);
+  orc_svm_lipschitz(n, row_ptr, vals, sigma, Li);
+  orc_svm_residuals(m, n, row_ptr, col_idx, vals, y, lambda, alpha, w);
+  orc_svm_eval(m, n, row_ptr, col_idx, vals, y, lambda, alpha, w, 0, out);
+  if (tau > n) tau = n;
+  if (tau < 1) tau = 1;
+  if (check_every < 1) check_every = 1;
+  const int64_t steps_per_epoch = (n + tau - 1) / tau;
+  uint64_t k = 0;
+  int64_t epochs = 0;
+  while (out[2] > target && epochs < max_epochs) {
+    orc_svm_minibatch(n, row_ptr, col_idx, vals, y, lambda, Li, alpha, w, seed, &k, tau,
+                      check_every * steps_per_epoch);
+    epochs += check_every;
+    orc_svm_residuals(m, n, row_ptr, col_idx, vals, y, lambda, alpha, w);
+    orc_svm_eval(m, n, row_ptr, col_idx, vals, y, lambda, alpha, w, 0, out);
+  }
+  free(Li);
+  return epochs;
+}
+
 /* MulticoreSVMDualLoss::computeObjectiveValue (MulticoreSVMDualLoss.h:63-117). */
 void orc_svm_eval(int64_t m, int64_t n, const int64_t* row_ptr, const int32_t* col_idx,
                   const double* vals, const double* y, double lambda, const double* alpha,

@@ -114,6 +114,21 @@ int64_t orc_svm_solve(int64_t m, int64_t n, const int64_t* row_ptr, const int32_
                       uint64_t seed, double target, int64_t max_epochs, int64_t check_every,
                       double* alpha, double* w, double* out);
 
+/* Synchronous mini-batch SDCA (hinge dual): tau-nice draws as the reference's
+ * mini-batch loop makes them (first tau distinct values of the uniform stream,
+ * counter *k), every delta of a step from the same w, then all applied in the
+ * order drawn.  orc_tau_nice writes one step's draws. */
+void orc_tau_nice(uint64_t seed, uint64_t* k, int64_t n, int64_t tau, int32_t* S);
+void orc_svm_minibatch(int64_t n, const int64_t* row_ptr, const int32_t* col_idx,
+                       const double* vals, const double* y, double lambda, const double* Li,
+                       double* alpha, double* w, uint64_t seed, uint64_t* k, int64_t tau,
+                       int64_t steps);
+int64_t orc_svm_minibatch_solve(int64_t m, int64_t n, const int64_t* row_ptr,
+                                const int32_t* col_idx, const double* vals, const double* y,
+                                double lambda, double sigma, uint64_t seed, int64_t tau,
+                                double target, int64_t max_epochs, int64_t check_every,
+                                double* alpha, double* w, double* out);
+
 /* ---- OpenMP asynchronous form (the reference's multicore engine:
  * omp parallel for over updates, CAS-loop atomic adds).  Returns seconds. */
 double orc_lasso_hogwild(int64_t n, const int64_t* col_ptr, const int32_t* row_idx,

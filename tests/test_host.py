@@ -108,6 +108,12 @@ def test_settings_check_refuses_every_out_of_range_field():
         assert not acdc.settings_ok(acdc.default_settings(**{field: value})), (field, value)
 
 
+def test_minibatch_is_for_the_svm_dual_only():
+    assert not acdc.settings_ok(acdc.default_settings(acdc.LOSS_L1_SQUARE, minibatch=1))
+    assert not acdc.settings_ok(acdc.default_settings(acdc.LOSS_SVM_DUAL, minibatch=2))
+    assert acdc.settings_ok(acdc.default_settings(acdc.LOSS_SVM_DUAL, minibatch=1))
+
+
 def test_generator_is_deterministic_and_thread_independent():
     a = acdc.gen_lasso(500, 2000, nnz_per_col=7, n_star=30, seed=42, threads=1)
     b = acdc.gen_lasso(500, 2000, nnz_per_col=7, n_star=30, seed=42, threads=4)

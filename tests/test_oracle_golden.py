@@ -221,3 +221,59 @@ def test_smooth_duality_gaps_close_at_the_optimum(loss):
     x, r, ev, ep = oracle.smooth_solve(loss, inst.m, inst.n, inst.col_ptr, inst.row_idx, inst.vals,
                                        b, lam, target=1e-10, max_epochs=20000)
     assert ev["rel_gap"] <= 1e-10 and abs(ev["primal"] - ev["dual"]) <= 1e-9 * abs(ev["primal"])
+
+
+def test_tau_nice_is_the_reference_rejection_loop():
+    """orc_tau_nice against the draw loop of cpp/src/experiments/mSDCA.cpp:60-74
+    restated here: each entry drawn from the uniform stream again while it
+    repeats an earlier entry of the step, one stream across steps."""
+    for seed, n, tau, steps in ((7, 40, 25, 5), (3, 5, 5, 4), (11, 100000, 300, 3), (1, 9, 1, 6)):
+        k, want = 0, []
+        for _ in range(steps):
+            S = []
+            for _ in range(tau):
+                while True:
+                    c = oracle.sample(seed, k, n)
+                    k += 1
+                    if c not in S:
+                        S.append(c)
+                        break
+            want.append(S)
+        got, k2 = oracle.tau_nice(seed, 0, n, tau, steps)
+        assert got.tolist() == want and k2 == k
+
+
+def test_minibatch_step_computes_every_delta_from_the_same_w():
+    """One synchronous step (mSDCA.cpp:79-105 with the hinge-dual update of
+    MulticoreSVMDualLoss.h:119-141) restated with numpy: all deltas from the w
+    the step found, then applied."""
+    sv = acdc.gen_svm(80, 400, nnz_median=20, w_star_nnz=40, lam=1e-2, seed=5)
+    tau, seed, beta = 30, 4, 1.7
+    O = oracle.SVM(sv.m, sv.n, sv.col_ptr, sv.row_idx, sv.vals, sv.rhs, sv.lam, sigma=beta)
+    O.updates(300, 9)  # a nontrivial start
+    O.k = 0
+    a0, w0 = O.x.copy(), O.r.copy()
+    S, _ = oracle.tau_nice(seed, 0, sv.n, tau, 1)
+    d = np.zeros(tau)
+    for t, i in enumerate(S[0]):
+        s, e = sv.col_ptr[i], sv.col_ptr[i + 1]
+        g = sv.vals[s:e] @ w0[sv.row_idx[s:e]]
+        d[t] = np.clip((1 - sv.rhs[i] * g) * sv.lam * sv.n * O.Li[i], -a0[i], 1 - a0[i])
+    a1, w1 = a0.copy(), w0.copy()
+    for t, i in enumerate(S[0]):
+        s, e = sv.col_ptr[i], sv.col_ptr[i + 1]
+        a1[i] += d[t]
+        np.add.at(w1, sv.row_idx[s:e], d[t] * sv.vals[s:e] * sv.rhs[i] / (sv.lam * sv.n))
+    O.minibatch(1, seed, tau)
+    np.testing.assert_allclose(O.x, a1, rtol=0, atol=1e-14)
+    np.testing.assert_allclose(O.r, w1, rtol=0, atol=1e-14)
+
+
+def test_minibatch_trajectory_fixture():
+    f = load("svm_minibatch_traj.npz")
+    O = oracle.SVM(int(f["m"]), int(f["n"]), f["row_ptr"], f["col_idx"], f["vals"], f["y"],
+                   float(f["lam"]), sigma=float(f["beta"]))
+    for e in range(len(f["alpha"])):
+        O.minibatch(int(f["steps_per_epoch"]), int(f["seed"]), int(f["tau"]))
+        assert np.array_equal(O.x, f["alpha"][e]) and np.array_equal(O.r, f["w"][e])
+        assert O.k == int(f["counter"][e])
