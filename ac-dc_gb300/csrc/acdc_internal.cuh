@@ -163,6 +163,13 @@ struct SlotCtl {
   double q;
   double omega;
   double beta;
+  // A stall rule like the single-problem solve's AUTO precision: the best
+  // relative gap of the current lambda and the updates spent when it last
+  // halved; a slot whose gap (below 1e-4) has not halved over stall_updates
+  // switches to FP64.
+  double best_gap;
+  uint64_t gain_at;
+  uint64_t stall_updates;
 };
 
 // Row of a per-lambda result: eval_out[0..9], lambda, converged, epochs, tau.
@@ -217,6 +224,9 @@ struct acdc_ctx {
   int device = 0;
   int sm_count = 0;
   cudaStream_t stream = nullptr;
+  // Second stream for the server's admissions (created by the first server):
+  // problems are created on it while rounds run on `stream`.
+  cudaStream_t admit_stream = nullptr;
   cudaMemPool_t pool = nullptr;  // device memory of the context's problems and tables
   // Pinned host slots (16 doubles of evaluation results + CNT_SLOTS counters
   // each) handed to problems: cut from blocks allocated once, so creating and

@@ -144,6 +144,10 @@ extern "C" int acdc_ctx_destroy(acdc_ctx* ctx) {
     return acdc_set_error(ctx, ACDC_EBUSY, "destroy every problem of the context first");
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);  // frees in flight complete
+  if (ctx->admit_stream) {
+    cudaStreamSynchronize(ctx->admit_stream);
+    cudaStreamDestroy(ctx->admit_stream);
+  }
   for (int i = 0; i < 6; ++i)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);

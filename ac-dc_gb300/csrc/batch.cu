@@ -197,6 +197,10 @@ class BatchEngine {
       c.round_updates = u.count;
       c.gap_target = gap_targets ? (*gap_targets)[(size_t)i] : o.gap_target;
       c.polish_rel_gap = p->s.polish_rel_gap;
+      c.best_gap = 1e300;
+      c.gain_at = 0;
+      c.stall_updates = (uint64_t)(p->s.polish_stall_epochs > 0 ? p->s.polish_stall_epochs : 10) *
+                        (uint64_t)p->d.n;
       c.lambdas = lambdas_ + (size_t)i * path;
       c.results = results_ + (size_t)i * path * ACDC_BATCH_RESULT_LEN;
       ublk_first[(size_t)i] = (int32_t)ublk_slot.size();
@@ -273,13 +277,19 @@ class BatchEngine {
 
   // Runs rounds without a graph (the slot set changes between calls).
   int run_rounds(int rounds, int64_t* count = nullptr) {
+    int rc = enqueue_rounds(rounds, count);
+    if (rc) return rc;
+    ACDC_CK(ctx_, cudaStreamSynchronize(ctx_->stream));
+    return ACDC_OK;
+  }
+
+  // Enqueues the rounds back to back without waiting for them.
+  int enqueue_rounds(int rounds, int64_t* count = nullptr) {
     if (*h_live_ <= 0) return ACDC_OK;
-    // All of the step's rounds back to back, one synchronisation at the end.
     for (int r = 0; r < rounds; ++r) {
       ACDC_CK(ctx_, enqueue_round());
       if (count) ++*count;
     }
-    ACDC_CK(ctx_, cudaStreamSynchronize(ctx_->stream));
     return ACDC_OK;
   }
 
@@ -490,14 +500,45 @@ struct acdc_server {
   std::map<int64_t, std::unique_ptr<Request>> all;
   BatchEngine* engine = nullptr;
   bool dirty = true;                        // resident set changed since the last build
+  bool in_flight = false;                   // rounds enqueued by the last step, not yet waited for
+  std::vector<Request*> built;              // the requests of the engine's slots, in slot order
   acdc_server_stats stats{};
 };
+
+namespace {
+// Makes the context's admission stream the one its calls use for the scope:
+// problems created inside are uploaded, laid out and checked on it, so their
+// work and their synchronisations do not wait for the rounds on the main
+// stream.
+struct AdmitStream {
+  acdc_ctx* ctx;
+  cudaStream_t main;
+  explicit AdmitStream(acdc_ctx* c) : ctx(c), main(c->stream) { ctx->stream = ctx->admit_stream; }
+  ~AdmitStream() { ctx->stream = main; }
+  AdmitStream(const AdmitStream&) = delete;
+  AdmitStream& operator=(const AdmitStream&) = delete;
+};
+
+// Waits for the rounds the last step enqueued.
+int finish_rounds(acdc_server* s) {
+  if (!s->in_flight) return ACDC_OK;
+  const double t0 = now_seconds();
+  ACDC_CK(s->ctx, cudaStreamSynchronize(s->ctx->stream));
+  s->in_flight = false;
+  s->stats.rounds_s += now_seconds() - t0;
+  return ACDC_OK;
+}
+}  // namespace
 
 extern "C" int acdc_server_create(acdc_ctx* ctx, const acdc_server_options* opt, acdc_server** out) {
   if (!ctx || !opt || !out) return ACDC_EINVAL;
   if (opt->memory_budget_bytes <= 0 || opt->max_slots < 1 || opt->quantum_epochs < 1 ||
       opt->max_epochs < 1)
     return acdc_set_error(ctx, ACDC_EINVAL, "invalid server options");
+  if (!ctx->admit_stream) {
+    ACDC_CK(ctx, cudaSetDevice(ctx->device));
+    ACDC_CK(ctx, cudaStreamCreateWithFlags(&ctx->admit_stream, cudaStreamNonBlocking));
+  }
   acdc_server* s = new acdc_server();
   s->ctx = ctx;
   s->opt = *opt;
@@ -553,24 +594,22 @@ extern "C" int acdc_server_submit(acdc_server* s, const acdc_request* req, int64
 }
 
 namespace {
-// Retires the resident requests whose slot finished (their only lambda done):
-// records the result, reads x back and frees the device buffers.
+// Retires the requests of the engine's slots whose lambda is done: records the
+// result, reads x back and frees the device buffers.  Only the slots of the
+// last build are looked at (requests admitted since then have no slot yet);
+// every slot's sampler counter and precision go back into its problem.
 int retire_finished(acdc_server* s) {
-  if (s->resident.empty()) return ACDC_OK;
+  if (s->built.empty()) return ACDC_OK;
   std::vector<acdc_problem*> probs;
-  for (Request* r : s->resident) probs.push_back(r->prob);
+  for (Request* r : s->built) probs.push_back(r->prob);
   std::vector<double> rows;
   std::vector<SlotCtl> ctl;
   int rc = s->engine->collect(probs, rows, ctl);
   if (rc) return rc;
-  std::vector<Request*> keep;
-  bool changed = false;
-  for (size_t i = 0; i < s->resident.size(); ++i) {
-    Request* r = s->resident[i];
-    if (ctl[i].live) {
-      keep.push_back(r);
-      continue;
-    }
+  std::vector<Request*> gone;
+  for (size_t i = 0; i < s->built.size(); ++i) {
+    Request* r = s->built[i];
+    if (ctl[i].live) continue;
     acdc_batch_result br;
     row_to_result(rows.data() + i * ACDC_BATCH_RESULT_LEN, &br);
     r->res.eval = br.eval;
@@ -585,11 +624,17 @@ int retire_finished(acdc_server* s) {
     s->used_bytes -= r->footprint;
     r->res.finish_time = now_seconds();
     r->res.state = r->res.status == ACDC_OK ? 2 : 3;
-    changed = true;
+    gone.push_back(r);
     s->stats.retired++;
   }
-  s->resident.swap(keep);
-  if (changed) s->dirty = true;
+  if (!gone.empty()) {
+    std::vector<Request*> keep;
+    for (Request* r : s->resident)
+      if (std::find(gone.begin(), gone.end(), r) == gone.end()) keep.push_back(r);
+    s->resident.swap(keep);
+    s->built.clear();  // the tables list retired slots: rebuilt before the next round
+    s->dirty = true;
+  }
   return ACDC_OK;
 }
 
@@ -599,8 +644,12 @@ void admit_one(acdc_server* s, Request* r, const int64_t* col_ptr, const int32_t
                const double* vals, const double* rhs) {
   const double t0 = now_seconds();
   acdc_problem* p = nullptr;
-  int rc = acdc_problem_create(s->ctx, r->loss, r->m, r->n, col_ptr, row_idx, vals, rhs,
-                               r->lambda, &p);
+  int rc;
+  {
+    AdmitStream on(s->ctx);
+    rc = acdc_problem_create(s->ctx, r->loss, r->m, r->n, col_ptr, row_idx, vals, rhs, r->lambda,
+                             &p);
+  }
   r->res.start_time = now_seconds();
   s->stats.admit_s += r->res.start_time - t0;
   if (rc != ACDC_OK) {
@@ -635,12 +684,25 @@ void admit(acdc_server* s) {
 }
 }  // namespace
 
+// A step is pipelined: it waits for the rounds the previous step enqueued,
+// retires the requests that finished, rebuilds the slot tables if the resident
+// set changed, enqueues this step's rounds and returns without waiting for
+// them, after admitting queued requests on the admission stream while those
+// rounds run (they join the next step's tables).
 extern "C" int acdc_server_step(acdc_server* s, int32_t* pending) {
   if (!s) return ACDC_EINVAL;
   acdc_ctx* ctx = s->ctx;
   ACDC_CK(ctx, cudaSetDevice(ctx->device));
   NvtxRange range("acdc_server_step");
-  admit(s);
+  int rc = finish_rounds(s);
+  if (rc) return rc;
+  {
+    const double t1 = now_seconds();
+    rc = retire_finished(s);
+    if (rc) return rc;
+    s->stats.retire_s += now_seconds() - t1;
+  }
+  if (s->resident.empty()) admit(s);  // nothing to overlap with: admit first
   if (!s->resident.empty()) {
     if (s->dirty) {
       // Rebuild the slot tables over the resident set: running slots keep their
@@ -655,21 +717,18 @@ extern "C" int acdc_server_step(acdc_server* s, int32_t* pending) {
         targets.push_back(r->gap_target);
       }
       const double t0 = now_seconds();
-      int rc = s->engine->build(probs, lams, 1, o, &targets);
+      rc = s->engine->build(probs, lams, 1, o, &targets);
       if (rc) return rc;
+      s->built = s->resident;
       s->dirty = false;
       s->stats.builds++;
       s->stats.build_s += now_seconds() - t0;
     }
-    double t0 = now_seconds();
-    int rc = s->engine->run_rounds(s->opt.quantum_epochs, &s->stats.rounds);
+    rc = s->engine->enqueue_rounds(s->opt.quantum_epochs, &s->stats.rounds);
     if (rc) return rc;
-    double t1 = now_seconds();
-    s->stats.rounds_s += t1 - t0;
-    rc = retire_finished(s);
-    if (rc) return rc;
-    s->stats.retire_s += now_seconds() - t1;
+    s->in_flight = true;
   }
+  admit(s);
   s->stats.steps++;
   if (pending) *pending = (int32_t)(s->queue.size() + s->resident.size());
   return ACDC_OK;
@@ -706,6 +765,12 @@ extern "C" int acdc_server_cancel(acdc_server* s, int64_t ticket) {
   if (it == s->all.end()) return ACDC_ENOTFOUND;
   Request* r = it->second.get();
   if (r->res.state >= 2) return ACDC_OK;
+  // no round may be in flight while a resident problem goes away, and the
+  // finished slots are retired before the tables are dropped
+  int rc = finish_rounds(s);
+  if (rc == ACDC_OK) rc = retire_finished(s);
+  if (rc) return rc;
+  if (r->res.state >= 2) return ACDC_OK;
   if (r->res.state == 0) {
     for (auto q = s->queue.begin(); q != s->queue.end(); ++q)
       if (*q == r) {
@@ -723,6 +788,7 @@ extern "C" int acdc_server_cancel(acdc_server* s, int64_t ticket) {
     if (r->prob) acdc_problem_destroy(r->prob);
     r->prob = nullptr;
     s->used_bytes -= r->footprint;
+    s->built.clear();
     s->dirty = true;
   }
   r->res.state = 3;
@@ -733,6 +799,8 @@ extern "C" int acdc_server_cancel(acdc_server* s, int64_t ticket) {
 
 extern "C" int acdc_server_destroy(acdc_server* s) {
   if (!s) return ACDC_EINVAL;
+  finish_rounds(s);
+  if (s->ctx->admit_stream) cudaStreamSynchronize(s->ctx->admit_stream);
   for (Request* r : s->resident)
     if (r->prob) acdc_problem_destroy(r->prob);
   delete s->engine;

@@ -1300,9 +1300,7 @@ enum {
   EV_REFRESH_INIT,
   EV_REFRESH_SCATTER,
   EV_REFRESH_FINISH,
-  EV_GAP_SHORT,
-  EV_GAP_LONG,
-  EV_GAP_SVM,
+  EV_GAP,  // the gap pass of the slot's loss (Lasso: short, then long columns)
   EV_ACTIVE_OMEGA
 };
 
@@ -1332,8 +1330,6 @@ __global__ void __launch_bounds__(ACDC_RED_THREADS) k_eval_batch(BatchDev b) {
   const int s = b.eblk_slot[blockIdx.x];
   if (!b.ctl[s].live) return;
   const EvalParams p = b.ep[s];
-  if ((KIND == EV_GAP_SHORT || KIND == EV_GAP_LONG) && p.loss != ACDC_LOSS_L1_SQUARE) return;
-  if (KIND == EV_GAP_SVM && p.loss != ACDC_LOSS_SVM_DUAL) return;
   const int64_t rank = (int64_t)blockIdx.x - b.eblk_first[s];
   const int64_t nb = b.eblk_count[s];
   if (KIND == EV_REFRESH_INIT) k_refresh_init_body(p, rank, nb);
@@ -1352,9 +1348,14 @@ __global__ void __launch_bounds__(ACDC_RED_THREADS) k_eval_batch(BatchDev b) {
   }
   if (KIND == EV_REFRESH_SCATTER) k_refresh_scatter_body(p, rank, nb);
   if (KIND == EV_REFRESH_FINISH) k_refresh_finish_body(p, rank, nb);
-  if (KIND == EV_GAP_SHORT) k_gap_lasso_short_body(p, rank, nb);
-  if (KIND == EV_GAP_LONG) k_gap_lasso_long_body(p, rank, nb);
-  if (KIND == EV_GAP_SVM) k_gap_svm_body(p, rank, nb);
+  if (KIND == EV_GAP) {
+    if (p.loss == ACDC_LOSS_L1_SQUARE) {
+      k_gap_lasso_short_body(p, rank, nb);
+      k_gap_lasso_long_body(p, rank, nb);
+    } else {
+      k_gap_svm_body(p, rank, nb);
+    }
+  }
 }
 
 // One block per slot: form the gap from the slot's partials, then decide.
@@ -1362,7 +1363,8 @@ __global__ void __launch_bounds__(ACDC_RED_THREADS) k_eval_batch(BatchDev b) {
 //    record the result row, move to the next lambda (warm start: x and the
 //    residual carry over; FP64 coordinates are rounded back to FP32 for the next
 //    bulk) or retire the slot after the last lambda;
-//  * otherwise, below polish_rel_gap in FP32: continue in FP64 (x64 = x).
+//  * otherwise, below polish_rel_gap in FP32, or stalled near it (the gap,
+//    below 1e-4, has not halved over stall_updates): continue in FP64 (x64 = x).
 __global__ void __launch_bounds__(kFinThreads) k_batch_control(BatchDev b) {
   __shared__ int s_action;
   const int s = blockIdx.x;
@@ -1378,6 +1380,10 @@ __global__ void __launch_bounds__(kFinThreads) k_batch_control(BatchDev b) {
     up.k_base += up.count;
     c.updates_here += up.count;
     const bool conv = o[3] <= c.gap_target;
+    if (o[3] < 0.5 * c.best_gap) {
+      c.best_gap = o[3];
+      c.gain_at = c.updates_here;
+    }
     int action = 0;
     if (conv || c.updates_here >= c.max_updates) {
       double* row = c.results + (int64_t)c.k * ACDC_BATCH_RESULT_LEN;
@@ -1388,6 +1394,8 @@ __global__ void __launch_bounds__(kFinThreads) k_batch_control(BatchDev b) {
       row[13] = (double)up.n_warps;
       c.k++;
       c.updates_here = 0;
+      c.best_gap = 1e300;
+      c.gain_at = 0;
       if (c.k >= c.path_len) {
         c.live = 0;
         atomicSub(b.live_count, 1);
@@ -1403,7 +1411,8 @@ __global__ void __launch_bounds__(kFinThreads) k_batch_control(BatchDev b) {
         }
         if (up.fp64) action = 2;
       }
-    } else if (!up.fp64 && o[3] <= c.polish_rel_gap) {
+    } else if (!up.fp64 && (o[3] <= c.polish_rel_gap ||
+                            (o[3] < 1e-4 && c.updates_here - c.gain_at >= c.stall_updates))) {
       action = 1;
     }
     // Next round: uniform right after a lambda change (the active list was built
@@ -1455,9 +1464,7 @@ cudaError_t launch_batch_eval(const BatchDev& b, int eval_blocks, cudaStream_t s
   k_eval_batch<EV_REFRESH_INIT><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
   k_eval_batch<EV_REFRESH_SCATTER><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
   k_eval_batch<EV_REFRESH_FINISH><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
-  k_eval_batch<EV_GAP_SHORT><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
-  k_eval_batch<EV_GAP_LONG><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
-  k_eval_batch<EV_GAP_SVM><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
+  k_eval_batch<EV_GAP><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
   k_eval_batch<EV_ACTIVE_OMEGA><<<eval_blocks, ACDC_RED_THREADS, 0, st>>>(b);
   k_batch_control<<<b.n_slots, kFinThreads, 0, st>>>(b);
   return cudaGetLastError();

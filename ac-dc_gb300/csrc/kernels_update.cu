@@ -586,18 +586,26 @@ __global__ void __launch_bounds__(256) k_pcdm_update_grouped(UpdateParams p, uin
 }
 
 // Batched launch: each block serves one slot at rank blockIdx.x - first block
-// of that slot.  One instantiation per loss and precision; a block whose slot
-// is of another kind (or finished) returns at once.
-template <int LOSS, typename T>
+// of that slot, with the body of that slot's loss and precision, so one launch
+// covers Lasso and SVM slots in FP32 and FP64 alike.
 __global__ void __launch_bounds__(256, 4) k_pcdm_update_batch(BatchDev b) {
   __shared__ WarpRing rings[kMaxWarps];
   const int s = b.ublk_slot[blockIdx.x];
   if (!b.ctl[s].live) return;
   const UpdateParams p = b.up[s];
-  const bool mine = (p.loss == ACDC_LOSS_SVM_DUAL) == (LOSS == ACDC_LOSS_SVM_DUAL) &&
-                    (p.fp64 != 0) == (sizeof(T) == 8);
-  if (!mine || p.count == 0) return;
-  pcdm_update_body<LOSS, T>(p, p.k_base, (int64_t)blockIdx.x - b.ublk_first[s], rings);
+  if (p.count == 0) return;
+  const int64_t rank = (int64_t)blockIdx.x - b.ublk_first[s];
+  if (p.loss == ACDC_LOSS_SVM_DUAL) {
+    if (p.fp64)
+      pcdm_update_body<ACDC_LOSS_SVM_DUAL, double>(p, p.k_base, rank, rings);
+    else
+      pcdm_update_body<ACDC_LOSS_SVM_DUAL, float>(p, p.k_base, rank, rings);
+  } else {
+    if (p.fp64)
+      pcdm_update_body<ACDC_LOSS_L1_SQUARE, double>(p, p.k_base, rank, rings);
+    else
+      pcdm_update_body<ACDC_LOSS_L1_SQUARE, float>(p, p.k_base, rank, rings);
+  }
 }
 
 // ---- synchronous mini-batch SDCA (hinge dual), tau-nice steps ----
@@ -899,10 +907,7 @@ cudaError_t launch_minibatch_step(const UpdateParams& p, const int32_t* S, int32
 cudaError_t launch_batch_update(const BatchDev& b, int update_blocks, cudaStream_t st) {
   if (update_blocks <= 0) return cudaSuccess;
   const dim3 grid(update_blocks), block(kMaxWarps * 32);
-  k_pcdm_update_batch<ACDC_LOSS_L1_SQUARE, float><<<grid, block, 0, st>>>(b);
-  k_pcdm_update_batch<ACDC_LOSS_L1_SQUARE, double><<<grid, block, 0, st>>>(b);
-  k_pcdm_update_batch<ACDC_LOSS_SVM_DUAL, float><<<grid, block, 0, st>>>(b);
-  k_pcdm_update_batch<ACDC_LOSS_SVM_DUAL, double><<<grid, block, 0, st>>>(b);
+  k_pcdm_update_batch<<<grid, block, 0, st>>>(b);
   return cudaGetLastError();
 }
 
@@ -922,9 +927,6 @@ cudaError_t update_kernels_init() {
   ACDC_CARVE(ACDC_LOSS_LOGISTIC, float);
   ACDC_CARVE(ACDC_LOSS_LOGISTIC, double);
 #undef ACDC_CARVE
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_L1_SQUARE, float>, a, carve);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_L1_SQUARE, double>, a, carve);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_SVM_DUAL, float>, a, carve);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch<ACDC_LOSS_SVM_DUAL, double>, a, carve);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch, a, carve);
   return e;
 }

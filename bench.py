@@ -99,15 +99,16 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--max-epochs", type=int, default=0,
                     help="cap each solve (profiling runs; the line then reports converged=false)")
-    ap.add_argument("--batch-instances", type=int, default=8,
+    ap.add_argument("--batch-instances", type=int, default=64,
                     help="instances of the batched lambda-path sample (0 = skip)")
-    ap.add_argument("--batch-max-epochs", type=int, default=300)
+    ap.add_argument("--batch-max-epochs", type=int, default=200)
     ap.add_argument("--svm-steps", type=int, default=10,
                     help="solves of the SVM-dual workload reported under the line's svm key "
                          "(0 = skip)")
-    ap.add_argument("--serve-requests", type=int, default=256,
-                    help="requests of the serving sample (0 = skip)")
-    ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-requests", type=int, default=64,
+                    help="requests of the serving sample at each rate (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=0.0,
+                    help="one arrival rate per second (0 = the sweep 50..2000)")
     ap.add_argument("--serve-quantum", type=int, default=4,
                     help="rounds per server step (acdc_server_options.quantum_epochs)")
     ap.add_argument("--active-passes", type=int, default=0,
@@ -213,6 +214,7 @@ def run_batched(ctx, count, max_epochs, rank=0, world=1, dist=None, dev=None):
            "nnz": int(round(sum_over_ranks(dist, sum(x.nnz for x in insts), dev))),
            "shards": [len(x) for x in shards],
            "scaling": "strong: the sample's instances dealt to the ranks by footprint"}
+    conv_mask = {}
     for plain in (0, 1):
         probs = [acdc.Problem(ctx, x) for x in insts]
         for q in probs:
@@ -227,36 +229,75 @@ def run_batched(ctx, count, max_epochs, rank=0, world=1, dist=None, dev=None):
         for q in probs:
             q.close()
         key = "plain" if plain else "batched"
+        conv_mask[key] = [[bool(r.converged) for r in row] for row in res]
         conv = sum(r.converged for row in res for r in row)
         conv = int(round(sum_over_ranks(dist, conv, dev)))
-        out[key] = {"seconds": dt, "solves_per_s": count * 16 / dt, "converged": conv,
-                    "converged_per_s": conv / dt}
+        out[key] = {"seconds": dt, "all_solves_per_s": count * 16 / dt, "converged": conv,
+                    "converged_per_s": conv / dt,
+                    "converged_per_lambda": [sum(row[k] for row in conv_mask[key])
+                                             for k in range(16)]}
+    # the metric: solves that reached the gap in both paths, per second of each
+    both = sum(a and b for ra, rb in zip(conv_mask["batched"], conv_mask["plain"])
+               for a, b in zip(ra, rb))
+    both = int(round(sum_over_ranks(dist, both, dev)))
+    out["converged_in_both"] = both
+    neither = sum((not a) and (not b) for ra, rb in zip(conv_mask["batched"], conv_mask["plain"])
+                  for a, b in zip(ra, rb))
+    out["neither_converged"] = int(round(sum_over_ranks(dist, neither, dev)))
+    for key in ("batched", "plain"):
+        out[key]["solves_per_s"] = both / out[key]["seconds"]
     out["speedup"] = out["batched"]["solves_per_s"] / out["plain"]["solves_per_s"]
+    out["metric_rule"] = ("solves_per_s counts the lambda points both paths solved to the gap "
+                          "target, over each path's own time (which includes the points that "
+                          "hit the epoch cap)")
     return out
 
 
-def serve_sample(count, rate, seed=0xACDC0004, scale=0.25, pinned=True):
-    """Requests of the serving workload: 70% Lasso of the lambda-path mix's size
-    distribution (m, n scaled by `scale`, lambda = lambda_max / 2), 30% SVM duals
-    from the SVM generator scaled down (samples log-uniform in [1,000, 50,000 x
-    scale], 10 features per sample, median 100 entries, lambda = 1e-3); Poisson
-    arrivals at `rate` per second."""
+SERVE_RATES = (50, 100, 200, 500, 1000, 2000)
+SERVE_MAX_EPOCHS = 1000  # per request, both paths
+
+
+def serve_pool(seed=0xACDC0004, lasso=24, svm=8, pinned=True):
+    """Instances the serving requests draw from: Lasso problems of the lambda-path
+    mix's size distribution, unscaled (m log-uniform in [500, 50,000], n in
+    [1,000, 200,000], 5..50 entries per column), and SVM duals from the SVM
+    generator with samples log-uniform in [1,000, 50,000] and the features
+    scaled with them (1,355,191 per 20,000 samples), median 450 entries per
+    sample, lambda = 1e-4.  A pool keeps the host memory of a long request
+    stream bounded: requests share matrices, not device state."""
     import acdc
+    las, svs = [], []
+    for i in range(lasso):
+        m, n = acdc.mix_sizes(seed, i)
+        las.append(acdc.gen_lasso(m, n, nnz_mode=acdc.NNZ_UNIFORM, nnz_min=5, nnz_max=50,
+                                  n_star=max(1, n // 100), lambda_frac=1.0, seed=seed + i,
+                                  pinned=pinned))
+    for i in range(svm):
+        _, ns = acdc.mix_sizes(seed + 0x10, i, n_lo=1000, n_hi=50000)
+        d = max(1000, int(round(ns * 1355191 / 20000)))
+        svs.append(acdc.gen_svm(ns, d, nnz_median=450, nnz_sigma=0.8,
+                                w_star_nnz=max(10, ns // 4), lam=1e-4, seed=seed + 0x10 + i,
+                                pinned=pinned))
+    return las, svs
+
+
+def serve_sample(pool, count, rate, seed=0xACDC0004):
+    """A request stream: 70% Lasso (a pool instance at lambda = lambda_max 0.5^k,
+    k uniform in 1..5: further along the 16-point path some underdetermined
+    instances need thousands of epochs),
+    30% SVM duals (a pool instance); Poisson arrivals at `rate` per second.
+    Returns (instance, lambda, seed) per request and the arrival times."""
     import numpy as np
-    rng = np.random.default_rng(seed)
+    las, svs = pool
+    rng = np.random.default_rng(seed + int(rate))
     reqs = []
     for i in range(count):
         if rng.random() < 0.7:
-            m, n = acdc.mix_sizes(seed, i, m_lo=500, m_hi=int(50000 * scale), n_lo=1000,
-                                  n_hi=int(200000 * scale))
-            reqs.append(acdc.gen_lasso(m, n, nnz_mode=acdc.NNZ_UNIFORM, nnz_min=5, nnz_max=50,
-                                       n_star=max(1, n // 100), lambda_frac=0.5, seed=seed + i,
-                                       pinned=pinned))
+            inst = las[int(rng.integers(len(las)))]
+            reqs.append((inst, inst.lam * 0.5 ** int(rng.integers(1, 6)), i + 1))
         else:
-            _, ns = acdc.mix_sizes(seed + 0x10, i, n_lo=1000, n_hi=int(50000 * scale))
-            reqs.append(acdc.gen_svm(ns, 10 * ns, nnz_median=100, nnz_sigma=0.8,
-                                     w_star_nnz=max(10, ns // 20), lam=1e-3, seed=seed + 0x10 + i,
-                                     pinned=pinned))
+            inst = svs[int(rng.integers(len(svs)))]
+            reqs.append((inst, inst.lam, i + 1))
     arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
     return reqs, arrivals
 
@@ -264,29 +305,29 @@ def serve_sample(count, rate, seed=0xACDC0004, scale=0.25, pinned=True):
 def latency_summary(lat_s, span_s, conv, count):
     import numpy as np
     lat = np.array(lat_s) * 1e3
-    return {"solves_per_s": count / span_s, "p50_ms": float(np.percentile(lat, 50)),
+    return {"solves_per_s": count / span_s, "converged": int(conv),
+            "converged_per_s": conv / span_s, "p50_ms": float(np.percentile(lat, 50)),
             "p90_ms": float(np.percentile(lat, 90)), "p99_ms": float(np.percentile(lat, 99)),
-            "converged": int(conv), "span_s": span_s}
+            "span_s": span_s}
 
 
-def run_serving(ctx, count, rate, quantum=4):
+def serve_one_rate(ctx, pool, count, rate, quantum):
     """Continuous batching (acdc_server_*) against the plain path (one request at
     a time through acdc_batch_solve_path with plain = 1) on the same arrivals;
-    latency = finish - arrival, host monotonic clock."""
+    latency = finish - arrival on the host's monotonic clock."""
     import acdc
     import numpy as np
-    reqs, arr = serve_sample(count, rate)
-    out = {"workload": "serve_mix_70_30", "requests": count, "rate_per_s": rate, "quantum_rounds": quantum,
-           "request_buffers": "pinned host memory (both paths)",
-           "gap_target": 1e-6, "nnz": int(sum(x.nnz for x in reqs))}
+    reqs, arr = serve_sample(pool, count, rate)
+    out = {"rate_per_s": rate, "requests": count}
     srv = acdc.Server(ctx, memory_budget_bytes=120 << 30, max_slots=256, quantum_rounds=quantum,
-                      max_epochs=3000, use_shrinking=1)
+                      max_epochs=SERVE_MAX_EPOCHS, use_shrinking=1)
     start = time.monotonic()
     tickets, nxt = {}, 0
     while True:
         now = time.monotonic() - start
         while nxt < count and arr[nxt] <= now:
-            tickets[nxt] = srv.submit(reqs[nxt], gap_target=1e-6, seed=1)
+            inst, lam, seed = reqs[nxt]
+            tickets[nxt] = srv.submit(inst, lam=lam, gap_target=1e-6, seed=seed)
             nxt += 1
         pend = srv.step()
         if nxt >= count and pend == 0:
@@ -308,10 +349,11 @@ def run_serving(ctx, count, rate, quantum=4):
         now = time.monotonic() - start
         if now < arr[i]:
             time.sleep(arr[i] - now)
-        q = acdc.Problem(ctx, reqs[i])
-        res, _ = acdc.batch_solve_path(ctx, [q], np.array([[reqs[i].lam]]), gap_target=1e-6,
-                                       max_epochs=3000, refresh_every=1, autotune=1, plain=1,
-                                       want_x=True, use_shrinking=1)
+        inst, lam, seed = reqs[i]
+        q = acdc.Problem(ctx, inst, seed=seed)
+        res, _ = acdc.batch_solve_path(ctx, [q], np.array([[lam]]), gap_target=1e-6,
+                                       max_epochs=SERVE_MAX_EPOCHS, refresh_every=1, autotune=1,
+                                       plain=1, want_x=True, use_shrinking=1)
         q.close()
         t = time.monotonic() - start
         lat.append(t - arr[i])
@@ -319,6 +361,24 @@ def run_serving(ctx, count, rate, quantum=4):
         conv += res[0][0].converged
     out["plain"] = latency_summary(lat, max(fin) - arr[0], conv, count)
     out["speedup"] = out["server"]["solves_per_s"] / out["plain"]["solves_per_s"]
+    return out
+
+
+def run_serving(ctx, count, rates, quantum=4):
+    """The serving workload at each arrival rate of the sweep."""
+    pool = serve_pool()
+    out = {"workload": "serve_mix_70_30", "requests_per_rate": count, "quantum_rounds": quantum,
+           "gap_target": 1e-6, "request_buffers": "pinned host memory (both paths)",
+           "pool": {"lasso": len(pool[0]), "svm": len(pool[1]),
+                    "lasso_nnz": int(sum(x.nnz for x in pool[0])),
+                    "svm_nnz": int(sum(x.nnz for x in pool[1])),
+                    "svm_samples": [x.n for x in pool[1]]},
+           "sizes": "Lasso: the 512-instance mix's distribution unscaled; SVM: samples "
+                    "logU[1e3, 5e4], features scaled with them, median 450 entries per sample"}
+    out["sweep"] = [serve_one_rate(ctx, pool, count, r, quantum) for r in rates]
+    top = out["sweep"][-1]
+    out["rate_per_s"] = top["rate_per_s"]
+    out["speedup"] = top["speedup"]
     return out
 
 
@@ -888,7 +948,8 @@ def run_ours(args, w):
         batched = run_batched(ctx, args.batch_instances, args.batch_max_epochs, rank, world, dist,
                               dev)
     if rank == 0 and not is_svm(w) and args.serve_requests > 0:
-        serving = run_serving(ctx, args.serve_requests, args.serve_rate, args.serve_quantum)
+        rates = [args.serve_rate] if args.serve_rate > 0 else list(SERVE_RATES)
+        serving = run_serving(ctx, args.serve_requests, rates, args.serve_quantum)
     if is_svm(w):
         solver_keys = {"gap_target_absolute": w["gap"], "q_shrinking": 0, "lambda": w["lam"]}
     else:
