@@ -402,7 +402,9 @@ def run_svm_section(ctx, steps=10, warmup=2, cpu=True):
         import numpy as np
         runs.append(("minibatch_rel_1e-6", 1, 1e-6 * abs(float(np.load(f)["primal"]))))
     for key, mb, gap in runs:
-        ws = dict(w, minibatch=mb, gap=gap)
+        # the mini-batch form checks the gap every epoch (n / 1024 steps), as the
+        # reference's loop does; the asynchronous form every 5 epochs
+        ws = dict(w, minibatch=mb, gap=gap, refresh_every=1 if mb else 5)
         p = acdc.Problem(ctx, inst, settings_for(ws))
         res = []
         for i in range(warmup + steps):
@@ -550,15 +552,19 @@ def duplicate_classes(inst):
     return cls, sign
 
 
+def class_mass(cls, sign, x, idx):
+    """Signed mass of each class over the coordinates idx of x."""
+    mass = {}
+    for c, v in zip(cls[idx].tolist(), (sign[idx] * x[idx]).tolist()):
+        mass[c] = mass.get(c, 0.0) + v
+    return mass
+
+
 def class_support(cls, sign, x, idx=None):
     """Classes whose signed mass is nonzero."""
     import numpy as np
     idx = np.nonzero(x)[0] if idx is None else idx
-    vals = x[idx] if len(x) == len(cls) else x
-    mass = {}
-    for c, v in zip(cls[idx].tolist(), (sign[idx] * vals).tolist()):
-        mass[c] = mass.get(c, 0.0) + v
-    return {c for c, v in mass.items() if v != 0.0}
+    return {c for c, v in class_mass(cls, sign, x, idx).items() if v != 0.0}
 
 
 def host_objective(inst, x):
@@ -619,12 +625,20 @@ def oracle_error(workload, inst, x, primal):
         out["max_abs_x_in_difference"] = float(np.abs(np.concatenate([x[sym], xo[sym]])).max()) \
             if len(sym) else 0.0
         cls, sign = duplicate_classes(inst)
-        cs = class_support(cls, sign, x, sup)
-        co = class_support(cls, sign, xo, sup_o)
+        mg = class_mass(cls, sign, x, sup)
+        mo = class_mass(cls, sign, xo, sup_o)
+        cs = {c for c, v in mg.items() if v != 0.0}
+        co = {c for c, v in mo.items() if v != 0.0}
         out["class_support"] = len(cs)
         out["oracle_class_support"] = len(co)
         out["class_symmetric_difference"] = len(cs ^ co)
         out["support_match"] = cs == co
+        # the classes that differ: the solution's and the oracle's mass on each
+        # (for a column class, c - m is the column; for a one-entry class, c is the row)
+        out["class_differences"] = [
+            {"class": int(c), "column": int(c - inst.m) if c >= inst.m else None,
+             "row": int(c) if c < inst.m else None, "mass": mg.get(c, 0.0),
+             "oracle_mass": mo.get(c, 0.0)} for c in sorted(cs ^ co)[:10]]
         out["support_rule"] = ("same nonzero classes; one-entry columns at one row form one class "
                                "(the same column up to sign, so the split of their mass is not unique)")
     else:
