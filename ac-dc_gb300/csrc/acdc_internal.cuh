@@ -24,6 +24,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -237,6 +238,9 @@ struct acdc_ctx {
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   std::string last_error;
   int64_t live_problems = 0;  // problems (and servers) created on this context
+  // tau chosen by the measured autotuner per size class, and its probe count
+  std::map<uint64_t, int> tau_cache;
+  int64_t tune_probes = 0;
 };
 
 struct acdc_problem {

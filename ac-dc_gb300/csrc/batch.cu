@@ -21,9 +21,9 @@
 
 namespace {
 
-// ESO-aware choice of tau for one instance: the largest power of two whose
-// beta = 1 + (omega-1)(tau-1)/(n-1) stays at most beta_max, with at least 32
-// columns per concurrent update and no more than 1024 warps.
+// Closed-form choice of tau (batch option autotune = 2): the largest power of
+// two whose beta = 1 + (omega-1)(tau-1)/(n-1) stays at most beta_max, with at
+// least 32 columns per concurrent update and no more than 1024 warps.
 int autotune_tau(int64_t n, int64_t omega, double beta_max) {
   int best = 1;
   for (int tau = 1; tau <= 1024; tau *= 2) {
@@ -33,6 +33,103 @@ int autotune_tau(int64_t n, int64_t omega, double beta_max) {
     best = tau;
   }
   return best;
+}
+
+// Measured choice of tau for one instance.  Candidates: powers of two with
+// beta = 1 + (omega-1)(tau-1)/(n-1) at most 1.5, at least 32 columns per
+// update in flight, at most 1024.  Each candidate runs a probe launch of a
+// quarter epoch (at least 64 tau updates) timed with CUDA events; the probes
+// use the step constants of the largest candidate's beta, which is safe for
+// every smaller tau, and their updates are real progress of the solve.  A
+// coordinate step is scaled by 1/beta, so the time to a given gap goes as
+// beta(tau) / (updates per second at tau): the candidate with the smallest
+// ratio wins.  The choice is cached per size class (log2 of n and m, mean
+// column length) on the context, so a batch or a server pays the probes once
+// per class.
+uint64_t size_class(const acdc_problem* p) {
+  auto lg = [](int64_t v) {
+    uint64_t b = 0;
+    while (v > 1) {
+      v >>= 1;
+      ++b;
+    }
+    return b;
+  };
+  const uint64_t mean_len = (uint64_t)(p->d.nnz / std::max<int64_t>(1, p->d.n));
+  return (lg(p->d.n) << 40) | (lg(p->d.m) << 20) | std::min<uint64_t>(mean_len, 0xfffff) |
+         ((uint64_t)p->loss << 60);
+}
+
+int measured_tau(acdc_problem* p, int wpb_cap, int* tau_out) {
+  acdc_ctx* ctx = p->ctx;
+  const uint64_t key = size_class(p);
+  auto it = ctx->tau_cache.find(key);
+  if (it != ctx->tau_cache.end()) {
+    *tau_out = it->second;
+    return ACDC_OK;
+  }
+  const int64_t n = p->d.n;
+  std::vector<int> cand;
+  for (int tau = 1; tau <= 1024; tau *= 2) {
+    const double beta =
+        n > 1 ? 1.0 + ((double)p->omega - 1.0) * ((double)tau - 1.0) / ((double)n - 1.0) : 1.0;
+    if (beta > 1.5 || (int64_t)tau * 32 > std::max<int64_t>(32, n)) break;
+    cand.push_back(tau);
+  }
+  // step constants of the largest candidate's beta for every probe
+  acdc_settings s = p->s;
+  s.tau = cand.back();
+  s.sigma = 0;
+  int rc = acdc_problem_set_settings(p, &s);
+  if (rc) return rc;
+  double best_cost = 0;
+  int best = cand.front();
+  for (int tau : cand) {
+    const uint64_t count = std::max<uint64_t>((uint64_t)n / 4, 64u * (uint64_t)tau);
+    UpdateParams u{};
+    u.meta = p->d.meta;
+    u.vals = p->d.vals;
+    u.idx = p->d.idx;
+    u.r = p->d.r32;
+    u.active = p->d.active;
+    u.counters = p->d.counters;
+    u.x64 = p->d.x64;
+    u.r64 = p->d.r64;
+    u.x32 = p->d.x32;
+    u.n = n;
+    u.count = count;
+    u.seed = p->s.seed;
+    if (p->loss == ACDC_LOSS_SVM_DUAL) {
+      u.lambda_d = p->lambda * (double)n;
+      u.inv_lambda_n_d = 1.0 / (p->lambda * (double)n);
+    } else {
+      u.lambda_d = p->lambda;
+    }
+    u.li_scale = 1.0;
+    u.n_warps = tau;
+    u.loss = p->loss;
+    u.fp64 = p->fp64_mode ? 1 : 0;
+    u.sm_count = ctx->sm_count;
+    ACDC_CK(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+    ACDC_CK(ctx, launch_update(u, p->k_next, std::min(wpb_cap, tau), ctx->stream));
+    ACDC_CK(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+    ACDC_CK(ctx, cudaEventSynchronize(ctx->ev[1]));
+    float ms = 0;
+    ACDC_CK(ctx, cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
+    p->k_next += count;
+    p->updates_done += count;
+    const double beta =
+        n > 1 ? 1.0 + ((double)p->omega - 1.0) * ((double)tau - 1.0) / ((double)n - 1.0) : 1.0;
+    const double cost = beta * (double)std::max(ms, 1e-3f) / (double)count;
+    if (tau == cand.front() || cost < best_cost) {
+      best_cost = cost;
+      best = tau;
+    }
+  }
+  ctx->tau_cache[key] = best;
+  ctx->tune_probes += (int64_t)cand.size();
+  *tau_out = best;
+  return ACDC_OK;
 }
 
 // Evaluation blocks for one instance: enough to stream its entries and rows.
@@ -86,10 +183,16 @@ int prepare(acdc_problem* p, const SolveOpts& o, int wpb_cap) {
   s.shrinking_starting_iter = 1;
   s.active_passes = o.active_passes;
   s.tau_active = 0;
-  if (o.tau_override > 0)
+  if (o.tau_override > 0) {
     s.tau = o.tau_override;
-  else if (o.autotune)
+  } else if (o.autotune == 2) {
     s.tau = autotune_tau(p->d.n, p->omega, 1.3);
+  } else if (o.autotune) {
+    int tau = 1;
+    const int rc = measured_tau(p, wpb_cap, &tau);
+    if (rc) return rc;
+    s.tau = tau;
+  }
   s.warps_per_block = std::min(wpb_cap, s.tau);
   return acdc_problem_set_settings(p, &s);
 }

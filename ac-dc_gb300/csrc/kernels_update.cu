@@ -683,99 +683,99 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-// Adds lane 0's count of every warp of the block to *dst with one atomic.
-// Every thread of the block calls it.
-__device__ __forceinline__ void block_count(unsigned long long v, unsigned long long* dst) {
-  __shared__ unsigned long long part[kMaxWarps];
-  const int w = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) part[w] = v;
+// Threads per block of the mini-batch phases: one block per drawn sample,
+// each thread taking 4 entries of every 4 * kPhaseThreads (one 128-bit load of
+// values and one of row indices per round).
+constexpr int kPhaseThreads = 128;
+
+// Values and row indices of entries e..e+3 of a column (zero past len).
+__device__ __forceinline__ Chunk entries4(const UpdateParams& p, uint64_t start, uint32_t len,
+                                          uint32_t e) {
+  Chunk c;
+  if (e < len) {
+    c.v = __ldcs(reinterpret_cast<const float4*>(p.vals + start + e));
+    c.i = __ldcs(reinterpret_cast<const int4*>(p.idx + start + e));
+  } else {
+    c.v = make_float4(0.f, 0.f, 0.f, 0.f);
+    c.i = make_int4(0, 0, 0, 0);
+  }
+  return c;
+}
+
+// Phase 1: block i computes delta_i = clip((1 - y g) lambda n Li, -a, 1 - a),
+// g = x_i^T w, for the i-th coordinate of the step, from w as the step found
+// it (MulticoreSVMDualLoss.h:119-141); the block's partial sums meet in shared
+// memory.
+template <typename T>
+__global__ void __launch_bounds__(kPhaseThreads) k_sdca_phase1(UpdateParams p, const int32_t* S,
+                                                               int32_t tau, T* dout) {
+  __shared__ T part[kPhaseThreads / 32];
+  const int lane = threadIdx.x & 31;
+  const int32_t j = S[blockIdx.x];
+  const int4 mt = __ldg(p.meta + j);
+  const T* r = reinterpret_cast<const T*>(sizeof(T) == 8 ? (const void*)p.r64 : (const void*)p.r);
+  T xj = T(0);  // read with the entries, used after the reduction
+  if (threadIdx.x == 0) {
+    if constexpr (sizeof(T) == 8)
+      xj = __ldcg(p.x64 + j);
+    else
+      xj = __ldcg(p.x32 + j);
+  }
+  const uint64_t start = (uint64_t)(uint32_t)mt.x << 2;
+  const uint32_t len = (uint32_t)mt.y;
+  T acc = T(0);
+  for (uint32_t base = 0; base < len; base += 4u * kPhaseThreads) {
+    const uint32_t e = base + 4u * threadIdx.x;
+    const Chunk c = entries4(p, start, len, e);
+    acc += gather_dot_head<ACDC_LOSS_SVM_DUAL, T>(r, c, e, len);
+  }
+  acc = warp_sum(acc);
+  if (lane == 0) part[threadIdx.x >> 5] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
-    unsigned long long t = 0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += part[i];
-    if (t) atomicAdd(dst, t);
+    T g = T(0);
+#pragma unroll
+    for (int w = 0; w < kPhaseThreads / 32; ++w) g += part[w];
+    const T li = (T)__int_as_float(mt.z) * (T)p.li_scale;
+    const T y = li < T(0) ? T(-1) : T(1);
+    T delta = (T(1) - g * y) * (T)p.lambda_d * fabs(li);
+    if (delta < -xj)
+      delta = -xj;
+    else if (delta > T(1) - xj)
+      delta = T(1) - xj;
+    dout[blockIdx.x] = delta;
+    atomicAdd(p.counters + CNT_NNZ_READ, (unsigned long long)len);
   }
-  __syncthreads();
 }
 
-// Phase 1: warp i computes delta_i = clip((1 - y g) lambda n Li, -a, 1 - a),
-// g = x_i^T w, for the i-th coordinate of the step, from w as the step found
-// it (MulticoreSVMDualLoss.h:119-141).  Entries stream in chunks of 128 with
-// the update kernel's loads and gathers.
-template <typename T>
-__global__ void __launch_bounds__(256) k_sdca_phase1(UpdateParams p, const int32_t* S, int32_t tau,
-                                                     T* dout) {
-  const int lane = threadIdx.x & 31;
-  const int64_t wi = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const T* r = reinterpret_cast<const T*>(sizeof(T) == 8 ? (const void*)p.r64 : (const void*)p.r);
-  unsigned long long nread = 0;
-  if (wi < tau) {
-    const int32_t j = S[wi];
-    const int4 mt = __ldg(p.meta + j);
-    const uint64_t start = (uint64_t)(uint32_t)mt.x << 2;
-    const uint32_t len = (uint32_t)mt.y;
-    T acc = T(0);
-    for (uint32_t off = 0; off < len; off += 128u) {
-      const Chunk c = load_chunk(p, start, len, off, lane);
-      acc += gather_dot_head<ACDC_LOSS_SVM_DUAL, T>(r, c, off + 4u * (uint32_t)lane, len);
-    }
-    const T g = warp_sum(acc);
-    if (lane == 0) {
-      T xj;
-      if constexpr (sizeof(T) == 8)
-        xj = __ldcg(p.x64 + j);
-      else
-        xj = __ldcg(p.x32 + j);
-      const T li = (T)__int_as_float(mt.z) * (T)p.li_scale;
-      const T y = li < T(0) ? T(-1) : T(1);
-      T delta = (T(1) - g * y) * (T)p.lambda_d * fabs(li);
-      if (delta < -xj)
-        delta = -xj;
-      else if (delta > T(1) - xj)
-        delta = T(1) - xj;
-      dout[wi] = delta;
-      nread = len;
-    }
-  }
-  block_count(nread, p.counters + CNT_NNZ_READ);
-}
-
-// Phase 2: warp i applies delta_i: alpha_i += delta_i (the coordinates of a
-// step are distinct, so no other warp writes it) and w += delta_i y_i/(lambda n)
+// Phase 2: block i applies delta_i: alpha_i += delta_i (the coordinates of a
+// step are distinct, so no other block writes it) and w += delta_i y_i/(lambda n)
 // x_i with red.global.
 template <typename T>
-__global__ void __launch_bounds__(256) k_sdca_phase2(UpdateParams p, const int32_t* S, int32_t tau,
-                                                     const T* din) {
-  const int lane = threadIdx.x & 31;
-  const int64_t wi = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void __launch_bounds__(kPhaseThreads) k_sdca_phase2(UpdateParams p, const int32_t* S,
+                                                               int32_t tau, const T* din) {
+  const int32_t j = S[blockIdx.x];
+  const T d = din[blockIdx.x];
+  if (threadIdx.x == 0) atomicAdd(p.counters + CNT_UPDATES, 1ull);
+  if (d == T(0)) return;
   T* r = reinterpret_cast<T*>(sizeof(T) == 8 ? (void*)p.r64 : (void*)p.r);
-  unsigned long long nz = 0, nscat = 0;
-  if (wi < tau) {
-    const T d = din[wi];
-    if (d != T(0)) {
-      const int32_t j = S[wi];
-      const int4 mt = __ldg(p.meta + j);
-      const uint64_t start = (uint64_t)(uint32_t)mt.x << 2;
-      const uint32_t len = (uint32_t)mt.y;
-      const T y = __int_as_float(mt.z) < 0.f ? T(-1) : T(1);
-      const T coef = d * y * (T)p.inv_lambda_n_d;
-      for (uint32_t off = 0; off < len; off += 128u) {
-        const Chunk c = load_chunk(p, start, len, off, lane);
-        scatter<T>(r, c, coef, off + 4u * (uint32_t)lane < len);
-      }
-      if (lane == 0) {
-        if constexpr (sizeof(T) == 8)
-          p.x64[j] = p.x64[j] + d;
-        else
-          p.x32[j] = p.x32[j] + d;
-        nz = 1;
-        nscat = len;
-      }
-    }
+  const int4 mt = __ldg(p.meta + j);
+  const uint64_t start = (uint64_t)(uint32_t)mt.x << 2;
+  const uint32_t len = (uint32_t)mt.y;
+  const T y = __int_as_float(mt.z) < 0.f ? T(-1) : T(1);
+  const T coef = d * y * (T)p.inv_lambda_n_d;
+  for (uint32_t base = 0; base < len; base += 4u * kPhaseThreads) {
+    const uint32_t e = base + 4u * threadIdx.x;
+    if (e < len) scatter_head<T>(r, entries4(p, start, len, e), coef, e, len);
   }
-  block_count(nz, p.counters + CNT_NONZERO);
-  block_count(nscat, p.counters + CNT_NNZ_SCATTERED);
-  block_count(wi < tau && lane == 0 ? 1ull : 0ull, p.counters + CNT_UPDATES);
+  if (threadIdx.x == 0) {
+    if constexpr (sizeof(T) == 8)
+      p.x64[j] = p.x64[j] + d;
+    else
+      p.x32[j] = p.x32[j] + d;
+    atomicAdd(p.counters + CNT_NONZERO, 1ull);
+    atomicAdd(p.counters + CNT_NNZ_SCATTERED, (unsigned long long)len);
+  }
 }
 
 // The sampler's uniform draw with a 64-bit result, so the stream can be checked
@@ -887,13 +887,8 @@ cudaError_t launch_tau_nice(uint64_t seed, int64_t n, int32_t tau, int32_t steps
 cudaError_t launch_minibatch_step(const UpdateParams& p, const int32_t* S, int32_t tau, void* delta,
                                   cudaStream_t st) {
   if (tau <= 0) return cudaSuccess;
-  // tau warps, spread over the SMs
-  int wpb = kMaxWarps;
-  if (p.sm_count > 0) {
-    const int spread = (tau + p.sm_count - 1) / p.sm_count;
-    if (spread < wpb) wpb = spread > 0 ? spread : 1;
-  }
-  const dim3 grid((unsigned)((tau + wpb - 1) / wpb)), block(wpb * 32);
+  // one block per drawn sample
+  const dim3 grid((unsigned)tau), block(kPhaseThreads);
   if (p.fp64) {
     k_sdca_phase1<double><<<grid, block, 0, st>>>(p, S, tau, static_cast<double*>(delta));
     k_sdca_phase2<double><<<grid, block, 0, st>>>(p, S, tau, static_cast<const double*>(delta));

@@ -376,7 +376,11 @@ typedef struct acdc_batch_options {
   int32_t max_epochs;       /* per lambda                                         */
   double gap_target;        /* per lambda, relative gap                           */
   int32_t refresh_every;    /* epochs between gap checks                          */
-  int32_t autotune;         /* 1: choose tau / CTA packing per instance           */
+  int32_t autotune;         /* 1: tau per instance by timed probe launches of
+                               each candidate (powers of two with ESO beta <= 1.5):
+                               the smallest beta / measured updates per second,
+                               cached per size class on the context; 2: the
+                               closed-form rule (largest tau with beta <= 1.3)   */
   int32_t tau_override;     /* > 0: fixed tau for every instance                  */
   int32_t plain;            /* 1: solve one instance per launch sequence (baseline) */
   int32_t use_shrinking;    /* 1: q-shrinking (q = 0.9) for Lasso instances, from
