@@ -8,7 +8,7 @@ values scaled to unit columns; x* has 10,000 entries +-1; b = A x* + N(0, 0.01^2
 lambda = 0.05 ||A^T b||_inf.  Seeded synthetic data (no dataset is shipped).
 PCDM with tau = 4096, FP32 bulk with FP64 refresh and duality gap every 5 epochs,
 q-shrinking (q = 0.9) after 5 epochs with 1024 updates in flight on the active
-set, 100 active-set passes between refreshes, screened evaluations and the
+set, 50 active-set passes between refreshes, screened evaluations and the
 hot-set tier (threshold 0.1); target relative duality gap 1e-6.
 
 A step is one solve from x = 0 to the target gap with the matrix resident in
@@ -39,7 +39,7 @@ WORKLOADS = {
     "lasso_m1e6_n1e7_zipf": dict(m=1_000_000, n=10_000_000, nnz_mode=1, zipf_s=1.5, nnz_min=1,
                                  nnz_max=2000, nnz_mean=20.0, n_star=10_000, noise_sigma=0.01,
                                  lambda_frac=0.05, seed=0xACDC0001, tau=4096, refresh_every=5,
-                                 gap=1e-6, max_epochs=12000, tau_active=1024, active_passes=100),
+                                 gap=1e-6, max_epochs=12000, tau_active=1024, active_passes=50),
     # the same generator at 3e5 x 3e6 (about 6e7 nonzeros): small enough for full
     # profiler captures
     "lasso_m3e5_n3e6_zipf": dict(m=300_000, n=3_000_000, nnz_mode=1, zipf_s=1.5, nnz_min=1,
@@ -113,7 +113,7 @@ def parse_args():
                     help="rounds per server step (acdc_server_options.quantum_epochs)")
     ap.add_argument("--active-passes", type=int, default=0,
                     help="passes over the active set per bulk while q-shrinking (Lasso; "
-                         "0 = the workload's own, 100 for the 1e6 x 1e7 Lasso)")
+                         "0 = the workload's own, 50 for the 1e6 x 1e7 Lasso)")
     ap.add_argument("--probe-launches", action="store_true",
                     help="profiling aid: run one uniform-draw update launch (refresh_every "
                          "epochs) and one active-set launch (active_passes |A|/q updates) on "
