@@ -36,7 +36,7 @@ int autotune_tau(int64_t n, int64_t omega, double beta_max) {
 }
 
 // Measured choice of tau for one instance.  Candidates: powers of two with
-// beta = 1 + (omega-1)(tau-1)/(n-1) at most 1.5, at least 32 columns per
+// beta = 1 + (omega-1)(tau-1)/(n-1) at most kTuneBetaMax, at least 32 columns per
 // update in flight, at most 1024.  Each candidate runs a probe launch of a
 // quarter epoch (at least 64 tau updates) timed with CUDA events; the probes
 // use the step constants of the largest candidate's beta, which is safe for
@@ -60,6 +60,12 @@ uint64_t size_class(const acdc_problem* p) {
          ((uint64_t)p->loss << 60);
 }
 
+// Largest ESO beta among the tuner's candidates: a step scaled by 1/beta is
+// always safe, and an instance whose rows are dense (beta grows fast with tau,
+// underdetermined Lasso) can gain more from updates in flight than it loses to
+// the smaller steps; the measurement decides.
+constexpr double kTuneBetaMax = 4.0;
+
 int measured_tau(acdc_problem* p, int wpb_cap, int* tau_out) {
   acdc_ctx* ctx = p->ctx;
   const uint64_t key = size_class(p);
@@ -73,7 +79,7 @@ int measured_tau(acdc_problem* p, int wpb_cap, int* tau_out) {
   for (int tau = 1; tau <= 1024; tau *= 2) {
     const double beta =
         n > 1 ? 1.0 + ((double)p->omega - 1.0) * ((double)tau - 1.0) / ((double)n - 1.0) : 1.0;
-    if (beta > 1.5 || (int64_t)tau * 32 > std::max<int64_t>(32, n)) break;
+    if (beta > kTuneBetaMax || (int64_t)tau * 32 > std::max<int64_t>(32, n)) break;
     cand.push_back(tau);
   }
   // step constants of the largest candidate's beta for every probe

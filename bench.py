@@ -99,7 +99,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--max-epochs", type=int, default=0,
                     help="cap each solve (profiling runs; the line then reports converged=false)")
-    ap.add_argument("--batch-instances", type=int, default=32,
+    ap.add_argument("--batch-instances", type=int, default=64,
                     help="instances of the batched lambda-path sample (0 = skip)")
     ap.add_argument("--batch-max-epochs", type=int, default=200)
     ap.add_argument("--svm-steps", type=int, default=10,

@@ -377,7 +377,7 @@ typedef struct acdc_batch_options {
   double gap_target;        /* per lambda, relative gap                           */
   int32_t refresh_every;    /* epochs between gap checks                          */
   int32_t autotune;         /* 1: tau per instance by timed probe launches of
-                               each candidate (powers of two with ESO beta <= 1.5):
+                               each candidate (powers of two with ESO beta <= 4):
                                the smallest beta / measured updates per second,
                                cached per size class on the context; 2: the
                                closed-form rule (largest tau with beta <= 1.3)   */
