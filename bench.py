@@ -105,7 +105,7 @@ def parse_args():
     ap.add_argument("--svm-steps", type=int, default=10,
                     help="solves of the SVM-dual workload reported under the line's svm key "
                          "(0 = skip)")
-    ap.add_argument("--serve-requests", type=int, default=64,
+    ap.add_argument("--serve-requests", type=int, default=256,
                     help="requests of the serving sample at each rate (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=0.0,
                     help="one arrival rate per second (0 = the sweep 50..2000)")
@@ -364,9 +364,23 @@ def serve_one_rate(ctx, pool, count, rate, quantum):
     return out
 
 
+def warm_tuner(ctx, pool):
+    """Untimed: one capped solve of every pool instance, so that the autotuner's
+    per-size-class choice of tau is cached on the context before either path
+    is timed (both paths then use the same cached choices)."""
+    import acdc
+    import numpy as np
+    for inst in pool[0] + pool[1]:
+        q = acdc.Problem(ctx, inst, seed=1)
+        acdc.batch_solve_path(ctx, [q], np.array([[inst.lam]]), gap_target=1e-6, max_epochs=1,
+                              refresh_every=1, autotune=1, plain=1, use_shrinking=1)
+        q.close()
+
+
 def run_serving(ctx, count, rates, quantum=4):
     """The serving workload at each arrival rate of the sweep."""
     pool = serve_pool()
+    warm_tuner(ctx, pool)
     out = {"workload": "serve_mix_70_30", "requests_per_rate": count, "quantum_rounds": quantum,
            "gap_target": 1e-6, "request_buffers": "pinned host memory (both paths)",
            "pool": {"lasso": len(pool[0]), "svm": len(pool[1]),
