@@ -214,6 +214,7 @@ def run_batched(ctx, count, max_epochs, rank=0, world=1, dist=None, dev=None):
            "nnz": int(round(sum_over_ranks(dist, sum(x.nnz for x in insts), dev))),
            "shards": [len(x) for x in shards],
            "scaling": "strong: the sample's instances dealt to the ranks by footprint"}
+    warm_tuner(ctx, (insts, []))
     conv_mask = {}
     for plain in (0, 1):
         probs = [acdc.Problem(ctx, x) for x in insts]
