@@ -99,3 +99,25 @@ def test_batch_mixes_losses_and_sizes(ctx):
                                     5e-4, seed=1, target=1e-10)
     assert abs(res[3][3].eval.primal - ev["primal"]) <= 1e-5 * abs(ev["primal"])
     assert np.all((xs[3] >= 0) & (xs[3] <= 1))
+
+
+def test_batched_path_at_mix_sizes_matches_oracle(ctx):
+    """Three instances of the 512-instance distribution itself (unscaled: 9,292,
+    85,384 and 63,997 columns, 5..50 entries per column), the first four lambdas
+    of the path, against the oracle's warm-started FP64 path (working-set
+    solver to relative gap 1e-10): objective within 1e-6 relative per lambda,
+    identical support at the end."""
+    sizes = [acdc.mix_sizes(0xACDC0003, i) for i in (0, 2, 4)]
+    insts = [acdc.gen_lasso(m, n, nnz_mode=acdc.NNZ_UNIFORM, nnz_min=5, nnz_max=50,
+                            n_star=max(1, n // 100), lambda_frac=1.0, seed=0xACDC0003 + i)
+             for (m, n), i in zip(sizes, (0, 2, 4))]
+    rb, xb = solve_batch(ctx, insts, plain=0, use_shrinking=1)
+    for i, inst in enumerate(insts):
+        x = None
+        for k, lam in enumerate(path_for(inst)):
+            x, r, ev, sw, ch = oracle.lasso_solve_ws(inst.m, inst.n, inst.col_ptr, inst.row_idx,
+                                                     inst.vals, inst.rhs, lam, target=1e-10,
+                                                     rel=True, x0=x)
+            assert rb[i][k].converged, (i, k, rb[i][k].eval.rel_gap)
+            assert abs(rb[i][k].eval.primal - ev["primal"]) <= 1e-6 * abs(ev["primal"]), (i, k)
+        assert set(np.nonzero(xb[i])[0]) == set(np.nonzero(x)[0]), i
