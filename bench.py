@@ -966,6 +966,11 @@ def run_ours(args, w):
                                   "gap %.3g after %d epochs, so its time-to-gap exceeds %.1f s "
                                   "(measured lower bound)" % (run["gap"], run["epochs"],
                                                               run["seconds"])))}
+        # the serial engine (the reference's -t 1) on the same workload, capped
+        serial = cpu_time_to_gap(inst, 1, w["gap"], rel, args.cpu_budget / 2)
+        cpu["serial"] = {"value": serial["seconds"], "cores": 1, "lower_bound": not serial["reached"],
+                         "gap_reached": serial["gap"], "epochs": serial["epochs"],
+                         "updates_per_s": serial["updates_per_s"]}
         cpu["config0_time_to_gap"] = cpu_config0(threads)
 
     p.close()
