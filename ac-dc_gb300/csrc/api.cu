@@ -86,8 +86,8 @@ const char* settings_fault(const acdc_settings* s) {
   if (s->polish_stall_epochs < 0) return "polish_stall_epochs";
   if (s->hot_polish_sweeps < 0) return "hot_polish_sweeps";
   if (s->polish_active_passes < 0) return "polish_active_passes";
-  if (s->lanes_per_update != 0 && s->lanes_per_update != -1 && s->lanes_per_update != 8 &&
-      s->lanes_per_update != 16 && s->lanes_per_update != 32)
+  if (s->lanes_per_update != 0 && s->lanes_per_update != -1 && s->lanes_per_update != 1 &&
+      s->lanes_per_update != 8 && s->lanes_per_update != 16 && s->lanes_per_update != 32)
     return "lanes_per_update";
   if (s->minibatch != 0 && (s->minibatch != 1 || s->loss != ACDC_LOSS_SVM_DUAL)) return "minibatch";
   return nullptr;
@@ -289,13 +289,14 @@ EvalParams eval_params(acdc_problem* p, bool build_active) {
   return e;
 }
 
-// Lanes per update of the problem's update launches (settings.lanes_per_update;
-// 0 = the one-warp ring kernel, the fastest per update in the measurements of
-// both the uniform and the active-set launches at the default tau).
+// Update kernel of the problem's launches (settings.lanes_per_update): 0 = the
+// lean one-warp kernel for the q-shrinking launches and the ring kernel for the
+// others, 1 = the lean kernel for all, -1 = the ring kernel for all, 8/16/32 =
+// the grouped kernel.
 int32_t lanes_for(const acdc_problem* p) {
   const int32_t l = p->s.lanes_per_update;
-  if (l == 8 || l == 16 || l == 32) return l;
-  return -1;
+  if (l == 1 || l == -1 || l == 8 || l == 16 || l == 32) return l;
+  return 0;
 }
 
 UpdateParams update_params(acdc_problem* p, uint64_t count, bool shrink) {

@@ -185,6 +185,42 @@ __device__ __forceinline__ void scatter(T* r, const Chunk& c, T coef, bool live)
   if (c.v.w != 0.f) atomicAdd(r + c.i.w, coef * (T)c.v.w);
 }
 
+// The step of one coordinate from g = a_j^T r (for the logistic loss the
+// gather already applied sigma), x_j and li = Li times the launch's step scale:
+// delta for x_j, and coef, the factor of a_j in the residual update
+// r += coef a_j.
+template <int LOSS, typename T>
+__device__ __forceinline__ T step_delta(T g, T xj, T li, T lam, T inv_ln, T& coef) {
+  T delta;
+  if (LOSS == ACDC_LOSS_L1_SQUARE) {
+    const T z = xj - li * g;
+    T a = fabs(z) - lam * li;
+    a = a < T(0) ? T(0) : a;
+    const T xn = z > T(0) ? a : (z < T(0) ? -a : T(0));
+    delta = xn - xj;
+    coef = delta;
+  } else if (LOSS == ACDC_LOSS_L2_SQUARE) {
+    // MulticoreL2SquareRegSquareLoss.h:56-78: delta = -Li (a_j^T r + lambda x_j)
+    delta = -li * (g + lam * xj);
+    coef = delta;
+  } else if (LOSS == ACDC_LOSS_LOGISTIC) {
+    // MulticoreL2SquareRegLogisticLoss.h:88-115 with the label folded into the
+    // values: gradient -sum_i v_i sigma(r_i) + lambda x_j, half step, and
+    // r_i += -delta v_i.
+    delta = -li * (lam * xj - g) / T(2);
+    coef = -delta;
+  } else {
+    const T y = li < T(0) ? T(-1) : T(1);
+    delta = (T(1) - g * y) * lam * fabs(li);
+    if (delta < -xj)
+      delta = -xj;
+    else if (delta > T(1) - xj)
+      delta = T(1) - xj;
+    coef = delta * y * inv_ln;
+  }
+  return delta;
+}
+
 __device__ __forceinline__ void issue_meta(WarpRing& w, const UpdateParams& p, int32_t j, int slot,
                                            int lane) {
   if (lane == 0) cp_async16(&w.meta[slot], p.meta + j);
@@ -296,33 +332,8 @@ __device__ __forceinline__ void pcdm_update_body(const UpdateParams& p, uint64_t
       const T g = column_sum<T>(acc, len);
 
       const T li = (T)__int_as_float(mt.z) * (cj < 0 ? li_scale_hot : li_scale);
-      T delta, coef;
-      if (LOSS == ACDC_LOSS_L1_SQUARE) {
-        const T z = xj - li * g;
-        T a = fabs(z) - lam * li;
-        a = a < T(0) ? T(0) : a;
-        const T xn = z > T(0) ? a : (z < T(0) ? -a : T(0));
-        delta = xn - xj;
-        coef = delta;
-      } else if (LOSS == ACDC_LOSS_L2_SQUARE) {
-        // MulticoreL2SquareRegSquareLoss.h:56-78: delta = -Li (a_j^T r + lambda x_j)
-        delta = -li * (g + lam * xj);
-        coef = delta;
-      } else if (LOSS == ACDC_LOSS_LOGISTIC) {
-        // MulticoreL2SquareRegLogisticLoss.h:88-115 with the label folded into the
-        // values: gradient -sum_i v_i sigma(r_i) + lambda x_j, half step, and
-        // r_i += -delta v_i.
-        delta = -li * (lam * xj - g) / T(2);
-        coef = -delta;
-      } else {
-        const T y = li < T(0) ? T(-1) : T(1);
-        delta = (T(1) - g * y) * lam * fabs(li);
-        if (delta < -xj)
-          delta = -xj;
-        else if (delta > T(1) - xj)
-          delta = T(1) - xj;
-        coef = delta * y * inv_ln;
-      }
+      T coef;
+      const T delta = step_delta<LOSS, T>(g, xj, li, lam, inv_ln, coef);
       chunk_read += len;
       // lanes with entries (and lane 0, which writes x_j) hold the column's sum
       const bool holds = e0 < len || lane == 0 || len > 16u;
@@ -361,6 +372,177 @@ template <int LOSS, typename T>
 __global__ void __launch_bounds__(256, 4) k_pcdm_update(UpdateParams p, uint64_t k_base) {
   __shared__ WarpRing rings[kMaxWarps];
   pcdm_update_body<LOSS, T>(p, k_base, blockIdx.x, rings);
+}
+
+// ---- lean update kernel: a record table per chunk and the entry ring only ----
+//
+// The same updates, draws and arithmetic as k_pcdm_update (at one update in
+// flight the two give identical iterates), with a shorter path per update for
+// the q-shrinking launches, whose draws mostly land on short columns (the
+// active set of a Zipf-length Lasso is about 94% columns of at most 4
+// entries):
+// - the records of all updates of a chunk are copied into a table when the
+//   chunk is drawn, and word 3 of each copy (0 in the layout) is overwritten
+//   with the drawn coordinate and its hot-tier bit, so an update reads its
+//   record, coordinate and tier with one 16-byte shared load, and there is no
+//   record ring;
+// - lane l copies, and later reads, only pieces l of the entry ring (entries
+//   4l..4l+3), so an update waits on its own lane's copies with
+//   cp.async.wait_group and needs no __syncwarp;
+// - a column of at most 4 entries sits in lane 0 and needs no shuffles;
+// - the work counter of the next chunk is taken while this one runs.
+constexpr int kLeanWarps = 8;  // warps per block
+
+struct WarpLean {
+  float4 vals[kDS][32];
+  int4 idx[kDS][32];
+  int4 rec[kChunk];  // {start4, len, Li, drawn coordinate | hot bit} per update
+};
+static_assert(sizeof(WarpLean) * kLeanWarps <= 48 * 1024, "static shared memory of a block");
+
+__device__ __forceinline__ void lean_issue(WarpLean& w, const UpdateParams& p, const int4 mt,
+                                           int dslot, int lane) {
+  const uint32_t len = (uint32_t)mt.y;
+  if (4u * (uint32_t)lane < len) {
+    const uint64_t src = ((uint64_t)(uint32_t)mt.x << 2) + 4u * (uint32_t)lane;
+    cp_async16(&w.vals[dslot][lane], p.vals + src);
+    cp_async16(&w.idx[dslot][lane], p.idx + src);
+  }
+}
+
+// Sum over the lanes holding a column of len entries (lane l: entries
+// 4l..4l+3): nothing to add for at most 4 entries (lane 0 alone), two steps up
+// to 16 (lanes 0..3), five beyond.
+template <typename T>
+__device__ __forceinline__ T lean_sum(T v, uint32_t len) {
+  if (len > 4u) {
+    v += __shfl_xor_sync(ACDC_FULL_MASK, v, 1);
+    v += __shfl_xor_sync(ACDC_FULL_MASK, v, 2);
+    if (len > 16u) {
+      v += __shfl_xor_sync(ACDC_FULL_MASK, v, 4);
+      v += __shfl_xor_sync(ACDC_FULL_MASK, v, 8);
+      v += __shfl_xor_sync(ACDC_FULL_MASK, v, 16);
+    }
+  }
+  return v;
+}
+
+template <int LOSS, typename T>
+__device__ __forceinline__ void pcdm_lean_body(const UpdateParams& p, uint64_t k_base,
+                                               int64_t rank, WarpLean* lean) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gwarp = (rank * blockDim.x + threadIdx.x) >> 5;
+  if (gwarp >= p.n_warps) return;
+  WarpLean& w = lean[threadIdx.x >> 5];
+  T* r = reinterpret_cast<T*>(sizeof(T) == 8 ? (void*)p.r64 : (void*)p.r);
+  T* x = reinterpret_cast<T*>(sizeof(T) == 8 ? (void*)p.x64 : (void*)p.x32);
+  unsigned long long* work = p.counters + CNT_WORK;
+  const int32_t active_cnt =
+      p.shrink_q32 ? (int32_t)min(p.counters[CNT_ACTIVE], (unsigned long long)p.n) : 0;
+  const int32_t hot_cnt =
+      p.hot_q32 ? (int32_t)min(p.counters[CNT_HOT], (unsigned long long)p.n) : 0;
+  const T lam = (T)p.lambda_d;
+  const T inv_ln = (T)p.inv_lambda_n_d;
+  const T li_scale = (T)p.li_scale;
+  const T li_scale_hot = (T)p.li_scale_hot;
+  const uint32_t e0 = 4u * (uint32_t)lane;
+  unsigned long long n_upd = 0, n_nz = 0, n_read = 0, n_scat = 0;
+
+  unsigned long long next = 0;
+  if (lane == 0) next = atomicAdd(work, (unsigned long long)kChunk);
+  for (;;) {
+    const unsigned long long base = __shfl_sync(ACDC_FULL_MASK, next, 0);
+    if (base >= p.count) break;
+    if (lane == 0) next = atomicAdd(work, (unsigned long long)kChunk);
+    const int cnt = (int)min((unsigned long long)kChunk, p.count - base);
+
+    // Draw the chunk and copy its records; then stamp each copy with its draw.
+    int32_t cj[kChunk / 32];
+#pragma unroll
+    for (int q = 0; q < kChunk / 32; ++q) {
+      const int s = 32 * q + lane;
+      cj[q] = s < cnt ? draw_coord(p, k_base + base + (uint64_t)s, active_cnt, hot_cnt) : 0;
+      if (s < cnt) cp_async16(&w.rec[s], p.meta + (cj[q] & kCoordMask));
+    }
+    cp_async_commit();
+    cp_async_wait<0>();
+#pragma unroll
+    for (int q = 0; q < kChunk / 32; ++q) {
+      const int s = 32 * q + lane;
+      if (s < cnt) w.rec[s].w = cj[q];
+    }
+    __syncwarp();
+    // Entries of updates 0..D-1, one commit group per update, so that
+    // wait_group(D-1) at update s means "this lane's copies of update s landed".
+#pragma unroll
+    for (int t = 0; t < kD; ++t) {
+      if (t < cnt) lean_issue(w, p, w.rec[t], t, lane);
+      cp_async_commit();
+    }
+
+    uint32_t chunk_read = 0, chunk_nz = 0, chunk_scat = 0;
+    for (int s = 0; s < cnt; ++s) {
+      const int ds = s & (kDS - 1);
+      cp_async_wait<kD - 1>();
+      const int4 mt = w.rec[s];
+      const int32_t j = mt.w & kCoordMask;
+      const T xj = __ldcg(x + j);
+      const uint32_t len = (uint32_t)mt.y;
+      Chunk c0;  // lanes past the column hold stale pieces, never used below
+      c0.v = w.vals[ds][lane];
+      c0.i = w.idx[ds][lane];
+      // Refill: entries of update s + D into the slot update s - 1 used (this
+      // lane's own pieces).  Issued before the gathers: the other order made the
+      // active-set launches 11% slower in the measurements.
+      if (s + kD < cnt) lean_issue(w, p, w.rec[s + kD], (s + kD) & (kDS - 1), lane);
+      cp_async_commit();
+      T acc = gather_dot_head<LOSS, T>(r, c0, e0, len);
+      const uint64_t start = (uint64_t)(uint32_t)mt.x << 2;
+      if (len > 128u) {
+        Chunk a = load_chunk(p, start, len, 128u, lane);
+        for (uint32_t off = 128u; off < len; off += 128u) {
+          Chunk b = load_chunk(p, start, len, off + 128u, lane);
+          acc += gather_dot<LOSS, T>(r, a, off + e0 < len);
+          a = b;
+        }
+      }
+      const T g = lean_sum<T>(acc, len);
+      const T li = (T)__int_as_float(mt.z) * (mt.w < 0 ? li_scale_hot : li_scale);
+      T coef;
+      const T delta = step_delta<LOSS, T>(g, xj, li, lam, inv_ln, coef);
+      chunk_read += len;
+      // the lanes holding entries (and lane 0, which writes x_j) hold the sum
+      const bool holds = e0 < len || lane == 0 || len > 16u;
+      if (holds && delta != T(0)) {
+        chunk_nz++;
+        chunk_scat += len;
+        scatter_head<T>(r, c0, coef, e0, len);
+        for (uint32_t off = 128u; off < len; off += 128u) {
+          Chunk a = load_chunk(p, start, len, off, lane);
+          scatter<T>(r, a, coef, off + e0 < len);
+        }
+        if (lane == 0) atomicAdd(x + j, delta);
+      }
+    }
+    cp_async_wait<0>();
+    __syncwarp();  // every lane is done with this chunk's record table
+    n_upd += (unsigned)cnt;
+    n_read += chunk_read;
+    n_nz += chunk_nz;
+    n_scat += chunk_scat;
+  }
+  if (lane == 0) {
+    atomicAdd(p.counters + CNT_UPDATES, n_upd);
+    atomicAdd(p.counters + CNT_NONZERO, n_nz);
+    atomicAdd(p.counters + CNT_NNZ_READ, n_read);
+    atomicAdd(p.counters + CNT_NNZ_SCATTERED, n_scat);
+  }
+}
+
+template <int LOSS, typename T>
+__global__ void __launch_bounds__(256, 4) k_pcdm_update_lean(UpdateParams p, uint64_t k_base) {
+  __shared__ WarpLean lean[kLeanWarps];
+  pcdm_lean_body<LOSS, T>(p, k_base, blockIdx.x, lean);
 }
 
 // ---- grouped update kernel: G lanes per update, 32/G updates per warp ----
@@ -511,29 +693,8 @@ __device__ __forceinline__ void pcdm_update_grouped_body(const UpdateParams& p, 
       const T g = group_sum<G, T>(acc, ACDC_FULL_MASK);
       if (live) {
         const T li = (T)__int_as_float(mt.z) * (cj < 0 ? li_scale_hot : li_scale);
-        T delta, coef;
-        if (LOSS == ACDC_LOSS_L1_SQUARE) {
-          const T z = xj - li * g;
-          T a = fabs(z) - lam * li;
-          a = a < T(0) ? T(0) : a;
-          const T xn = z > T(0) ? a : (z < T(0) ? -a : T(0));
-          delta = xn - xj;
-          coef = delta;
-        } else if (LOSS == ACDC_LOSS_L2_SQUARE) {
-          delta = -li * (g + lam * xj);
-          coef = delta;
-        } else if (LOSS == ACDC_LOSS_LOGISTIC) {
-          delta = -li * (lam * xj - g) / T(2);
-          coef = -delta;
-        } else {
-          const T y = li < T(0) ? T(-1) : T(1);
-          delta = (T(1) - g * y) * lam * fabs(li);
-          if (delta < -xj)
-            delta = -xj;
-          else if (delta > T(1) - xj)
-            delta = T(1) - xj;
-          coef = delta * y * inv_ln;
-        }
+        T coef;
+        const T delta = step_delta<LOSS, T>(g, xj, li, lam, inv_ln, coef);
         n_read += len;
         if (delta != T(0)) {
           n_nz++;
@@ -587,9 +748,24 @@ __global__ void __launch_bounds__(256) k_pcdm_update_grouped(UpdateParams p, uin
 
 // Batched launch: each block serves one slot at rank blockIdx.x - first block
 // of that slot, with the body of that slot's loss and precision, so one launch
-// covers Lasso and SVM slots in FP32 and FP64 alike.
+// covers Lasso and SVM slots in FP32 and FP64 alike.  The kernel choice is the
+// single-problem launch's: the lean body for a slot's q-shrinking rounds, the
+// ring body for the others.
+union BatchShared {
+  WarpRing ring[kMaxWarps];
+  WarpLean lean[kLeanWarps];
+};
+
+template <int LOSS, typename T>
+__device__ __forceinline__ void batch_body(const UpdateParams& p, int64_t rank, BatchShared& sm) {
+  if (p.lanes == 1 || (p.lanes == 0 && p.shrink_q32 != 0))
+    pcdm_lean_body<LOSS, T>(p, p.k_base, rank, sm.lean);
+  else
+    pcdm_update_body<LOSS, T>(p, p.k_base, rank, sm.ring);
+}
+
 __global__ void __launch_bounds__(256, 4) k_pcdm_update_batch(BatchDev b) {
-  __shared__ WarpRing rings[kMaxWarps];
+  __shared__ BatchShared sm;
   const int s = b.ublk_slot[blockIdx.x];
   if (!b.ctl[s].live) return;
   const UpdateParams p = b.up[s];
@@ -597,14 +773,14 @@ __global__ void __launch_bounds__(256, 4) k_pcdm_update_batch(BatchDev b) {
   const int64_t rank = (int64_t)blockIdx.x - b.ublk_first[s];
   if (p.loss == ACDC_LOSS_SVM_DUAL) {
     if (p.fp64)
-      pcdm_update_body<ACDC_LOSS_SVM_DUAL, double>(p, p.k_base, rank, rings);
+      batch_body<ACDC_LOSS_SVM_DUAL, double>(p, rank, sm);
     else
-      pcdm_update_body<ACDC_LOSS_SVM_DUAL, float>(p, p.k_base, rank, rings);
+      batch_body<ACDC_LOSS_SVM_DUAL, float>(p, rank, sm);
   } else {
     if (p.fp64)
-      pcdm_update_body<ACDC_LOSS_L1_SQUARE, double>(p, p.k_base, rank, rings);
+      batch_body<ACDC_LOSS_L1_SQUARE, double>(p, rank, sm);
     else
-      pcdm_update_body<ACDC_LOSS_L1_SQUARE, float>(p, p.k_base, rank, rings);
+      batch_body<ACDC_LOSS_L1_SQUARE, float>(p, rank, sm);
   }
 }
 
@@ -852,6 +1028,28 @@ cudaError_t launch_update(const UpdateParams& p, uint64_t k_base, int warps_per_
   }
   const int blocks = (p.n_warps + warps_per_block - 1) / warps_per_block;
   dim3 grid(blocks), block(warps_per_block * 32);
+  // the lean kernel for every launch (lanes 1) or for the q-shrinking ones (0)
+  const bool lean = p.lanes == 1 || (p.lanes == 0 && p.shrink_q32 != 0);
+  if (lean) {
+#define ACDC_LAUNCH(L, T) k_pcdm_update_lean<L, T><<<grid, block, 0, st>>>(p, k_base)
+    if (p.fp64) {
+      switch (p.loss) {
+        case ACDC_LOSS_L1_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L1_SQUARE, double); break;
+        case ACDC_LOSS_L2_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L2_SQUARE, double); break;
+        case ACDC_LOSS_SVM_DUAL: ACDC_LAUNCH(ACDC_LOSS_SVM_DUAL, double); break;
+        default: ACDC_LAUNCH(ACDC_LOSS_LOGISTIC, double); break;
+      }
+    } else {
+      switch (p.loss) {
+        case ACDC_LOSS_L1_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L1_SQUARE, float); break;
+        case ACDC_LOSS_L2_SQUARE: ACDC_LAUNCH(ACDC_LOSS_L2_SQUARE, float); break;
+        case ACDC_LOSS_SVM_DUAL: ACDC_LAUNCH(ACDC_LOSS_SVM_DUAL, float); break;
+        default: ACDC_LAUNCH(ACDC_LOSS_LOGISTIC, float); break;
+      }
+    }
+#undef ACDC_LAUNCH
+    return cudaGetLastError();
+  }
 #define ACDC_LAUNCH(L, T) k_pcdm_update<L, T><<<grid, block, 0, st>>>(p, k_base)
   if (p.fp64) {
     switch (p.loss) {
@@ -906,7 +1104,8 @@ cudaError_t launch_batch_update(const BatchDev& b, int update_blocks, cudaStream
   return cudaGetLastError();
 }
 
-// Four 37 KB blocks per SM need the shared-memory side of the L1 carveout.
+// Four 37 KB (ring) or 48 KB (lean) blocks per SM need the shared-memory side
+// of the L1 carveout.
 cudaError_t update_kernels_init() {
   const int carve = cudaSharedmemCarveoutMaxShared;
   const cudaFuncAttribute a = cudaFuncAttributePreferredSharedMemoryCarveout;
@@ -922,6 +1121,17 @@ cudaError_t update_kernels_init() {
   ACDC_CARVE(ACDC_LOSS_LOGISTIC, float);
   ACDC_CARVE(ACDC_LOSS_LOGISTIC, double);
 #undef ACDC_CARVE
+#define ACDC_CARVE_LEAN(L, T) \
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_lean<L, T>, a, carve)
+  ACDC_CARVE_LEAN(ACDC_LOSS_L1_SQUARE, float);
+  ACDC_CARVE_LEAN(ACDC_LOSS_L1_SQUARE, double);
+  ACDC_CARVE_LEAN(ACDC_LOSS_SVM_DUAL, float);
+  ACDC_CARVE_LEAN(ACDC_LOSS_SVM_DUAL, double);
+  ACDC_CARVE_LEAN(ACDC_LOSS_L2_SQUARE, float);
+  ACDC_CARVE_LEAN(ACDC_LOSS_L2_SQUARE, double);
+  ACDC_CARVE_LEAN(ACDC_LOSS_LOGISTIC, float);
+  ACDC_CARVE_LEAN(ACDC_LOSS_LOGISTIC, double);
+#undef ACDC_CARVE_LEAN
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcdm_update_batch, a, carve);
   return e;
 }

@@ -89,9 +89,10 @@ def parse_args():
     ap.add_argument("--workload", default="lasso_m1e6_n1e7_zipf", choices=sorted(WORKLOADS))
     ap.add_argument("--e2e-steps", type=int, default=3,
                     help="end-to-end solves through the C-ABI from host buffers (mean reported)")
-    ap.add_argument("--lanes", type=int, default=0, choices=[-1, 0, 8, 16, 32],
-                    help="lanes per update of the update kernel (settings.lanes_per_update: "
-                         "8 or 32 grouped, -1 the one-warp ring kernel, 0 by column length)")
+    ap.add_argument("--lanes", type=int, default=0, choices=[-1, 0, 1, 8, 16, 32],
+                    help="update kernel (settings.lanes_per_update): 0 the lean kernel for "
+                         "the q-shrinking launches, 1 the lean kernel for all, -1 the ring "
+                         "kernel for all, 8/16/32 the grouped kernel")
     ap.add_argument("--cpu-budget", type=float, default=20.0,
                     help="seconds of computation for the CPU baseline run of the workload")
     ap.add_argument("--ref-step-seconds", type=float, default=0,
@@ -114,6 +115,8 @@ def parse_args():
     ap.add_argument("--active-passes", type=int, default=0,
                     help="passes over the active set per bulk while q-shrinking (Lasso; "
                          "0 = the workload's own, 50 for the 1e6 x 1e7 Lasso)")
+    ap.add_argument("--probe-repeat", type=int, default=1,
+                    help="--probe-launches: active-set launches to time (the first is counted)")
     ap.add_argument("--probe-launches", action="store_true",
                     help="profiling aid: run one uniform-draw update launch (refresh_every "
                          "epochs) and one active-set launch (active_passes |A|/q updates) on "
@@ -148,8 +151,12 @@ def probe_launches(w):
     p.reset_stats()
     t2 = timed(count)
     second = p.stats()
-    print(json.dumps({"workload": w.get("name"), "uniform_launch": dict(first, host_ms=t1),
-                      "active_launch": dict(second, active_set=ev["active"], host_ms=t2)}),
+    # further active-set launches of the same size (same active set) for timing
+    more = [timed(count) for _ in range(max(0, w.get("probe_repeat", 1) - 1))]
+    print(json.dumps({"workload": w.get("name"), "lanes_per_update": s.lanes_per_update,
+                      "uniform_launch": dict(first, host_ms=t1),
+                      "active_launch": dict(second, active_set=ev["active"], host_ms=t2,
+                                            repeat_host_ms=more)}),
           flush=True)
     p.close()
     ctx.close()
@@ -1047,6 +1054,7 @@ def main():
     if args.active_passes > 0 and "active_passes" in w:
         w["active_passes"] = args.active_passes
     w["lanes"] = args.lanes
+    w["probe_repeat"] = args.probe_repeat
     if args.probe_launches:
         return probe_launches(w)
     if args.max_epochs > 0:

@@ -121,13 +121,22 @@ typedef struct acdc_settings {
                                      this many passes (|A|/q updates each) of the
                                      q-shrinking draws in FP64, tau_active in
                                      flight; 0 = none, default 2                  */
-  int32_t lanes_per_update;       /* update kernel: 0 (default) or -1 = one warp
-                                     per update with a shared-memory copy ring;
-                                     8, 16 or 32 = the grouped kernel, in which
-                                     that many lanes perform one update (32/lanes
-                                     updates per warp) with records and entries
-                                     prefetched into registers.  tau counts the
-                                     updates in flight either way.                */
+  int32_t lanes_per_update;       /* update kernel, one warp per update unless
+                                     8/16/32: -1 = the ring kernel (records and
+                                     entries staged through shared-memory copy
+                                     rings) for every launch; 1 = the lean kernel
+                                     (the records of a chunk of draws staged at
+                                     once, an entry ring, columns of at most 4
+                                     entries summed in one lane) for every
+                                     launch; 0 (default) = the lean kernel for
+                                     the q-shrinking launches, the ring kernel
+                                     for the others; 8, 16 or 32 = the grouped
+                                     kernel, in which that many lanes perform one
+                                     update (32/lanes updates per warp) with
+                                     records and entries prefetched into
+                                     registers.  The iterates do not depend on
+                                     the kernel at one update in flight; tau
+                                     counts the updates in flight in every case. */
   int32_t minibatch;              /* SVM dual (loss 2) only, 1: synchronous
                                      mini-batch SDCA as the reference's mini-batch
                                      loop runs it (cpp/src/experiments/mSDCA.cpp:

@@ -92,8 +92,10 @@ def test_settings_check_refuses_every_out_of_range_field():
             ("gap_target", 1e300), ("tau_active", 0), ("max_epochs", 0), ("warps_per_block", 8),
             ("precision", acdc.PREC_FP64), ("hot_threshold", 0.0), ("polish_stall_epochs", 0),
             ("hot_polish_sweeps", 0), ("polish_active_passes", 0), ("active_passes", -3),
-            ("shrinking_starting_iter", -1)]
-    bad = [("loss", -1), ("loss", 4), ("tau", 0), ("tau_active", -1), ("warps_per_block", 0),
+            ("shrinking_starting_iter", -1), ("lanes_per_update", -1), ("lanes_per_update", 1),
+            ("lanes_per_update", 8), ("lanes_per_update", 16), ("lanes_per_update", 32)]
+    bad = [("lanes_per_update", 2), ("lanes_per_update", 4), ("lanes_per_update", 64),
+           ("lanes_per_update", -2), ("loss", -1), ("loss", 4), ("tau", 0), ("tau_active", -1), ("warps_per_block", 0),
            ("warps_per_block", 9), ("refresh_every", 0), ("max_epochs", -1), ("sigma", nan),
            ("sigma", inf), ("sigma", -inf), ("gap_target", -1e-9), ("gap_target", nan),
            ("shrinking_probability", -0.1), ("shrinking_probability", 1.01),
