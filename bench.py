@@ -124,6 +124,45 @@ def parse_args():
     return ap.parse_args()
 
 
+def update_kernel_label(s, w):
+    """The update kernels a solve with settings s launches."""
+    if is_svm(w) and s.minibatch:
+        return "k_sdca_phase1 + k_sdca_phase2 (synchronous mini-batch steps)"
+    lanes = s.lanes_per_update
+    if lanes in (8, 16, 32):
+        return "k_pcdm_update_grouped<%d>" % lanes
+    if lanes == 1:
+        return "k_pcdm_update_lean"
+    if lanes == 0 and s.use_shrinking:
+        return "k_pcdm_update (uniform bulks) + k_pcdm_update_lean (q-shrinking bulks)"
+    return "k_pcdm_update"
+
+
+def bulk_phases(traces, s):
+    """Update bulks of the timed solves by kind (from the solve traces): uniform
+    draws, q-shrinking draws, and either in FP64.  Per kind: bulks, updates,
+    event-timed milliseconds, updates/s, the updates in flight (tau or
+    tau_active) and the microseconds one update takes at that many in flight
+    (in flight x time / updates)."""
+    out = {}
+    for rows in traces:
+        prev = 0
+        for row in rows[1:]:
+            n = row["updates"] - prev
+            prev = row["updates"]
+            kind = ("active" if row["shrink"] else "uniform") + ("_fp64" if row["fp64"] else "")
+            k = out.setdefault(kind, {"bulks": 0, "updates": 0, "ms": 0.0})
+            k["bulks"] += 1
+            k["updates"] += n
+            k["ms"] += row["update_ms"]
+    for kind, k in out.items():
+        fly = s.tau_active if kind.startswith("active") and s.tau_active > 0 else s.tau
+        k["in_flight"] = fly
+        k["updates_per_s"] = k["updates"] / (k["ms"] * 1e-3) if k["ms"] > 0 else None
+        k["us_per_update_in_flight"] = (fly * k["ms"] * 1e3 / k["updates"]) if k["updates"] else None
+    return out
+
+
 def probe_launches(w):
     """Two update launches of known size for a profiler capture: a uniform bulk
     from x = 0, then (after a full evaluation built the active set) one bulk of
@@ -857,10 +896,13 @@ def run_ours(args, w):
     p = acdc.Problem(ctx, inst, s)
     info = p.info()
 
+    traces = []
+
     def one_solve():
         p.reset()
         p.reset_stats()
-        r = p.solve()
+        r, rows = p.solve_traced(cap=100000)
+        traces.append(rows)
         return r
 
     for _ in range(args.warmup):
@@ -869,6 +911,7 @@ def run_ours(args, w):
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
+    del traces[:]
     clocks = ClockSampler(local)
     clocks.start()
     t0 = time.perf_counter()
@@ -917,9 +960,10 @@ def run_ours(args, w):
                    traffic_rec["active_dram_bytes_per_update"] * (updates - uniform)) / launches
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if peak else None, "traffic": traffic,
-                "peak_source": peak_src, "kernel": "k_pcdm_update",
+                "peak_source": peak_src, "kernel": update_kernel_label(s, w),
                 "alg_bytes_per_launch": alg_bytes / launches if launches else 0,
-                "avg_launch_ms": upd_ms / launches if launches else 0}
+                "avg_launch_ms": upd_ms / launches if launches else 0,
+                "phases": bulk_phases(traces, s)}
 
     if is_svm(w):
         k_full, k_scr = KERNELS_PER_EVAL_SVM, 0
