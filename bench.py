@@ -277,12 +277,18 @@ def run_batched(ctx, count, max_epochs, rank=0, world=1, dist=None, dev=None):
             q.close()
         key = "plain" if plain else "batched"
         conv_mask[key] = [[bool(r.converged) for r in row] for row in res]
+        # tau per instance: the measured autotuner's choice (cached per size class)
+        taus = {}
+        for row in res:
+            if len(row):
+                taus[int(row[0].tau)] = taus.get(int(row[0].tau), 0) + 1
         conv = sum(r.converged for row in res for r in row)
         conv = int(round(sum_over_ranks(dist, conv, dev)))
         out[key] = {"seconds": dt, "all_solves_per_s": count * 16 / dt, "converged": conv,
                     "converged_per_s": conv / dt,
                     "converged_per_lambda": [sum(row[k] for row in conv_mask[key])
-                                             for k in range(16)]}
+                                             for k in range(16)],
+                    "tau_chosen": {str(t): c for t, c in sorted(taus.items())}}
     # the metric: solves that reached the gap in both paths, per second of each
     both = sum(a and b for ra, rb in zip(conv_mask["batched"], conv_mask["plain"])
                for a, b in zip(ra, rb))
