@@ -1064,6 +1064,15 @@ def run_ours(args, w):
                        "precision": "fp32 bulk; fp64 refresh, gap and hot-column polish",
                        "updates": int(updates), "update_launches": int(launches),
                        "updates_per_s": updates / (upd_ms * 1e-3) if upd_ms > 0 else None,
+                       # where a solve's device time goes: update bulks, evaluations
+                       # (both event-timed), and the rest (polish launches, host
+                       # turnarounds between a bulk and the next)
+                       "time_split_ms": {
+                           "solve": statistics.mean(dev_ms),
+                           "update_bulks": statistics.mean(r.stats.update_ms for r in results),
+                           "evaluations": statistics.mean(r.stats.eval_ms for r in results),
+                           "evaluation_count": statistics.mean(r.stats.eval_launches
+                                                               for r in results)},
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (no flush)", "omega": info.omega,
                        "beta": info.sigma, "epochs": epochs,
