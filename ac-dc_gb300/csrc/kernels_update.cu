@@ -30,6 +30,13 @@
 // Precision: T = float keeps x and r in FP32 (the bulk mode); T = double keeps
 // x and r in FP64 arrays (the polish mode).  Matrix
 // values are FP32 in both.
+//
+// Kernels of this file: k_pcdm_update (the ring kernel above, for uniform
+// bulks), k_pcdm_update_lean (the same updates with a per-chunk record table,
+// for the q-shrinking bulks), k_pcdm_update_grouped (8, 16 or 32 lanes per
+// update, a setting), k_pcdm_update_batch (one launch over the slots of a
+// batch, with the ring or lean body per slot), and the synchronous mini-batch
+// SDCA kernels (k_tau_nice, k_sdca_phase1, k_sdca_phase2).
 #include "acdc_internal.cuh"
 
 namespace {
